@@ -1,0 +1,227 @@
+/*
+ * hora_gb300.h -- C ABI of the GB300-native zone-graph engine (libhora_gb300.so).
+ *
+ * This is the drop-in boundary for HORA's zone-graph hot path: the frontier successor pipeline,
+ * the passed-store subsumption probe and the backward greatest-fixpoint sweep. Every entry point
+ * takes plain pointers and sizes, returns an integer status (never throws across the ABI) and
+ * leaves a message for hora_gb_last_error() on failure.
+ *
+ * Reference interfaces each entry point stands in for (file:line within horaverify/PTCTCL):
+ *   hora_gb_reachable_net      bool reachable_net(const Network&, const NetTarget&, Backend,
+ *                              ReachStats*)                         include/hora/reachability.hpp:61-62
+ *   hora_gb_deadlock_reachable bool deadlock_reachable(const Network&, Backend, ReachStats*,
+ *                              const std::atomic<bool>* cancel)     include/hora/liveness.hpp:144-146
+ *   hora_gb_leads_to           bool leads_to_clocks / leads_to_otf(const Network&, const DiscPred& p,
+ *                              const DiscPred& q, GfpStats*)        include/hora/liveness.hpp:120-124
+ *   hora_gb_expand             NetGpuExpander::expand(...)          include/hora/gpu/network.hpp:52-58
+ *   hora_gb_batch_run          no reference counterpart (the reference runs one query at a time);
+ *                              same verdict contract as the three entry points above, per instance
+ *   hora_gb_server_*           no reference counterpart (continuous-batching request loop)
+ *
+ * Network encoding. A network of timed automata is passed flattened (hora_net_desc). It carries
+ * exactly what include/hora/network.hpp's Network/NProc/NEdge/Location hold for the fast path
+ * (clock guards, `var OP const` integer guards, clock resets, `var := const` updates, binary and
+ * broadcast channels, urgent/committed locations, location invariants). General-expression guards
+ * and updates (NEdge::gen_guard / gen_update) are not representable; networks that need them are
+ * out of scope for this engine, as they are for the reference's GPU encoder
+ * (include/hora/gpu/encode.hpp:36-44).
+ *
+ * Clock constraints are triples (i, j, raw) meaning x_i - x_j <| bound with raw = (bound << 1) | weak,
+ * clock 0 the constant-zero reference clock, exactly the HDBM encoding the reference uses
+ * (src/metal/netengine_metal.mm:76-100).
+ */
+#ifndef HORA_GB300_H
+#define HORA_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HORA_GB_ABI_VERSION 1
+
+/* ---- status codes ------------------------------------------------------------------------- */
+enum {
+  HORA_OK = 0,
+  HORA_E_INVALID = 1,        /* malformed descriptor or argument */
+  HORA_E_NOT_SUPPORTED = 2,  /* network outside the engine's scope (diagonal constraints, more than
+                                16 clocks, discrete key wider than 63 bits); the caller keeps its
+                                own engine, as the reference does when make_net_gpu_cuda returns
+                                nullptr (src/reachability/engine.cpp:1557-1561) */
+  HORA_E_CUDA = 3,           /* a CUDA runtime call failed; message in hora_gb_last_error() */
+  HORA_E_OVERFLOW = 4,       /* a fixed-capacity device structure overflowed (verdict unusable) */
+  HORA_E_TIMEOUT = 5,        /* a bounded device-side wait gave up (verdict unusable) */
+  HORA_E_BUDGET = 6,         /* request rejected: device-memory budget exceeded */
+  HORA_E_NOMEM = 7,          /* device allocation failed */
+  HORA_E_CANCELLED = 8,      /* cancelled through the cancel flag between BFS levels */
+  HORA_E_NO_DEVICE = 9       /* no CUDA device visible */
+};
+
+/* Backend selector, same values and meaning as `enum class Backend { Seq, Omp, Cuda, Metal }`
+ * (include/hora/reach.hpp:21). This library implements HORA_BACKEND_CUDA only; passing another
+ * value returns HORA_E_NOT_SUPPORTED so that the caller keeps its own CPU engine. */
+enum { HORA_BACKEND_SEQ = 0, HORA_BACKEND_OMP = 1, HORA_BACKEND_CUDA = 2, HORA_BACKEND_METAL = 3 };
+
+/* Integer-atom operators, the order of `enum class IntOp { Eq, Ne, Lt, Le, Gt, Ge }`
+ * (include/hora/network.hpp:23). */
+enum { HORA_IOP_EQ = 0, HORA_IOP_NE = 1, HORA_IOP_LT = 2, HORA_IOP_LE = 3, HORA_IOP_GT = 4, HORA_IOP_GE = 5 };
+
+/* Channel flags and location flags. */
+enum { HORA_CHAN_BROADCAST = 1, HORA_CHAN_URGENT = 2 };
+enum { HORA_LOC_URGENT = 1, HORA_LOC_COMMITTED = 2 };
+
+/* Flattened network. Locations are numbered process-major: process p's location l has global id
+ * loc_base(p) + l, where loc_base(p) = sum of proc_nlocs[0..p). Edges are grouped by process
+ * (edge_proc non-decreasing); within a process, edge order is NProc::edges order, which fixes the
+ * successor emission order (src/liveness/operators.cpp:55-206). */
+typedef struct hora_net_desc {
+  int32_t nclocks;              /* clocks, not counting the reference clock; DBM dim = nclocks+1 */
+  int32_t nprocs;
+  int32_t nints;
+  int32_t nchans;
+  const int32_t* chan_flags;    /* [nchans] HORA_CHAN_* bits */
+  const int32_t* int_lo;        /* [nints] declared range and initial value */
+  const int32_t* int_hi;
+  const int32_t* int_init;
+  const int32_t* proc_nlocs;    /* [nprocs] */
+  const int32_t* proc_init;     /* [nprocs] initial location, local index */
+  const int32_t* loc_flags;     /* [total locations] HORA_LOC_* bits */
+  const int32_t* loc_inv_off;   /* [total locations + 1] invariant constraints, offsets into cons */
+  int32_t nedges;
+  const int32_t* edge_proc;     /* [nedges] */
+  const int32_t* edge_src;      /* [nedges] local source location */
+  const int32_t* edge_tgt;      /* [nedges] local target location */
+  const int32_t* edge_chan;     /* [nedges] channel id or -1 */
+  const int32_t* edge_dir;      /* [nedges] +1 send (a!), -1 receive (a?), 0 none */
+  const int32_t* edge_guard_off;  /* [nedges+1] clock guard, offsets into cons */
+  const int32_t* edge_iguard_off; /* [nedges+1] integer guard, offsets into iatoms (triples) */
+  const int32_t* edge_reset_off;  /* [nedges+1] clock resets, offsets into resets */
+  const int32_t* edge_iupd_off;   /* [nedges+1] integer updates, offsets into iupds (pairs) */
+  const int32_t* cons;          /* constraint triples (i, j, raw) */
+  const int32_t* iatoms;        /* integer atom triples (var, op, val) */
+  const int32_t* resets;        /* clock indices in 1..nclocks */
+  const int32_t* iupds;         /* update pairs (var, val) */
+} hora_net_desc;
+
+/* A conjunction of location, integer and clock atoms: NetTarget (include/hora/network.hpp:152-165)
+ * for reachability, and DiscPred's plain conjunction (include/hora/predicate.hpp:39-84) for the
+ * two sides of a leads-to. */
+typedef struct hora_pred_desc {
+  int32_t nloc;
+  const int32_t* loc_req;       /* pairs (proc, local location) */
+  int32_t nint;
+  const int32_t* int_cond;      /* triples (var, op, val) */
+  int32_t nclk;
+  const int32_t* clk_cond;      /* triples (i, j, raw) */
+  int32_t never;                /* 1: the literal `false` (NetTarget::never) */
+} hora_pred_desc;
+
+/* Query kinds for the batched and serving entry points. */
+enum {
+  HORA_Q_REACH = 0,     /* E<> target  (A[] not target is its negation) */
+  HORA_Q_DEADLOCK = 1,  /* is a deadlocked state reachable?  (A[] not deadlock is its negation) */
+  HORA_Q_LEADSTO = 2    /* p --> q */
+};
+
+typedef struct hora_query_desc {
+  int32_t kind;
+  hora_pred_desc p;             /* target for HORA_Q_REACH; p for HORA_Q_LEADSTO */
+  hora_pred_desc q;             /* q for HORA_Q_LEADSTO */
+} hora_query_desc;
+
+/* Counters, a superset of ReachStats (include/hora/reach.hpp:10-19) and the GfpStats fields the
+ * leads-to route reports (include/hora/liveness.hpp:57-77). */
+typedef struct hora_stats {
+  uint64_t explored;     /* frontier states expanded, summed over BFS levels (ReachStats::explored) */
+  uint64_t generated;    /* non-empty successor zones generated (ReachStats::generated) */
+  uint64_t expanded;     /* same as explored for the forward routes */
+  uint64_t stored;       /* live zones in the passed store at the end */
+  uint64_t keys;         /* distinct discrete states in the passed store */
+  uint64_t levels;       /* BFS levels run */
+  uint64_t probes;       /* stored zones read by the subsumption probe (algorithmic bytes) */
+  uint64_t pre_calls;    /* exact_predecessor evaluations in the backward sweep */
+  uint64_t gfp_iters;    /* sweeps of the backward fixpoint */
+  uint64_t kernel_launches;
+  double   seconds;      /* wall time of the call */
+  double   device_seconds; /* time on the device, CUDA events around the level loop */
+  int32_t  extrapolating; /* 1 if the adaptive switch to Extra_LU+ fired */
+  int32_t  status;       /* HORA_OK or an error code for this query */
+} hora_stats;
+
+/* ---- errors and device ---------------------------------------------------------------------- */
+
+/* Thread-local text of the last failure (empty string when none). */
+const char* hora_gb_last_error(void);
+/* ABI version compiled into the library. */
+int32_t hora_gb_abi_version(void);
+/* Number of visible CUDA devices (0 when none); returns a status. */
+int32_t hora_gb_device_count(int32_t* count);
+
+/* ---- single-query entry points ---------------------------------------------------------------- */
+
+/* E<> target. On HORA_OK, *result = 1 iff a symbolic state matching target is reachable. */
+int32_t hora_gb_reachable_net(const hora_net_desc* net, const hora_pred_desc* target, int32_t backend,
+                              hora_stats* stats, int32_t* result);
+
+/* Is a state with a deadlocked valuation reachable?  A[] not deadlock holds iff *result == 0.
+ * `cancel` may be null; when non-null it is polled between BFS levels and a non-zero value ends the
+ * search with HORA_E_CANCELLED. */
+int32_t hora_gb_deadlock_reachable(const hora_net_desc* net, int32_t backend, hora_stats* stats,
+                                   const volatile int32_t* cancel, int32_t* result);
+
+/* p --> q. On HORA_OK, *result = 1 iff the property holds. */
+int32_t hora_gb_leads_to(const hora_net_desc* net, const hora_pred_desc* p, const hora_pred_desc* q,
+                         int32_t backend, hora_stats* stats, int32_t* result);
+
+/* Successor pipeline on host buffers, for differential testing against a CPU implementation.
+ * Inputs: n source states (locs[n*nprocs], ints[n*nints], zones[n*dim*dim] canonical, non-empty),
+ * the per-clock bounds L, U [dim] used by Extra_LU+, the query clock mask qmask [dim] (1 = the
+ * active-clock reduction must keep that clock) and emode (0 none, 1 Extra_LU+).
+ * Outputs, at most `cap` successors in (source, emission order): out_src[k] source index,
+ * out_ord[k] emission ordinal within its source, out_locs, out_ints, out_zones. *out_n receives the
+ * successor count; when it exceeds cap only the first cap are written and HORA_E_OVERFLOW is
+ * returned. */
+int32_t hora_gb_expand(const hora_net_desc* net, int32_t n, const int32_t* locs, const int32_t* ints,
+                       const int32_t* zones, const int32_t* L, const int32_t* U, const uint8_t* qmask,
+                       int32_t emode, int64_t cap, int32_t* out_src, int32_t* out_ord,
+                       int32_t* out_locs, int32_t* out_ints, int32_t* out_zones, int64_t* out_n);
+
+/* Deadlock predicate on host buffers (state_has_deadlock, src/reachability/deadlock.cpp:74-270):
+ * out[k] = 1 iff state k contains a deadlocked valuation. */
+int32_t hora_gb_has_deadlock(const hora_net_desc* net, int32_t n, const int32_t* locs,
+                             const int32_t* ints, const int32_t* zones, int32_t* out);
+
+/* ---- batched form ----------------------------------------------------------------------------- */
+
+/* Run n independent (network, query) instances together on the device. verdicts[k] receives the
+ * result in the single-query convention of the query's kind (reach: reachable; deadlock: deadlock
+ * reachable; leads-to: holds); stats (may be null) one record per instance. Returns HORA_OK when
+ * every instance ran; per-instance failures are reported in stats[k].status and verdicts[k] = -1. */
+int32_t hora_gb_batch_run(int32_t n, const hora_net_desc* nets, const hora_query_desc* queries,
+                          int32_t* verdicts, hora_stats* stats);
+
+/* ---- serving form ------------------------------------------------------------------------------ */
+
+typedef struct hora_server hora_server;
+
+/* budget_bytes: device memory the passed/waiting stores of admitted requests may hold together;
+ * max_inflight: instances interleaved on the device at once. */
+int32_t hora_gb_server_create(uint64_t budget_bytes, int32_t max_inflight, hora_server** out);
+/* Queue a request; the descriptors are copied. *ticket identifies it. A request whose own store
+ * estimate exceeds the whole budget is rejected with HORA_E_BUDGET. */
+int32_t hora_gb_server_submit(hora_server* s, const hora_net_desc* net, const hora_query_desc* q,
+                              int64_t* ticket);
+/* Advance the device by one interleaved step over every admitted request, admitting queued ones as
+ * slots and budget free up. *active receives the number still queued or running. */
+int32_t hora_gb_server_step(hora_server* s, int32_t* active);
+/* Fetch a finished request: *done = 1 and verdict/stats filled once it has finished. */
+int32_t hora_gb_server_poll(hora_server* s, int64_t ticket, int32_t* done, int32_t* verdict,
+                            hora_stats* stats);
+int32_t hora_gb_server_destroy(hora_server* s);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HORA_GB300_H */

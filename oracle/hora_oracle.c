@@ -1,0 +1,1231 @@
+/*
+ * hora_oracle.c -- CPU oracle for the zone-graph hot path.  TEST INFRASTRUCTURE ONLY.
+ *
+ * See hora_oracle.h for what this is restating and how it is pinned. Each function cites the
+ * reference file:line it follows. Everything is single-threaded, integer-exact C11.
+ */
+#include "hora_oracle.h"
+
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+
+/* ============================================================================================
+ * Raw bounds: (value << 1) | weak, kInf = 1<<30 (src/metal/netengine_metal.mm:76-100)
+ * ============================================================================================ */
+static inline int32_t r_le(int32_t v) { return (int32_t)((uint32_t)v << 1) | 1; }
+static inline int32_t r_lt(int32_t v) { return (int32_t)((uint32_t)v << 1); }
+static inline int32_t r_bound(int32_t r) { return r >> 1; }
+static inline int r_strict(int32_t r) { return (r & 1) == 0; }
+static inline int32_t r_add(int32_t a, int32_t b) {
+  if (a >= ORC_INF || b >= ORC_INF) return ORC_INF;
+  int32_t v = r_bound(a) + r_bound(b);
+  return (!r_strict(a) && !r_strict(b)) ? r_le(v) : r_lt(v);
+}
+static inline int32_t r_negate(int32_t r) {  /* complement of x_i-x_j <| v, as x_j-x_i <| -v */
+  int32_t v = r_bound(r);
+  return r_strict(r) ? r_le(-v) : r_lt(-v);
+}
+static inline int32_t imax(int32_t a, int32_t b) { return a > b ? a : b; }
+
+/* ============================================================================================
+ * DBM primitives (netengine_metal.mm:101-124, 225-238; engine_metal.mm:80-93)
+ * ============================================================================================ */
+void orc_dbm_init(int32_t* d, int32_t dim) {
+  for (int i = 0; i < dim * dim; ++i) d[i] = ORC_ZERO_LE;
+}
+int32_t orc_dbm_empty(const int32_t* d, int32_t dim) {
+  for (int i = 0; i < dim; ++i) if (d[i * dim + i] < ORC_ZERO_LE) return 1;
+  return 0;
+}
+void orc_dbm_close(int32_t* d, int32_t dim) {
+  for (int k = 0; k < dim; ++k)
+    for (int i = 0; i < dim; ++i) {
+      int32_t ik = d[i * dim + k];
+      if (ik >= ORC_INF) continue;
+      for (int j = 0; j < dim; ++j) {
+        int32_t s = r_add(ik, d[k * dim + j]);
+        if (s < d[i * dim + j]) d[i * dim + j] = s;
+      }
+    }
+}
+/* Incremental closure after tightening x_a - x_b to `raw` (netengine_metal.mm:110-124). */
+int32_t orc_dbm_constrain(int32_t* d, int32_t dim, int32_t a, int32_t b, int32_t raw) {
+  if (raw >= d[a * dim + b]) return !orc_dbm_empty(d, dim);
+  d[a * dim + b] = raw;
+  for (int i = 0; i < dim; ++i) {
+    int32_t via = r_add(d[i * dim + a], raw);
+    if (via < d[i * dim + b]) d[i * dim + b] = via;
+  }
+  for (int i = 0; i < dim; ++i) {
+    int32_t ib = d[i * dim + b];
+    if (ib >= ORC_INF) continue;
+    for (int k = 0; k < dim; ++k) {
+      int32_t via = r_add(ib, d[b * dim + k]);
+      if (via < d[i * dim + k]) d[i * dim + k] = via;
+    }
+  }
+  return !orc_dbm_empty(d, dim);
+}
+void orc_dbm_reset(int32_t* d, int32_t dim, int32_t k) {
+  for (int j = 0; j < dim; ++j) { d[k * dim + j] = d[0 * dim + j]; d[j * dim + k] = d[j * dim + 0]; }
+  d[k * dim + k] = ORC_ZERO_LE;
+}
+void orc_dbm_delay(int32_t* d, int32_t dim) {
+  for (int i = 1; i < dim; ++i) d[i * dim + 0] = ORC_INF;
+}
+/* Time predecessor (HDBM dbm_down, used by exact_predecessor src/liveness/operators.cpp:278-303
+ * and state_has_deadlock src/reachability/deadlock.cpp:244): every lower bound relaxes to the
+ * tightest bound any clock difference still imposes, and never below zero. */
+void orc_dbm_down(int32_t* d, int32_t dim) {
+  for (int j = 1; j < dim; ++j) {
+    int32_t m = ORC_ZERO_LE;
+    for (int i = 1; i < dim; ++i) if (d[i * dim + j] < m) m = d[i * dim + j];
+    d[0 * dim + j] = m;
+  }
+}
+/* Existentially quantify clock k (HDBM dbm_free): k becomes any value >= 0. */
+void orc_dbm_free(int32_t* d, int32_t dim, int32_t k) {
+  for (int i = 0; i < dim; ++i) {
+    if (i == k) continue;
+    d[k * dim + i] = ORC_INF;
+    d[i * dim + k] = d[i * dim + 0];
+  }
+  d[k * dim + 0] = ORC_INF;
+  d[0 * dim + k] = ORC_ZERO_LE;
+  d[k * dim + k] = ORC_ZERO_LE;
+}
+int32_t orc_dbm_includes(const int32_t* a, const int32_t* b, int32_t dim) {
+  for (int i = 0; i < dim * dim; ++i) if (b[i] > a[i]) return 0;
+  return 1;
+}
+/* z ≼_aLU zp (netengine_metal.mm:240-252; passed_set.hpp:41-48). */
+int32_t orc_dbm_alu_le(const int32_t* z, const int32_t* zp, int32_t dim, const int32_t* L,
+                       const int32_t* U) {
+  for (int x = 0; x < dim; ++x) {
+    if (U[x] == ORC_ALU_NEG_INF) continue;
+    if (z[0 * dim + x] < r_le(-U[x])) continue;
+    for (int y = 0; y < dim; ++y) {
+      if (x == y) continue;
+      if (L[y] == ORC_ALU_NEG_INF) continue;
+      if (zp[y * dim + x] < z[y * dim + x] && r_add(zp[y * dim + x], r_lt(-L[y])) < z[0 * dim + x])
+        return 0;
+    }
+  }
+  return 1;
+}
+/* Extra_LU+ then close (engine_metal.mm:80-93). */
+void orc_dbm_extrap_lu_plus(int32_t* d, int32_t dim, const int32_t* L, const int32_t* U) {
+  int32_t row0[64];
+  for (int k = 0; k < dim; ++k) row0[k] = d[k];
+  for (int i = 0; i < dim; ++i)
+    for (int j = 0; j < dim; ++j) {
+      if (i == j) continue;
+      int32_t e = d[i * dim + j];
+      if (e >= ORC_INF) continue;
+      if (r_bound(e) > L[i]) { d[i * dim + j] = ORC_INF; continue; }
+      if (-r_bound(row0[i]) > L[i]) { d[i * dim + j] = ORC_INF; continue; }
+      if (i != 0 && -r_bound(row0[j]) > U[j]) { d[i * dim + j] = ORC_INF; continue; }
+      if (e < r_lt(-U[j])) d[i * dim + j] = r_lt(-U[j]);
+    }
+  orc_dbm_close(d, dim);
+}
+/* Exact convex union (netengine_metal.mm:310-335): a ∪ b is convex iff every region the hull
+ * gains by relaxing one of a's constraints lies in b, and vice versa. Every tightening constraint
+ * is tested, which decides the same set identity the minimal-graph filter decides (a redundant
+ * constraint's complement is covered by the complements of the generating ones). */
+int32_t orc_dbm_try_union(int32_t* a, const int32_t* b, int32_t dim) {
+  int32_t H[64 * 64], R[64 * 64];
+  const int d2 = dim * dim;
+  for (int k = 0; k < d2; ++k) H[k] = a[k] > b[k] ? a[k] : b[k];
+  for (int pass = 0; pass < 2; ++pass) {
+    const int32_t* z = pass == 0 ? a : b;
+    const int32_t* other = pass == 0 ? b : a;
+    for (int i = 0; i < dim; ++i)
+      for (int j = 0; j < dim; ++j) {
+        if (i == j || z[i * dim + j] >= H[i * dim + j]) continue;
+        memcpy(R, H, sizeof(int32_t) * d2);
+        if (!orc_dbm_constrain(R, dim, j, i, r_negate(z[i * dim + j]))) continue;
+        if (!orc_dbm_includes(other, R, dim)) return 0;
+      }
+  }
+  memcpy(a, H, sizeof(int32_t) * d2);
+  return 1;
+}
+
+/* Is z covered by the union of the k zones w? Depth-first subtraction: z \ w0 splits into disjoint
+ * pieces z ∧ c_1 ∧ .. ∧ c_{m-1} ∧ ¬c_m over w0's tightening constraints c_m, and each piece must be
+ * covered by w1..w{k-1} (fed_subtract semantics, src/reachability/deadlock.cpp:262-267). */
+static int fed_covers_rec(const int32_t* z, const int32_t* w, int k, int dim) {
+  const int d2 = dim * dim;
+  int i = 0;
+  int32_t t[64 * 64];
+  for (; i < k; ++i) {
+    /* skip w[i] that misses z entirely */
+    memcpy(t, z, sizeof(int32_t) * d2);
+    int ok = 1;
+    for (int a = 0; a < dim && ok; ++a)
+      for (int b = 0; b < dim && ok; ++b)
+        if (a != b && w[i * d2 + a * dim + b] < t[a * dim + b])
+          ok = orc_dbm_constrain(t, dim, a, b, w[i * d2 + a * dim + b]);
+    if (ok) break;
+  }
+  if (i == k) return 0;
+  const int32_t* wi = w + (size_t)i * d2;
+  if (orc_dbm_includes(wi, z, dim)) return 1;
+  int32_t* r = (int32_t*)malloc(sizeof(int32_t) * d2 * 2);
+  int32_t* p = r + d2;
+  memcpy(r, z, sizeof(int32_t) * d2);
+  int res = 1;
+  for (int a = 0; a < dim && res; ++a)
+    for (int b = 0; b < dim && res; ++b) {
+      if (a == b || wi[a * dim + b] >= r[a * dim + b]) continue;
+      memcpy(p, r, sizeof(int32_t) * d2);
+      if (orc_dbm_constrain(p, dim, b, a, r_negate(wi[a * dim + b])))
+        if (!fed_covers_rec(p, w + (size_t)(i + 1) * d2, k - i - 1, dim)) res = 0;
+      if (!res) break;
+      if (!orc_dbm_constrain(r, dim, a, b, wi[a * dim + b])) { a = dim; break; }
+    }
+  free(r);
+  return res;
+}
+int32_t orc_fed_covers(const int32_t* z, const int32_t* w, int32_t k, int32_t dim) {
+  if (orc_dbm_empty(z, dim)) return 1;
+  return fed_covers_rec(z, w, k, dim);
+}
+
+/* ============================================================================================
+ * Compiled model: indices and the static analyses of src/model/network.cpp
+ * ============================================================================================ */
+typedef struct {
+  const hora_net_desc* n;
+  int dim, nlocs_total;
+  int* loc_base;        /* [nprocs] */
+  int* eloc_off;        /* [nlocs_total+1] edges of each (global) location, in edge order */
+  int* eloc;            /* edge ids */
+  int32_t *L, *U;       /* global Extra_LU bounds [dim] */
+  int32_t *Lloc, *Uloc; /* per-location a_LU bounds [nlocs_total*dim] */
+  uint64_t* act;        /* active masks [nlocs_total] */
+  int* kshift;          /* [nprocs+nints] discrete-key field offsets */
+  int* kwidth;          /* [nprocs+nints] discrete-key field widths */
+  int keybits;
+  int has_urgent_chan;
+  int has_diag;
+} Model;
+
+static int ceil_log2(long n) { int b = 0; while ((1L << b) < n) ++b; return b; }
+
+static void model_free(Model* m) {
+  free(m->loc_base); free(m->eloc_off); free(m->eloc); free(m->L); free(m->U);
+  free(m->Lloc); free(m->Uloc); free(m->act); free(m->kshift); free(m->kwidth);
+}
+
+/* compute_bounds (network.cpp:59-85), compute_loc_bounds (:105-182), compute_active (:184-232). */
+static int model_build(const hora_net_desc* n, Model* m) {
+  memset(m, 0, sizeof *m);
+  m->n = n;
+  if (n->nclocks < 0 || n->nclocks > 62 || n->nprocs <= 0) return HORA_E_INVALID;
+  const int dim = n->nclocks + 1;
+  m->dim = dim;
+  m->loc_base = (int*)calloc(n->nprocs, sizeof(int));
+  int tot = 0;
+  for (int p = 0; p < n->nprocs; ++p) { m->loc_base[p] = tot; tot += n->proc_nlocs[p]; }
+  m->nlocs_total = tot;
+  m->eloc_off = (int*)calloc(tot + 1, sizeof(int));
+  m->eloc = (int*)calloc(n->nedges > 0 ? n->nedges : 1, sizeof(int));
+  for (int e = 0; e < n->nedges; ++e) m->eloc_off[m->loc_base[n->edge_proc[e]] + n->edge_src[e] + 1]++;
+  for (int l = 0; l < tot; ++l) m->eloc_off[l + 1] += m->eloc_off[l];
+  int* fill = (int*)calloc(tot, sizeof(int));
+  for (int e = 0; e < n->nedges; ++e) {
+    int gl = m->loc_base[n->edge_proc[e]] + n->edge_src[e];
+    m->eloc[m->eloc_off[gl] + fill[gl]++] = e;
+  }
+  free(fill);
+  /* diagonal / urgent-channel flags */
+  for (int l = 0; l < tot; ++l)
+    for (int c = n->loc_inv_off[l]; c < n->loc_inv_off[l + 1]; ++c)
+      if (n->cons[3 * c] > 0 && n->cons[3 * c + 1] > 0) m->has_diag = 1;
+  for (int e = 0; e < n->nedges; ++e)
+    for (int c = n->edge_guard_off[e]; c < n->edge_guard_off[e + 1]; ++c)
+      if (n->cons[3 * c] > 0 && n->cons[3 * c + 1] > 0) m->has_diag = 1;
+  for (int ch = 0; ch < n->nchans; ++ch) if (n->chan_flags[ch] & HORA_CHAN_URGENT) m->has_urgent_chan = 1;
+  /* global bounds */
+  m->L = (int32_t*)calloc(dim, sizeof(int32_t));
+  m->U = (int32_t*)calloc(dim, sizeof(int32_t));
+#define SCAN_GLOBAL(c0, c1)                                                         \
+  for (int c = (c0); c < (c1); ++c) {                                               \
+    int i = n->cons[3 * c], j = n->cons[3 * c + 1], v = r_bound(n->cons[3 * c + 2]); \
+    if (i > 0 && j == 0) { if (v > m->U[i]) m->U[i] = v; }                          \
+    else if (i == 0 && j > 0) { if (-v > m->L[j]) m->L[j] = -v; }                   \
+    else if (i > 0 && j > 0) {                                                      \
+      int a = v < 0 ? -v : v;                                                       \
+      m->U[i] = imax(m->U[i], a); m->U[j] = imax(m->U[j], a);                       \
+      m->L[i] = imax(m->L[i], a); m->L[j] = imax(m->L[j], a);                       \
+    }                                                                               \
+  }
+  for (int l = 0; l < tot; ++l) SCAN_GLOBAL(n->loc_inv_off[l], n->loc_inv_off[l + 1]);
+  for (int e = 0; e < n->nedges; ++e) SCAN_GLOBAL(n->edge_guard_off[e], n->edge_guard_off[e + 1]);
+#undef SCAN_GLOBAL
+  m->L[0] = m->U[0] = 0;
+  /* per-location a_LU bounds: backward least fixpoint within each process */
+  m->Lloc = (int32_t*)malloc(sizeof(int32_t) * tot * dim);
+  m->Uloc = (int32_t*)malloc(sizeof(int32_t) * tot * dim);
+  for (int k = 0; k < tot * dim; ++k) m->Lloc[k] = m->Uloc[k] = ORC_ALU_NEG_INF;
+  int32_t* Lc = (int32_t*)malloc(sizeof(int32_t) * dim);
+  int32_t* Uc = (int32_t*)malloc(sizeof(int32_t) * dim);
+  char* rst = (char*)malloc(dim);
+#define SCAN_LOC(c0, c1)                                                            \
+  for (int c = (c0); c < (c1); ++c) {                                               \
+    int i = n->cons[3 * c], j = n->cons[3 * c + 1], v = r_bound(n->cons[3 * c + 2]); \
+    if (i > 0 && j == 0) Uc[i] = imax(Uc[i], v);                                    \
+    else if (i == 0 && j > 0) Lc[j] = imax(Lc[j], -v);                              \
+    else if (i > 0 && j > 0) {                                                      \
+      int a = v < 0 ? -v : v;                                                       \
+      Uc[i] = imax(Uc[i], a); Uc[j] = imax(Uc[j], a);                               \
+      Lc[i] = imax(Lc[i], a); Lc[j] = imax(Lc[j], a);                               \
+    }                                                                               \
+  }
+  for (int p = 0; p < n->nprocs; ++p) {
+    const int nl = n->proc_nlocs[p], base = m->loc_base[p];
+    int changed = 1;
+    while (changed) {
+      changed = 0;
+      for (int l = 0; l < nl; ++l) {
+        for (int c = 0; c < dim; ++c) Lc[c] = Uc[c] = ORC_ALU_NEG_INF;
+        SCAN_LOC(n->loc_inv_off[base + l], n->loc_inv_off[base + l + 1]);
+        for (int k = m->eloc_off[base + l]; k < m->eloc_off[base + l + 1]; ++k) {
+          const int e = m->eloc[k];
+          SCAN_LOC(n->edge_guard_off[e], n->edge_guard_off[e + 1]);
+          memset(rst, 0, dim);
+          for (int r = n->edge_reset_off[e]; r < n->edge_reset_off[e + 1]; ++r) rst[n->resets[r]] = 1;
+          const int tg = base + n->edge_tgt[e];
+          for (int c = 1; c < dim; ++c)
+            if (!rst[c]) {
+              Lc[c] = imax(Lc[c], m->Lloc[tg * dim + c]);
+              Uc[c] = imax(Uc[c], m->Uloc[tg * dim + c]);
+            }
+        }
+        for (int c = 1; c < dim; ++c) {
+          if (Lc[c] > m->Lloc[(base + l) * dim + c]) { m->Lloc[(base + l) * dim + c] = Lc[c]; changed = 1; }
+          if (Uc[c] > m->Uloc[(base + l) * dim + c]) { m->Uloc[(base + l) * dim + c] = Uc[c]; changed = 1; }
+        }
+      }
+    }
+  }
+#undef SCAN_LOC
+  /* active clocks */
+  m->act = (uint64_t*)calloc(tot, sizeof(uint64_t));
+  for (int p = 0; p < n->nprocs; ++p) {
+    const int nl = n->proc_nlocs[p], base = m->loc_base[p];
+    int changed = 1;
+    while (changed) {
+      changed = 0;
+      for (int l = 0; l < nl; ++l) {
+        uint64_t A = 0;
+        for (int c = n->loc_inv_off[base + l]; c < n->loc_inv_off[base + l + 1]; ++c) {
+          if (n->cons[3 * c] > 0) A |= 1ull << n->cons[3 * c];
+          if (n->cons[3 * c + 1] > 0) A |= 1ull << n->cons[3 * c + 1];
+        }
+        for (int k = m->eloc_off[base + l]; k < m->eloc_off[base + l + 1]; ++k) {
+          const int e = m->eloc[k];
+          for (int c = n->edge_guard_off[e]; c < n->edge_guard_off[e + 1]; ++c) {
+            if (n->cons[3 * c] > 0) A |= 1ull << n->cons[3 * c];
+            if (n->cons[3 * c + 1] > 0) A |= 1ull << n->cons[3 * c + 1];
+          }
+          uint64_t r = 0;
+          for (int q = n->edge_reset_off[e]; q < n->edge_reset_off[e + 1]; ++q) r |= 1ull << n->resets[q];
+          A |= m->act[base + n->edge_tgt[e]] & ~r;
+        }
+        A &= ~1ull;
+        if (A & ~m->act[base + l]) { m->act[base + l] |= A; changed = 1; }
+      }
+    }
+  }
+  free(Lc); free(Uc); free(rst);
+  /* discrete key layout (DiscKeyCodecT, src/reachability/engine.cpp:967-1026) */
+  m->kshift = (int*)calloc(n->nprocs + n->nints + 1, sizeof(int));
+  m->kwidth = (int*)calloc(n->nprocs + n->nints + 1, sizeof(int));
+  int off = 0;
+  for (int p = 0; p < n->nprocs; ++p) {
+    m->kshift[p] = off; m->kwidth[p] = ceil_log2(n->proc_nlocs[p]); off += m->kwidth[p];
+  }
+  for (int v = 0; v < n->nints; ++v) {
+    m->kshift[n->nprocs + v] = off;
+    m->kwidth[n->nprocs + v] = ceil_log2((long)n->int_hi[v] - n->int_lo[v] + 1);
+    off += m->kwidth[n->nprocs + v];
+  }
+  m->keybits = off;
+  return HORA_OK;
+}
+
+int32_t orc_static_bounds(const hora_net_desc* net, int32_t* L, int32_t* U, int32_t* Lloc,
+                          int32_t* Uloc, uint64_t* act) {
+  Model m;
+  int rc = model_build(net, &m);
+  if (rc) { model_free(&m); return rc; }
+  memcpy(L, m.L, sizeof(int32_t) * m.dim);
+  memcpy(U, m.U, sizeof(int32_t) * m.dim);
+  memcpy(Lloc, m.Lloc, sizeof(int32_t) * m.dim * m.nlocs_total);
+  memcpy(Uloc, m.Uloc, sizeof(int32_t) * m.dim * m.nlocs_total);
+  memcpy(act, m.act, sizeof(uint64_t) * m.nlocs_total);
+  model_free(&m);
+  return HORA_OK;
+}
+
+static uint64_t key_encode(const Model* m, const int32_t* locs, const int32_t* ints) {
+  uint64_t k = 0;
+  for (int p = 0; p < m->n->nprocs; ++p) k |= (uint64_t)(uint32_t)locs[p] << m->kshift[p];
+  for (int v = 0; v < m->n->nints; ++v)
+    k |= (uint64_t)(uint32_t)(ints[v] - m->n->int_lo[v]) << m->kshift[m->n->nprocs + v];
+  return k;
+}
+static void key_decode(const Model* m, uint64_t k, int32_t* locs, int32_t* ints) {
+  const hora_net_desc* n = m->n;
+  for (int p = 0; p < n->nprocs; ++p)
+    locs[p] = (int32_t)((k >> m->kshift[p]) & ((1ull << m->kwidth[p]) - 1));
+  for (int v = 0; v < n->nints; ++v) {
+    const int f = n->nprocs + v;
+    ints[v] = (int32_t)((k >> m->kshift[f]) & ((1ull << m->kwidth[f]) - 1)) + n->int_lo[v];
+  }
+}
+
+/* ============================================================================================
+ * Transition semantics (include/hora/detail/semantics.hpp)
+ * ============================================================================================ */
+static int int_ok(const hora_net_desc* n, int e, const int32_t* ints) {  /* semantics.hpp:53-68 */
+  for (int a = n->edge_iguard_off[e]; a < n->edge_iguard_off[e + 1]; ++a) {
+    const int32_t x = ints[n->iatoms[3 * a]], op = n->iatoms[3 * a + 1], v = n->iatoms[3 * a + 2];
+    int r = 0;
+    switch (op) {
+      case HORA_IOP_EQ: r = x == v; break;
+      case HORA_IOP_NE: r = x != v; break;
+      case HORA_IOP_LT: r = x < v; break;
+      case HORA_IOP_LE: r = x <= v; break;
+      case HORA_IOP_GT: r = x > v; break;
+      case HORA_IOP_GE: r = x >= v; break;
+    }
+    if (!r) return 0;
+  }
+  return 1;
+}
+static int ints_ok(const int32_t* atoms, int na, const int32_t* ints) {
+  for (int a = 0; a < na; ++a) {
+    const int32_t x = ints[atoms[3 * a]], op = atoms[3 * a + 1], v = atoms[3 * a + 2];
+    int r = 0;
+    switch (op) {
+      case HORA_IOP_EQ: r = x == v; break;
+      case HORA_IOP_NE: r = x != v; break;
+      case HORA_IOP_LT: r = x < v; break;
+      case HORA_IOP_LE: r = x <= v; break;
+      case HORA_IOP_GT: r = x > v; break;
+      case HORA_IOP_GE: r = x >= v; break;
+    }
+    if (!r) return 0;
+  }
+  return 1;
+}
+static int apply_cons(int32_t* z, int dim, const int32_t* cons, int c0, int c1) {  /* apply_all */
+  for (int c = c0; c < c1; ++c)
+    if (!orc_dbm_constrain(z, dim, cons[3 * c], cons[3 * c + 1], cons[3 * c + 2])) return 0;
+  return 1;
+}
+static int apply_inv(const Model* m, int32_t* z, const int32_t* locs) {  /* all_invariants+apply_all */
+  const hora_net_desc* n = m->n;
+  for (int p = 0; p < n->nprocs; ++p) {
+    const int gl = m->loc_base[p] + locs[p];
+    if (!apply_cons(z, m->dim, n->cons, n->loc_inv_off[gl], n->loc_inv_off[gl + 1])) return 0;
+  }
+  return 1;
+}
+static inline int loc_committed(const Model* m, int p, int l) {
+  return (m->n->loc_flags[m->loc_base[p] + l] & HORA_LOC_COMMITTED) != 0;
+}
+/* urgent_sync_enabled (semantics.hpp:118-139) */
+static int urgent_sync_enabled(const Model* m, const int32_t* locs, const int32_t* ints) {
+  const hora_net_desc* n = m->n;
+  if (!m->has_urgent_chan) return 0;
+  for (int i = 0; i < n->nprocs; ++i) {
+    const int gi = m->loc_base[i] + locs[i];
+    for (int k = m->eloc_off[gi]; k < m->eloc_off[gi + 1]; ++k) {
+      const int se = m->eloc[k];
+      if (n->edge_chan[se] < 0 || n->edge_dir[se] != 1) continue;
+      if (!(n->chan_flags[n->edge_chan[se]] & HORA_CHAN_URGENT)) continue;
+      if (!int_ok(n, se, ints)) continue;
+      if (n->chan_flags[n->edge_chan[se]] & HORA_CHAN_BROADCAST) return 1;
+      for (int j = 0; j < n->nprocs; ++j) {
+        if (j == i) continue;
+        const int gj = m->loc_base[j] + locs[j];
+        for (int q = m->eloc_off[gj]; q < m->eloc_off[gj + 1]; ++q) {
+          const int re = m->eloc[q];
+          if (n->edge_chan[re] != n->edge_chan[se] || n->edge_dir[re] != -1) continue;
+          if (int_ok(n, re, ints)) return 1;
+        }
+      }
+    }
+  }
+  return 0;
+}
+/* frozen_flags (semantics.hpp:160-169) */
+static void frozen_flags(const Model* m, const int32_t* locs, const int32_t* ints, int* committed,
+                         int* urgent) {
+  *committed = *urgent = 0;
+  for (int p = 0; p < m->n->nprocs; ++p) {
+    int f = m->n->loc_flags[m->loc_base[p] + locs[p]];
+    if (f & HORA_LOC_COMMITTED) *committed = 1;
+    if (f & HORA_LOC_URGENT) *urgent = 1;
+  }
+  if (!*urgent && urgent_sync_enabled(m, locs, ints)) *urgent = 1;
+}
+/* reset_inactive (semantics.hpp:186-215) */
+static void reset_inactive(const Model* m, const int32_t* locs, int32_t* z, const uint8_t* qmask) {
+  uint64_t a = 0;
+  for (int p = 0; p < m->n->nprocs; ++p) a |= m->act[m->loc_base[p] + locs[p]];
+  for (int c = 1; c < m->dim; ++c) if (qmask && qmask[c]) a |= 1ull << c;
+  uint64_t dead = ~a & (((1ull << m->n->nclocks) - 1) << 1);
+  while (dead) {
+    int c = __builtin_ctzll(dead);
+    dead &= dead - 1;
+    orc_dbm_reset(z, m->dim, c);
+  }
+}
+/* close_succ_zone without the avoid-set (semantics.hpp:522-568). Returns 0 when the target
+ * invariant is unsatisfiable; the caller tests emptiness. */
+static int close_succ_zone(const Model* m, const int32_t* tl, const int32_t* ti, int32_t* z,
+                           const uint8_t* qmask, const int32_t* L, const int32_t* U, int emode) {
+  if (!apply_inv(m, z, tl)) return 0;
+  int c, u;
+  frozen_flags(m, tl, ti, &c, &u);
+  if (!c && !u) { orc_dbm_delay(z, m->dim); apply_inv(m, z, tl); }
+  reset_inactive(m, tl, z, qmask);
+  if (emode == 1) orc_dbm_extrap_lu_plus(z, m->dim, L, U);
+  return 1;
+}
+
+/* Broadcast receiver options (build_broadcast_parts, semantics.hpp:275-303). */
+#define MAXOPT 128
+#define MAXPART 64
+typedef struct {
+  int proc;
+  int nopt;
+  int edge[MAXOPT];        /* edge id, or -1 for an abstain option */
+  int xoff[MAXOPT];        /* abstain option: offset into xcons (triples) */
+  int xn[MAXOPT];          /* abstain option: constraint count */
+} Part;
+typedef struct {
+  int nparts;
+  Part parts[MAXPART];
+  int32_t* xcons;
+  int nx, capx;
+} Parts;
+static void xpush(Parts* P, int i, int j, int32_t raw) {
+  if (P->nx + 1 > P->capx) {
+    P->capx = P->capx ? P->capx * 2 : 256;
+    P->xcons = (int32_t*)realloc(P->xcons, sizeof(int32_t) * 3 * P->capx);
+  }
+  P->xcons[3 * P->nx] = i; P->xcons[3 * P->nx + 1] = j; P->xcons[3 * P->nx + 2] = raw;
+  P->nx++;
+}
+/* One broadcast-enumeration scratch block, reused across calls (the oracle is single-threaded). */
+static Parts* parts_scratch(void) {
+  static Parts* P = NULL;
+  if (!P) P = (Parts*)calloc(1, sizeof(Parts));
+  return P;
+}
+static int build_broadcast_parts(const Model* m, const int32_t* locs, const int32_t* ints, int se,
+                                 int sender, Parts* P) {
+  const hora_net_desc* n = m->n;
+  P->nparts = 0; P->nx = 0;
+  for (int j = 0; j < n->nprocs; ++j) {
+    if (j == sender) continue;
+    Part* pt = &P->parts[P->nparts];
+    pt->proc = j; pt->nopt = 0;
+    int guards[MAXOPT], ng = 0;
+    const int gj = m->loc_base[j] + locs[j];
+    for (int q = m->eloc_off[gj]; q < m->eloc_off[gj + 1]; ++q) {
+      const int re = m->eloc[q];
+      if (n->edge_chan[re] == n->edge_chan[se] && n->edge_dir[re] == -1 && int_ok(n, re, ints)) {
+        pt->edge[pt->nopt] = re; pt->xoff[pt->nopt] = 0; pt->xn[pt->nopt] = 0; pt->nopt++;
+        guards[ng++] = re;
+      }
+    }
+    if (pt->nopt == 0) continue;
+    /* DNF of the complement of the disjunction of the enabled receivers' clock guards */
+    int ndnf = 1, empty_guard = 0;
+    for (int g = 0; g < ng; ++g) {
+      int len = n->edge_guard_off[guards[g] + 1] - n->edge_guard_off[guards[g]];
+      if (len == 0) { empty_guard = 1; break; }
+      ndnf *= len;
+    }
+    if (!empty_guard) {
+      if (pt->nopt + ndnf > MAXOPT) return 0;
+      for (int t = 0; t < ndnf; ++t) {
+        /* disjunct t picks atom index (t / prod of earlier lengths) % len of each guard, in the
+           order the reference's cross product appends them (earlier guards vary slowest) */
+        int o = pt->nopt++;
+        pt->edge[o] = -1; pt->xoff[o] = P->nx; pt->xn[o] = ng;
+        int rem = t;
+        int idx[MAXOPT];
+        for (int g = ng - 1; g >= 0; --g) {
+          int len = n->edge_guard_off[guards[g] + 1] - n->edge_guard_off[guards[g]];
+          idx[g] = rem % len; rem /= len;
+        }
+        for (int g = 0; g < ng; ++g) {
+          int c = n->edge_guard_off[guards[g]] + idx[g];
+          /* negate(c): x_i - x_j <| v  ->  x_j - x_i <|' -v */
+          xpush(P, n->cons[3 * c + 1], n->cons[3 * c], r_negate(n->cons[3 * c + 2]));
+        }
+      }
+    }
+    if (++P->nparts > MAXPART) return 0;
+  }
+  return 1;
+}
+
+/* Successor generation (successors_net, src/reachability/engine.cpp:243-368; the same emission
+ * order as tagged_successors, src/liveness/operators.cpp:55-206). Calls emit() per non-empty
+ * successor in order. */
+typedef void (*emit_fn)(void* ctx, const int32_t* locs, const int32_t* ints, const int32_t* zone);
+static int successors(const Model* m, const int32_t* locs, const int32_t* ints, const int32_t* zone,
+                      const int32_t* L, const int32_t* U, const uint8_t* qmask, int emode,
+                      emit_fn emit, void* ctx) {
+  const hora_net_desc* n = m->n;
+  const int dim = m->dim, d2 = dim * dim, np = n->nprocs, ni = n->nints;
+  int32_t z1[64 * 64];
+  int32_t tl[64], ti[64];
+  int src_c, src_u;
+  frozen_flags(m, locs, ints, &src_c, &src_u);
+  /* local edges */
+  for (int p = 0; p < np; ++p) {
+    if (src_c && !loc_committed(m, p, locs[p])) continue;
+    const int gp = m->loc_base[p] + locs[p];
+    for (int k = m->eloc_off[gp]; k < m->eloc_off[gp + 1]; ++k) {
+      const int e = m->eloc[k];
+      if (n->edge_chan[e] >= 0) continue;
+      if (!int_ok(n, e, ints)) continue;
+      memcpy(z1, zone, sizeof(int32_t) * d2);
+      if (!apply_cons(z1, dim, n->cons, n->edge_guard_off[e], n->edge_guard_off[e + 1])) continue;
+      for (int r = n->edge_reset_off[e]; r < n->edge_reset_off[e + 1]; ++r) orc_dbm_reset(z1, dim, n->resets[r]);
+      memcpy(tl, locs, sizeof(int32_t) * np); tl[p] = n->edge_tgt[e];
+      memcpy(ti, ints, sizeof(int32_t) * ni);
+      for (int u = n->edge_iupd_off[e]; u < n->edge_iupd_off[e + 1]; ++u) ti[n->iupds[2 * u]] = n->iupds[2 * u + 1];
+      if (!close_succ_zone(m, tl, ti, z1, qmask, L, U, emode)) continue;
+      if (orc_dbm_empty(z1, dim)) continue;
+      emit(ctx, tl, ti, z1);
+    }
+  }
+  /* binary synchronisation */
+  for (int i = 0; i < np; ++i) {
+    const int gi = m->loc_base[i] + locs[i];
+    for (int k = m->eloc_off[gi]; k < m->eloc_off[gi + 1]; ++k) {
+      const int se = m->eloc[k];
+      if (n->edge_chan[se] < 0 || n->edge_dir[se] != 1) continue;
+      if (n->chan_flags[n->edge_chan[se]] & HORA_CHAN_BROADCAST) continue;
+      if (!int_ok(n, se, ints)) continue;
+      const int i_comm = loc_committed(m, i, locs[i]);
+      for (int j = 0; j < np; ++j) {
+        if (j == i) continue;
+        const int gj = m->loc_base[j] + locs[j];
+        for (int q = m->eloc_off[gj]; q < m->eloc_off[gj + 1]; ++q) {
+          const int re = m->eloc[q];
+          if (n->edge_chan[re] != n->edge_chan[se] || n->edge_dir[re] != -1) continue;
+          if (src_c && !(i_comm || loc_committed(m, j, locs[j]))) continue;
+          if (!int_ok(n, re, ints)) continue;
+          memcpy(z1, zone, sizeof(int32_t) * d2);
+          if (!apply_cons(z1, dim, n->cons, n->edge_guard_off[se], n->edge_guard_off[se + 1])) continue;
+          if (!apply_cons(z1, dim, n->cons, n->edge_guard_off[re], n->edge_guard_off[re + 1])) continue;
+          for (int r = n->edge_reset_off[se]; r < n->edge_reset_off[se + 1]; ++r) orc_dbm_reset(z1, dim, n->resets[r]);
+          for (int r = n->edge_reset_off[re]; r < n->edge_reset_off[re + 1]; ++r) orc_dbm_reset(z1, dim, n->resets[r]);
+          memcpy(tl, locs, sizeof(int32_t) * np); tl[i] = n->edge_tgt[se]; tl[j] = n->edge_tgt[re];
+          memcpy(ti, ints, sizeof(int32_t) * ni);
+          for (int u = n->edge_iupd_off[se]; u < n->edge_iupd_off[se + 1]; ++u) ti[n->iupds[2 * u]] = n->iupds[2 * u + 1];
+          for (int u = n->edge_iupd_off[re]; u < n->edge_iupd_off[re + 1]; ++u) ti[n->iupds[2 * u]] = n->iupds[2 * u + 1];
+          if (!close_succ_zone(m, tl, ti, z1, qmask, L, U, emode)) continue;
+          if (orc_dbm_empty(z1, dim)) continue;
+          emit(ctx, tl, ti, z1);
+        }
+      }
+    }
+  }
+  /* broadcast synchronisation */
+  Parts* P = parts_scratch();
+  int ok_all = 1;
+  for (int i = 0; i < np && ok_all; ++i) {
+    const int gi = m->loc_base[i] + locs[i];
+    for (int k = m->eloc_off[gi]; k < m->eloc_off[gi + 1]; ++k) {
+      const int se = m->eloc[k];
+      if (n->edge_chan[se] < 0 || n->edge_dir[se] != 1 || !(n->chan_flags[n->edge_chan[se]] & HORA_CHAN_BROADCAST)) continue;
+      if (!int_ok(n, se, ints)) continue;
+      if (!build_broadcast_parts(m, locs, ints, se, i, P)) { ok_all = 0; break; }
+      int pick[MAXPART];
+      memset(pick, 0, sizeof pick);
+      for (;;) {
+        int part_comm = loc_committed(m, i, locs[i]);
+        for (int t = 0; t < P->nparts; ++t) {
+          const Part* pt = &P->parts[t];
+          if (pt->edge[pick[t]] >= 0 && loc_committed(m, pt->proc, locs[pt->proc])) part_comm = 1;
+        }
+        if (!src_c || part_comm) {
+          memcpy(z1, zone, sizeof(int32_t) * d2);
+          int ok = apply_cons(z1, dim, n->cons, n->edge_guard_off[se], n->edge_guard_off[se + 1]);
+          for (int t = 0; ok && t < P->nparts; ++t) {
+            const Part* pt = &P->parts[t];
+            const int o = pick[t];
+            if (pt->edge[o] >= 0)
+              ok = apply_cons(z1, dim, n->cons, n->edge_guard_off[pt->edge[o]], n->edge_guard_off[pt->edge[o] + 1]);
+            else
+              ok = apply_cons(z1, dim, P->xcons, pt->xoff[o], pt->xoff[o] + pt->xn[o]);
+          }
+          if (ok) {
+            memcpy(tl, locs, sizeof(int32_t) * np);
+            memcpy(ti, ints, sizeof(int32_t) * ni);
+            tl[i] = n->edge_tgt[se];
+            for (int u = n->edge_iupd_off[se]; u < n->edge_iupd_off[se + 1]; ++u) ti[n->iupds[2 * u]] = n->iupds[2 * u + 1];
+            for (int r = n->edge_reset_off[se]; r < n->edge_reset_off[se + 1]; ++r) orc_dbm_reset(z1, dim, n->resets[r]);
+            for (int t = 0; t < P->nparts; ++t) {
+              const Part* pt = &P->parts[t];
+              const int re = pt->edge[pick[t]];
+              if (re < 0) continue;
+              tl[pt->proc] = n->edge_tgt[re];
+              for (int u = n->edge_iupd_off[re]; u < n->edge_iupd_off[re + 1]; ++u) ti[n->iupds[2 * u]] = n->iupds[2 * u + 1];
+              for (int r = n->edge_reset_off[re]; r < n->edge_reset_off[re + 1]; ++r) orc_dbm_reset(z1, dim, n->resets[r]);
+            }
+            if (close_succ_zone(m, tl, ti, z1, qmask, L, U, emode) && !orc_dbm_empty(z1, dim))
+              emit(ctx, tl, ti, z1);
+          }
+        }
+        if (P->nparts == 0) break;
+        int t = 0;
+        for (; t < P->nparts; ++t) { if (++pick[t] < P->parts[t].nopt) break; pick[t] = 0; }
+        if (t == P->nparts) break;
+      }
+    }
+  }
+  return ok_all;
+}
+
+/* ============================================================================================
+ * Deadlock predicate (state_has_deadlock, src/reachability/deadlock.cpp:74-270)
+ * ============================================================================================ */
+typedef struct {
+  int32_t* w;
+  int nw, cap, dim;
+  const int32_t* Z;
+  int covered;
+} Escapes;
+static void esc_add(Escapes* E, const Model* m, int32_t* g, const int32_t* tl, const uint64_t rmask) {
+  /* pull the target invariant back through the resets (deadlock.cpp:118-127) */
+  const hora_net_desc* n = m->n;
+  const int dim = m->dim, d2 = dim * dim;
+  for (int p = 0; p < n->nprocs; ++p) {
+    const int gl = m->loc_base[p] + tl[p];
+    for (int c = n->loc_inv_off[gl]; c < n->loc_inv_off[gl + 1]; ++c) {
+      int i = n->cons[3 * c], j = n->cons[3 * c + 1];
+      const int32_t b = n->cons[3 * c + 2];
+      if ((rmask >> i) & 1) i = 0;
+      if ((rmask >> j) & 1) j = 0;
+      if (i == j) { if (b < ORC_ZERO_LE) return; continue; }
+      if (!orc_dbm_constrain(g, dim, i, j, b)) return;
+    }
+  }
+  if (orc_dbm_empty(g, dim)) return;
+  if (memcmp(g, E->Z, sizeof(int32_t) * d2) == 0) { E->covered = 1; return; }
+  if (E->nw == E->cap) {
+    E->cap = E->cap ? E->cap * 2 : 16;
+    E->w = (int32_t*)realloc(E->w, sizeof(int32_t) * d2 * E->cap);
+  }
+  memcpy(E->w + (size_t)E->nw * d2, g, sizeof(int32_t) * d2);
+  E->nw++;
+}
+static uint64_t reset_mask(const hora_net_desc* n, int e) {
+  uint64_t r = 0;
+  for (int q = n->edge_reset_off[e]; q < n->edge_reset_off[e + 1]; ++q) r |= 1ull << n->resets[q];
+  return r;
+}
+static int state_has_deadlock(const Model* m, const int32_t* locs, const int32_t* ints, const int32_t* zone) {
+  const hora_net_desc* n = m->n;
+  const int dim = m->dim, d2 = dim * dim, np = n->nprocs, ni = n->nints;
+  if (orc_dbm_empty(zone, dim)) return 0;
+  int src_c, src_u;
+  frozen_flags(m, locs, ints, &src_c, &src_u);
+  const int frozen = src_c || src_u;
+  int32_t Z[64 * 64], g[64 * 64];
+  int32_t tl[64];
+  memcpy(Z, zone, sizeof(int32_t) * d2);
+  if (!frozen) orc_dbm_delay(Z, dim);
+  if (!apply_inv(m, Z, locs)) return 0;
+  Escapes E = {0};
+  E.dim = dim; E.Z = Z;
+  (void)ni;
+  for (int p = 0; p < np && !E.covered; ++p) {
+    if (src_c && !loc_committed(m, p, locs[p])) continue;
+    const int gp = m->loc_base[p] + locs[p];
+    for (int k = m->eloc_off[gp]; k < m->eloc_off[gp + 1] && !E.covered; ++k) {
+      const int e = m->eloc[k];
+      if (n->edge_chan[e] >= 0) continue;
+      if (!int_ok(n, e, ints)) continue;
+      memcpy(g, Z, sizeof(int32_t) * d2);
+      if (!apply_cons(g, dim, n->cons, n->edge_guard_off[e], n->edge_guard_off[e + 1])) continue;
+      memcpy(tl, locs, sizeof(int32_t) * np); tl[p] = n->edge_tgt[e];
+      esc_add(&E, m, g, tl, reset_mask(n, e));
+    }
+  }
+  for (int i = 0; i < np && !E.covered; ++i) {
+    const int gi = m->loc_base[i] + locs[i];
+    for (int k = m->eloc_off[gi]; k < m->eloc_off[gi + 1] && !E.covered; ++k) {
+      const int se = m->eloc[k];
+      if (n->edge_chan[se] < 0 || n->edge_dir[se] != 1) continue;
+      if (n->chan_flags[n->edge_chan[se]] & HORA_CHAN_BROADCAST) continue;
+      if (!int_ok(n, se, ints)) continue;
+      const int i_comm = loc_committed(m, i, locs[i]);
+      for (int j = 0; j < np && !E.covered; ++j) {
+        if (j == i) continue;
+        const int gj = m->loc_base[j] + locs[j];
+        for (int q = m->eloc_off[gj]; q < m->eloc_off[gj + 1] && !E.covered; ++q) {
+          const int re = m->eloc[q];
+          if (n->edge_chan[re] != n->edge_chan[se] || n->edge_dir[re] != -1) continue;
+          if (src_c && !(i_comm || loc_committed(m, j, locs[j]))) continue;
+          if (!int_ok(n, re, ints)) continue;
+          memcpy(g, Z, sizeof(int32_t) * d2);
+          if (!apply_cons(g, dim, n->cons, n->edge_guard_off[se], n->edge_guard_off[se + 1])) continue;
+          if (!apply_cons(g, dim, n->cons, n->edge_guard_off[re], n->edge_guard_off[re + 1])) continue;
+          memcpy(tl, locs, sizeof(int32_t) * np); tl[i] = n->edge_tgt[se]; tl[j] = n->edge_tgt[re];
+          esc_add(&E, m, g, tl, reset_mask(n, se) | reset_mask(n, re));
+        }
+      }
+    }
+  }
+  Parts* P = parts_scratch();
+  for (int i = 0; i < np && !E.covered; ++i) {
+    const int gi = m->loc_base[i] + locs[i];
+    for (int k = m->eloc_off[gi]; k < m->eloc_off[gi + 1] && !E.covered; ++k) {
+      const int se = m->eloc[k];
+      if (n->edge_chan[se] < 0 || n->edge_dir[se] != 1 || !(n->chan_flags[n->edge_chan[se]] & HORA_CHAN_BROADCAST)) continue;
+      if (!int_ok(n, se, ints)) continue;
+      build_broadcast_parts(m, locs, ints, se, i, P);
+      int pick[MAXPART];
+      memset(pick, 0, sizeof pick);
+      for (;;) {
+        int part_comm = loc_committed(m, i, locs[i]);
+        for (int t = 0; t < P->nparts; ++t) {
+          const Part* pt = &P->parts[t];
+          if (pt->edge[pick[t]] >= 0 && loc_committed(m, pt->proc, locs[pt->proc])) part_comm = 1;
+        }
+        if (!src_c || part_comm) {
+          memcpy(g, Z, sizeof(int32_t) * d2);
+          int ok = apply_cons(g, dim, n->cons, n->edge_guard_off[se], n->edge_guard_off[se + 1]);
+          uint64_t rm = reset_mask(n, se);
+          memcpy(tl, locs, sizeof(int32_t) * np); tl[i] = n->edge_tgt[se];
+          for (int t = 0; ok && t < P->nparts; ++t) {
+            const Part* pt = &P->parts[t];
+            const int o = pick[t];
+            if (pt->edge[o] < 0) { ok = apply_cons(g, dim, P->xcons, pt->xoff[o], pt->xoff[o] + pt->xn[o]); continue; }
+            const int re = pt->edge[o];
+            ok = apply_cons(g, dim, n->cons, n->edge_guard_off[re], n->edge_guard_off[re + 1]);
+            rm |= reset_mask(n, re);
+            tl[pt->proc] = n->edge_tgt[re];
+          }
+          if (ok) esc_add(&E, m, g, tl, rm);
+          if (E.covered) break;
+        }
+        if (P->nparts == 0) break;
+        int t = 0;
+        for (; t < P->nparts; ++t) { if (++pick[t] < P->parts[t].nopt) break; pick[t] = 0; }
+        if (t == P->nparts) break;
+      }
+    }
+  }
+  int dead;
+  if (E.covered) dead = 0;
+  else {
+    if (!frozen) for (int w = 0; w < E.nw; ++w) orc_dbm_down(E.w + (size_t)w * d2, dim);
+    dead = -1;
+    for (int w = 0; w < E.nw; ++w)
+      if (orc_dbm_includes(E.w + (size_t)w * d2, Z, dim)) { dead = 0; break; }
+    if (dead < 0) dead = !orc_fed_covers(Z, E.w, E.nw, dim);
+  }
+  free(E.w);
+  return dead;
+}
+
+/* ============================================================================================
+ * Host-buffer entry points
+ * ============================================================================================ */
+typedef struct {
+  int64_t cap, n;
+  int src, ord;
+  int np, ni, d2;
+  int32_t *out_src, *out_ord, *out_locs, *out_ints, *out_zones;
+} ExpCtx;
+static void exp_emit(void* c, const int32_t* locs, const int32_t* ints, const int32_t* zone) {
+  ExpCtx* x = (ExpCtx*)c;
+  if (x->n < x->cap) {
+    const int64_t k = x->n;
+    x->out_src[k] = x->src; x->out_ord[k] = x->ord;
+    memcpy(x->out_locs + k * x->np, locs, sizeof(int32_t) * x->np);
+    if (x->ni) memcpy(x->out_ints + k * x->ni, ints, sizeof(int32_t) * x->ni);
+    memcpy(x->out_zones + k * x->d2, zone, sizeof(int32_t) * x->d2);
+  }
+  x->n++;
+  x->ord++;
+}
+int32_t orc_expand(const hora_net_desc* net, int32_t n, const int32_t* locs, const int32_t* ints,
+                   const int32_t* zones, const int32_t* L, const int32_t* U, const uint8_t* qmask,
+                   int32_t emode, int64_t cap, int32_t* out_src, int32_t* out_ord,
+                   int32_t* out_locs, int32_t* out_ints, int32_t* out_zones, int64_t* out_n) {
+  Model m;
+  int rc = model_build(net, &m);
+  if (rc) { model_free(&m); return rc; }
+  ExpCtx x = {cap, 0, 0, 0, net->nprocs, net->nints, m.dim * m.dim,
+              out_src, out_ord, out_locs, out_ints, out_zones};
+  for (int s = 0; s < n; ++s) {
+    x.src = s; x.ord = 0;
+    successors(&m, locs + (size_t)s * net->nprocs, ints + (size_t)s * net->nints,
+               zones + (size_t)s * x.d2, L, U, qmask, emode, exp_emit, &x);
+  }
+  *out_n = x.n;
+  model_free(&m);
+  return x.n > cap ? HORA_E_OVERFLOW : HORA_OK;
+}
+int32_t orc_has_deadlock(const hora_net_desc* net, int32_t n, const int32_t* locs,
+                         const int32_t* ints, const int32_t* zones, int32_t* out) {
+  Model m;
+  int rc = model_build(net, &m);
+  if (rc) { model_free(&m); return rc; }
+  const int d2 = m.dim * m.dim;
+  for (int s = 0; s < n; ++s)
+    out[s] = state_has_deadlock(&m, locs + (size_t)s * net->nprocs, ints + (size_t)s * net->nints,
+                                zones + (size_t)s * d2);
+  model_free(&m);
+  return HORA_OK;
+}
+
+/* ============================================================================================
+ * Passed store (NetPassedT::add, include/hora/detail/passed_set.hpp:287-444)
+ * ============================================================================================ */
+typedef struct {
+  int32_t* zones;   /* node zone storage */
+  int* next; int* level; char* dead;
+  int nn, capn;
+  uint64_t* skey; int* shead; int* stouch;  /* open-addressing slots */
+  uint64_t smask; int nkeys;
+  int d2;
+  long nlive;
+} Store;
+static uint64_t mix64(uint64_t k) { return k * 0x9e3779b97f4a7c15ULL; }
+static void store_init(Store* S, int d2) {
+  memset(S, 0, sizeof *S);
+  S->d2 = d2;
+  S->smask = 1023;
+  S->skey = (uint64_t*)calloc(1024, sizeof(uint64_t));
+  S->shead = (int*)malloc(sizeof(int) * 1024);
+  S->stouch = (int*)calloc(1024, sizeof(int));
+  for (int i = 0; i < 1024; ++i) S->shead[i] = -2;   /* -2 free, -1 key present with no live node */
+}
+static void store_free(Store* S) {
+  free(S->zones); free(S->next); free(S->level); free(S->dead);
+  free(S->skey); free(S->shead); free(S->stouch);
+}
+static uint64_t slot_of(const Store* S, uint64_t k) {
+  uint64_t i = (mix64(k) >> 20) & S->smask;
+  while (S->shead[i] != -2 && S->skey[i] != k) i = (i + 1) & S->smask;
+  return i;
+}
+static void store_grow(Store* S) {
+  uint64_t ncap = (S->smask + 1) * 2, nmask = ncap - 1;
+  uint64_t* nk = (uint64_t*)calloc(ncap, sizeof(uint64_t));
+  int* nh = (int*)malloc(sizeof(int) * ncap);
+  int* nt = (int*)calloc(ncap, sizeof(int));
+  for (uint64_t i = 0; i < ncap; ++i) nh[i] = -2;
+  for (uint64_t i = 0; i <= S->smask; ++i)
+    if (S->shead[i] != -2) {
+      uint64_t j = (mix64(S->skey[i]) >> 20) & nmask;
+      while (nh[j] != -2) j = (j + 1) & nmask;
+      nk[j] = S->skey[i]; nh[j] = S->shead[i]; nt[j] = S->stouch[i];
+    }
+  free(S->skey); free(S->shead); free(S->stouch);
+  S->skey = nk; S->shead = nh; S->stouch = nt; S->smask = nmask;
+}
+static int store_node(Store* S, const int32_t* z, int level, int next) {
+  if (S->nn == S->capn) {
+    S->capn = S->capn ? S->capn * 2 : 1024;
+    S->zones = (int32_t*)realloc(S->zones, sizeof(int32_t) * S->d2 * (size_t)S->capn);
+    S->next = (int*)realloc(S->next, sizeof(int) * S->capn);
+    S->level = (int*)realloc(S->level, sizeof(int) * S->capn);
+    S->dead = (char*)realloc(S->dead, S->capn);
+  }
+  const int id = S->nn++;
+  memcpy(S->zones + (size_t)id * S->d2, z, sizeof(int32_t) * S->d2);
+  S->next[id] = next; S->level[id] = level; S->dead[id] = 0;
+  S->nlive++;
+  return id;
+}
+#define MERGE_SCAN 32   /* kMergeScan, include/hora/detail/engine_config.hpp:52 */
+/* Returns the new node id, or -1 when the zone was subsumed. `z` may be replaced by a hull. */
+static int store_add(Store* S, uint64_t k, int32_t* z, int level, int dim, const int32_t* Ls,
+                     const int32_t* Us, int64_t* probes) {
+  if ((uint64_t)(S->nkeys + 1) * 10 >= (S->smask + 1) * 7) store_grow(S);
+  const uint64_t si = slot_of(S, k);
+  if (S->shead[si] == -2) {
+    S->skey[si] = k;
+    S->shead[si] = store_node(S, z, level, -1);
+    S->nkeys++;
+    return S->shead[si];
+  }
+  const int d2 = S->d2;
+  /* live chain, newest first */
+  int nlv = 0, cap = 64;
+  int* live = (int*)malloc(sizeof(int) * cap);
+  for (int i = S->shead[si]; i >= 0; i = S->next[i])
+    if (!S->dead[i]) { if (nlv == cap) { cap *= 2; live = (int*)realloc(live, sizeof(int) * cap); } live[nlv++] = i; }
+  /* (1)+(2): dropped when simulated by a stored zone (plain inclusion implies simulation) */
+  for (int t = 0; t < nlv; ++t) {
+    if (probes) (*probes)++;
+    if (orc_dbm_alu_le(z, S->zones + (size_t)live[t] * d2, dim, Ls, Us)) { free(live); return -1; }
+  }
+  /* (3): retire stored zones simulated by z */
+  int w = 0;
+  for (int t = 0; t < nlv; ++t) {
+    if (orc_dbm_alu_le(S->zones + (size_t)live[t] * d2, z, dim, Ls, Us)) { S->dead[live[t]] = 1; S->nlive--; }
+    else live[w++] = live[t];
+  }
+  nlv = w;
+  /* (4): convex-union absorb within the newest MERGE_SCAN live zones, restarting after each */
+  for (int merged = 1; merged;) {
+    merged = 0;
+    for (int t = 0; t < nlv && t < MERGE_SCAN; ++t) {
+      if (orc_dbm_try_union(z, S->zones + (size_t)live[t] * d2, dim)) {
+        S->dead[live[t]] = 1; S->nlive--;
+        memmove(live + t, live + t + 1, sizeof(int) * (nlv - t - 1));
+        nlv--;
+        merged = 1;
+        break;
+      }
+    }
+  }
+  free(live);
+  /* (5): prepend */
+  const int id = store_node(S, z, level, S->shead[si]);
+  S->shead[si] = id;
+  return id;
+}
+
+/* ============================================================================================
+ * Level-synchronous BFS (reach_engine, src/reachability/engine.cpp:1410-1497, 2045-2200)
+ *
+ * Canonical order: a level's frontier is sorted by discrete key, and within a key lists the live
+ * zones stored at the previous level in chain order (newest first). Successors are inserted in
+ * (frontier position, emission ordinal) order -- the order the reference's --deterministic mode
+ * uses (engine.cpp:2148-2162) -- and the target test covers the whole level before the verdict.
+ * ============================================================================================ */
+typedef struct { uint64_t key; int node; } FItem;
+static int fcmp(const void* a, const void* b) {
+  const FItem* x = (const FItem*)a; const FItem* y = (const FItem*)b;
+  if (x->key != y->key) return x->key < y->key ? -1 : 1;
+  return 0;   /* qsort is not stable: ties are resolved by construction below */
+}
+typedef struct {
+  int32_t* locs; int32_t* ints; int32_t* zones;
+  int n, cap, np, ni, d2;
+} SuccBuf;
+static void sb_emit(void* c, const int32_t* locs, const int32_t* ints, const int32_t* zone) {
+  SuccBuf* b = (SuccBuf*)c;
+  if (b->n == b->cap) {
+    b->cap = b->cap ? b->cap * 2 : 1024;
+    b->locs = (int32_t*)realloc(b->locs, sizeof(int32_t) * b->np * (size_t)b->cap);
+    b->ints = (int32_t*)realloc(b->ints, sizeof(int32_t) * (b->ni ? b->ni : 1) * (size_t)b->cap);
+    b->zones = (int32_t*)realloc(b->zones, sizeof(int32_t) * b->d2 * (size_t)b->cap);
+  }
+  memcpy(b->locs + (size_t)b->n * b->np, locs, sizeof(int32_t) * b->np);
+  if (b->ni) memcpy(b->ints + (size_t)b->n * b->ni, ints, sizeof(int32_t) * b->ni);
+  memcpy(b->zones + (size_t)b->n * b->d2, zone, sizeof(int32_t) * b->d2);
+  b->n++;
+}
+
+typedef struct {
+  int kind;                      /* 0 target, 1 deadlock */
+  const hora_pred_desc* target;
+} Goal;
+static int goal_hit(const Model* m, const Goal* g, const int32_t* locs, const int32_t* ints,
+                    const int32_t* zone) {
+  if (g->kind == 1) return state_has_deadlock(m, locs, ints, zone);
+  const hora_pred_desc* t = g->target;
+  if (t->never) return 0;
+  for (int k = 0; k < t->nloc; ++k) if (locs[t->loc_req[2 * k]] != t->loc_req[2 * k + 1]) return 0;
+  if (!ints_ok(t->int_cond, t->nint, ints)) return 0;
+  int32_t z[64 * 64];
+  memcpy(z, zone, sizeof(int32_t) * m->dim * m->dim);
+  return apply_cons(z, m->dim, t->clk_cond, 0, t->nclk);
+}
+
+static double now_s(void) {
+  struct timespec ts; clock_gettime(CLOCK_MONOTONIC, &ts);
+  return ts.tv_sec + ts.tv_nsec * 1e-9;
+}
+
+/* The engine shared by E<> and deadlock. `collapse` selects the a_M bounds of deadlock_reachable
+ * (engine.cpp:2363-2405, the HORA_DL_MODE=m route). */
+static int32_t run_reach(const hora_net_desc* net, const Goal* goal, int collapse, hora_stats* st,
+                         int32_t* result) {
+  double t0 = now_s();
+  Model m;
+  int rc = model_build(net, &m);
+  if (rc) { model_free(&m); return rc; }
+  if (m.keybits > 63) { model_free(&m); return HORA_E_NOT_SUPPORTED; }
+  const int dim = m.dim, d2 = dim * dim, np = net->nprocs, ni = net->nints;
+  if (collapse) {
+    for (int c = 0; c < dim; ++c) m.L[c] = m.U[c] = imax(m.L[c], m.U[c]);
+    for (int k = 0; k < m.nlocs_total * dim; ++k) m.Lloc[k] = m.Uloc[k] = imax(m.Lloc[k], m.Uloc[k]);
+  }
+  /* query constants: extend_bounds (engine.cpp:1417-1419) and Lq/Uq, qmask (:1440-1455) */
+  uint8_t qmask[64] = {0};
+  int32_t Lq[64], Uq[64];
+  for (int c = 0; c < dim; ++c) Lq[c] = Uq[c] = ORC_ALU_NEG_INF;
+  if (goal->kind == 0) {
+    const hora_pred_desc* t = goal->target;
+    for (int k = 0; k < t->nclk; ++k) {
+      const int i = t->clk_cond[3 * k], j = t->clk_cond[3 * k + 1], v = r_bound(t->clk_cond[3 * k + 2]);
+      if (i > 0) qmask[i] = 1;
+      if (j > 0) qmask[j] = 1;
+      if (i > 0 && j == 0) { m.U[i] = imax(m.U[i], v); Uq[i] = imax(Uq[i], v); }
+      else if (i == 0 && j > 0) { m.L[j] = imax(m.L[j], -v); Lq[j] = imax(Lq[j], -v); }
+      else if (i > 0 && j > 0) {
+        const int a = v < 0 ? -v : v;
+        m.U[i] = imax(m.U[i], a); m.U[j] = imax(m.U[j], a); m.L[i] = imax(m.L[i], a); m.L[j] = imax(m.L[j], a);
+        Uq[i] = imax(Uq[i], a); Uq[j] = imax(Uq[j], a); Lq[i] = imax(Lq[i], a); Lq[j] = imax(Lq[j], a);
+      }
+    }
+  }
+  m.L[0] = m.U[0] = 0;
+  int emode = 0;
+  hora_stats S0;
+  memset(&S0, 0, sizeof S0);
+  /* initial state */
+  int32_t locs[64], ints[64], zone[64 * 64];
+  for (int p = 0; p < np; ++p) locs[p] = net->proc_init[p];
+  for (int v = 0; v < ni; ++v) ints[v] = net->int_init[v];
+  orc_dbm_init(zone, dim);
+  int found = 0;
+  Store S;
+  store_init(&S, d2);
+  SuccBuf B = {0};
+  B.np = np; B.ni = ni; B.d2 = d2;
+  FItem* fr = NULL; int nfr = 0, capfr = 0;
+  int32_t Ls[64], Us[64];
+  if (!close_succ_zone(&m, locs, ints, zone, qmask, m.L, m.U, emode) || orc_dbm_empty(zone, dim)) {
+    *result = 0;
+    goto done;
+  }
+  if (goal_hit(&m, goal, locs, ints, zone)) { found = 1; goto done; }
+  {
+    const uint64_t k0 = key_encode(&m, locs, ints);
+    int id = store_add(&S, k0, zone, 0, dim, m.L, m.U, NULL);
+    capfr = 16; fr = (FItem*)malloc(sizeof(FItem) * capfr);
+    fr[0].key = k0; fr[0].node = id; nfr = 1;
+  }
+  int level = 0;
+  while (nfr > 0) {
+    S0.explored += nfr;
+    ++level;
+    B.n = 0;
+    /* expand in frontier order; successor b's insertion order is its buffer position */
+    for (int f = 0; f < nfr; ++f) {
+      key_decode(&m, fr[f].key, locs, ints);
+      successors(&m, locs, ints, S.zones + (size_t)fr[f].node * d2, m.L, m.U, qmask, emode, sb_emit, &B);
+    }
+    S0.generated += B.n;
+    for (int b = 0; b < B.n && !found; ++b)
+      if (goal_hit(&m, goal, B.locs + (size_t)b * np, B.ints + (size_t)b * ni, B.zones + (size_t)b * d2)) found = 1;
+    if (found) { S0.levels = level; goto done; }
+    /* insert in order */
+    for (int b = 0; b < B.n; ++b) {
+      const int32_t* sl = B.locs + (size_t)b * np;
+      const uint64_t k = key_encode(&m, sl, B.ints + (size_t)b * ni);
+      for (int c = 1; c < dim; ++c) {
+        int32_t lv = ORC_ALU_NEG_INF, uv = ORC_ALU_NEG_INF;
+        for (int p = 0; p < np; ++p) {
+          const int gl = m.loc_base[p] + sl[p];
+          lv = imax(lv, m.Lloc[gl * dim + c]); uv = imax(uv, m.Uloc[gl * dim + c]);
+        }
+        Ls[c] = imax(lv, Lq[c]); Us[c] = imax(uv, Uq[c]);
+      }
+      Ls[0] = Us[0] = 0;
+      const uint64_t si = slot_of(&S, k);
+      int64_t pr = 0;
+      int id = store_add(&S, k, B.zones + (size_t)b * d2, level, dim, Ls, Us, &pr);
+      S0.probes += pr;
+      (void)si;
+      if (id >= 0) S.stouch[slot_of(&S, k)] = level;
+    }
+    /* next frontier: touched keys ascending, chain order within a key */
+    nfr = 0;
+    for (uint64_t i = 0; i <= S.smask; ++i) {
+      if (S.shead[i] == -2 || S.stouch[i] != level) continue;
+      for (int nd = S.shead[i]; nd >= 0; nd = S.next[nd]) {
+        if (S.dead[nd] || S.level[nd] != level) continue;
+        if (nfr == capfr) { capfr = capfr ? capfr * 2 : 16; fr = (FItem*)realloc(fr, sizeof(FItem) * capfr); }
+        fr[nfr].key = S.skey[i]; fr[nfr].node = nd; nfr++;
+      }
+    }
+    /* stable sort by key: collect per-key runs are contiguous already (one slot per key), so
+       sorting whole runs by key keeps the chain order inside each run */
+    {
+      /* sort run heads, then rebuild */
+      int nr = 0;
+      FItem* heads = (FItem*)malloc(sizeof(FItem) * (nfr ? nfr : 1));
+      int* start = (int*)malloc(sizeof(int) * (nfr + 1));
+      for (int f = 0; f < nfr; ++f)
+        if (f == 0 || fr[f].key != fr[f - 1].key) { heads[nr].key = fr[f].key; heads[nr].node = f; nr++; }
+      qsort(heads, nr, sizeof(FItem), fcmp);
+      FItem* out = (FItem*)malloc(sizeof(FItem) * (nfr ? nfr : 1));
+      int o = 0;
+      for (int r = 0; r < nr; ++r)
+        for (int f = heads[r].node; f < nfr && fr[f].key == heads[r].key; ++f) out[o++] = fr[f];
+      memcpy(fr, out, sizeof(FItem) * nfr);
+      free(out); free(heads); free(start);
+    }
+    /* adaptive switch to Extra_LU+ (engine.cpp:2178-2184) */
+    if (emode == 0 && S.nkeys && (double)S.nlive >= 4.0 * (double)S.nkeys) { emode = 1; S0.extrapolating = 1; }
+    S0.levels = level;
+  }
+done:
+  *result = found;
+  S0.stored = (uint64_t)S.nlive;
+  S0.keys = (uint64_t)S.nkeys;
+  S0.expanded = S0.explored;
+  S0.seconds = now_s() - t0;
+  if (st) *st = S0;
+  free(fr); free(B.locs); free(B.ints); free(B.zones);
+  store_free(&S);
+  model_free(&m);
+  return HORA_OK;
+}
+
+int32_t orc_reachable_net(const hora_net_desc* net, const hora_pred_desc* target, hora_stats* st,
+                          int32_t* result) {
+  Goal g = {0, target};
+  return run_reach(net, &g, 0, st, result);
+}
+int32_t orc_deadlock_reachable(const hora_net_desc* net, hora_stats* st, int32_t* result) {
+  Goal g = {1, NULL};
+  return run_reach(net, &g, 1, st, result);
+}
+
+int32_t orc_initial_state(const hora_net_desc* net, const uint8_t* qmask, int32_t* locs,
+                          int32_t* ints, int32_t* zone) {
+  Model m;
+  if (model_build(net, &m)) { model_free(&m); return 0; }
+  for (int p = 0; p < net->nprocs; ++p) locs[p] = net->proc_init[p];
+  for (int v = 0; v < net->nints; ++v) ints[v] = net->int_init[v];
+  orc_dbm_init(zone, m.dim);
+  int ok = close_succ_zone(&m, locs, ints, zone, qmask, m.L, m.U, 0) && !orc_dbm_empty(zone, m.dim);
+  model_free(&m);
+  return ok;
+}
+
+int32_t orc_leads_to(const hora_net_desc* net, const hora_pred_desc* p, const hora_pred_desc* q,
+                     hora_stats* st, int32_t* result) {
+  (void)net; (void)p; (void)q; (void)st; (void)result;
+  return HORA_E_NOT_SUPPORTED;
+}
