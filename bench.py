@@ -1,0 +1,242 @@
+"""Benchmark of the GB300 zone-graph engine: zone successors/s on the exhaustive-reachability
+workload (8 automata x 10 locations, 8 clocks = 9x9 DBM, 4 binary + 1 broadcast channel, 10%
+committed and 10% urgent locations, constants in [0,50], query A[] not deadlock).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--seed S]
+
+A step is one complete query (deadlock_reachable) through the C ABI with the network in host
+memory: the descriptor upload, every BFS level and the verdict readback are inside the step.
+  value  = generated successors / device time of the level loop (CUDA events on the engine's
+           stream, summed over the K timed steps)
+  e2e    = generated successors / wall time of the C-ABI calls (host buffers in, verdict out)
+The passed store of one query (hundreds of MB at this size) exceeds L2; L2 is also flushed by a
+256 MB write between steps. Under torchrun each rank runs an independent replica on its own GPU
+(the single-query path does not shard) and value sums successors over ranks / max time.
+
+--impl reference times the CPU restatement of the reference's algorithm (oracle/, single
+threaded: the reference's deadlock route is sequential code) on a bounded sample of the same
+workload, on this machine's host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD_CONFIG = 2
+WORKLOAD_SEED = int(os.environ.get("HORA_BENCH_SEED", "23"))
+CPU_SAMPLE_SECONDS = 20.0
+METRIC = "zone successors/s"
+UNIT = "successors/s"
+
+
+def workload(seed: int):
+    from ptctcl_gb300.generator import config_instance
+    return config_instance(WORKLOAD_CONFIG, seed)
+
+
+def sample_clocks(stop: threading.Event, out: list):
+    q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    try:
+        p = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits", "-lms", "200"],
+                             stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+    except OSError:
+        return
+    while not stop.is_set():
+        line = p.stdout.readline()
+        if not line:
+            break
+        out.append(line.strip())
+    p.terminate()
+
+
+def clock_summary(lines, dev_index: int):
+    sm, mx, reasons = [], [], set()
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    for ln in lines:
+        f = [x.strip() for x in ln.split(",")]
+        if len(f) < 9 or f[0] != str(dev_index):
+            continue
+        try:
+            sm.append(float(f[1])); mx.append(float(f[2]))
+        except ValueError:
+            continue
+        for n, v in zip(names, f[5:9]):
+            if v.lower().startswith("active"):
+                reasons.add(n)
+    if not sm:
+        return None
+    return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return json.load(fh), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def cpu_baseline(net, seconds: float):
+    from oracle import pyoracle
+    pyoracle.set_time_limit(seconds)
+    try:
+        t = time.perf_counter()
+        _, st = pyoracle.deadlock_reachable(net)
+        dt = time.perf_counter() - t
+    finally:
+        pyoracle.set_time_limit(0)
+    return {"value": st["generated"] / dt if dt > 0 else 0.0, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"{'first ' + str(st['levels']) + ' BFS levels' if st['status'] else 'whole query'} of "
+                      f"the workload, {st['generated']} successors in {dt:.1f} s"}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    net, kind, p, q = workload(args.seed)
+    vals, samples = [], []
+    for _ in range(args.warmup):
+        cpu_baseline(net, min(2.0, CPU_SAMPLE_SECONDS))
+    t_all = time.perf_counter()
+    for _ in range(args.steps):
+        b = cpu_baseline(net, CPU_SAMPLE_SECONDS)
+        vals.append(b["value"]); samples.append(b["sample"])
+    dt = time.perf_counter() - t_all
+    v = statistics.mean(vals) if vals else 0.0
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * dt / max(1, args.steps), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+            "config": {"workload": f"config2 A[] not deadlock, seed {args.seed}", "sample": samples[-1] if samples else ""},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
+                             "sample": samples[-1] if samples else ""},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--seed", type=int, default=WORKLOAD_SEED)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+
+    import torch
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    from ptctcl_gb300 import capi, engine
+    from ptctcl_gb300.engine import Backend, ReachStats
+    capi.load()
+    net, kind, p, q = workload(args.seed + rank * 0)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    verdict = None
+    for _ in range(args.warmup):
+        verdict = engine.deadlock_reachable(net, Backend.Cuda, ReachStats())
+    stop, clk = threading.Event(), []
+    th = threading.Thread(target=sample_clocks, args=(stop, clk), daemon=True)
+    th.start()
+    stats = []
+    walls = []
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        st = ReachStats()
+        tw = time.perf_counter()
+        v = engine.deadlock_reachable(net, Backend.Cuda, st)
+        walls.append(time.perf_counter() - tw)
+        assert verdict is None or v == verdict
+        stats.append(st)
+    barrier()
+    total = time.perf_counter() - t0
+    stop.set()
+    gen = sum(s.generated for s in stats)
+    dev = sum(s.device_seconds for s in stats)
+    wall = sum(walls)
+    vals = torch.tensor([gen, dev, wall, total], dtype=torch.float64, device="cuda")
+    if dist is not None:
+        g = vals.clone(); dist.all_reduce(g, op=dist.ReduceOp.SUM)
+        m = vals.clone(); dist.all_reduce(m, op=dist.ReduceOp.MAX)
+        gen_all, dev_max, wall_max, total_max = g[0].item(), m[1].item(), m[2].item(), m[3].item()
+    else:
+        gen_all, dev_max, wall_max, total_max = gen, dev, wall, total
+    if rank != 0:
+        dist.destroy_process_group()
+        return
+    s0 = stats[-1]
+    peaks, peak_kind = measured_peaks()
+    # dominant kernel family and its algorithmic bytes per launch (9x9 int32 zones)
+    d2 = net.dim * net.dim * 4
+    line = {
+        "metric": METRIC, "value": gen_all / dev_max if dev_max > 0 else 0.0, "unit": UNIT,
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * total_max / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+        "config": {"workload": f"config2: 8 automata x 10 locations, 8 clocks (9x9 DBM), 4 binary + 1 broadcast "
+                               f"channels, A[] not deadlock, seed {args.seed}",
+                   "stored_zones": s0.stored, "successors_per_query": s0.generated, "levels": s0.levels,
+                   "verdict_deadlock_reachable": bool(verdict), "l2": "flushed (256 MB write) between steps; "
+                   "passed store exceeds L2", "parallelism": f"replicas x{world}"},
+        "e2e": {"value": gen_all / wall_max if wall_max > 0 else 0.0, "unit": UNIT,
+                "h2d_bytes_per_step": int(s0.h2d_bytes), "d2h_bytes_per_step": int(s0.d2h_bytes)},
+        "gpu_launches": int(sum(s.kernel_launches for s in stats)),
+    }
+    kern = s0.kernels
+    dom = max(kern, key=lambda k: kern[k]["seconds"])
+    kd = kern[dom]
+    calls = max(1, kd["calls"])
+    per_launch_s = kd["seconds"] / calls
+    if dom == "expand":
+        algo = d2 * (s0.explored + s0.generated) / calls
+    elif dom in ("probe", "merge"):
+        algo = d2 * (s0.generated + s0.probes) / calls
+    else:
+        algo = d2 * s0.generated / calls
+    ach = algo / per_launch_s / 1e9 if per_launch_s > 0 else 0.0
+    line["roofline"] = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peaks.get("hbm_gbs"),
+                        "unit": "GB/s", "frac": ach / peaks.get("hbm_gbs", 1.0), "traffic": None,
+                        "peak_source": peak_kind,
+                        "kernel_time_share": {k: round(v["seconds"] / max(1e-12, sum(x["seconds"] for x in kern.values())), 4)
+                                              for k, v in kern.items()}}
+    cs = clock_summary(clk, local)
+    if cs:
+        line["clocks"] = cs
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(net, CPU_SAMPLE_SECONDS)
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

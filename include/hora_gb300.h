@@ -41,6 +41,12 @@ extern "C" {
 
 #define HORA_GB_ABI_VERSION 1
 
+#if defined(__GNUC__)
+#define HORA_GB_API __attribute__((visibility("default")))
+#else
+#define HORA_GB_API
+#endif
+
 /* ---- status codes ------------------------------------------------------------------------- */
 enum {
   HORA_OK = 0,
@@ -147,31 +153,37 @@ typedef struct hora_stats {
   double   device_seconds; /* time on the device, CUDA events around the level loop */
   int32_t  extrapolating; /* 1 if the adaptive switch to Extra_LU+ fired */
   int32_t  status;       /* HORA_OK or an error code for this query */
+  /* per kernel family, CUDA-event time on the engine's stream and launch count:
+   * [0] expand, [1] probe, [2] deadlock test, [3] group, [4] merge, [5] other (init, rehash) */
+  double   kernel_seconds[6];
+  uint64_t kernel_calls[6];
+  uint64_t h2d_bytes;    /* host-to-device bytes moved by the call (descriptor, counters) */
+  uint64_t d2h_bytes;    /* device-to-host bytes moved by the call (counters, verdict) */
 } hora_stats;
 
 /* ---- errors and device ---------------------------------------------------------------------- */
 
 /* Thread-local text of the last failure (empty string when none). */
-const char* hora_gb_last_error(void);
+HORA_GB_API const char* hora_gb_last_error(void);
 /* ABI version compiled into the library. */
-int32_t hora_gb_abi_version(void);
+HORA_GB_API int32_t hora_gb_abi_version(void);
 /* Number of visible CUDA devices (0 when none); returns a status. */
-int32_t hora_gb_device_count(int32_t* count);
+HORA_GB_API int32_t hora_gb_device_count(int32_t* count);
 
 /* ---- single-query entry points ---------------------------------------------------------------- */
 
 /* E<> target. On HORA_OK, *result = 1 iff a symbolic state matching target is reachable. */
-int32_t hora_gb_reachable_net(const hora_net_desc* net, const hora_pred_desc* target, int32_t backend,
+HORA_GB_API int32_t hora_gb_reachable_net(const hora_net_desc* net, const hora_pred_desc* target, int32_t backend,
                               hora_stats* stats, int32_t* result);
 
 /* Is a state with a deadlocked valuation reachable?  A[] not deadlock holds iff *result == 0.
  * `cancel` may be null; when non-null it is polled between BFS levels and a non-zero value ends the
  * search with HORA_E_CANCELLED. */
-int32_t hora_gb_deadlock_reachable(const hora_net_desc* net, int32_t backend, hora_stats* stats,
+HORA_GB_API int32_t hora_gb_deadlock_reachable(const hora_net_desc* net, int32_t backend, hora_stats* stats,
                                    const volatile int32_t* cancel, int32_t* result);
 
 /* p --> q. On HORA_OK, *result = 1 iff the property holds. */
-int32_t hora_gb_leads_to(const hora_net_desc* net, const hora_pred_desc* p, const hora_pred_desc* q,
+HORA_GB_API int32_t hora_gb_leads_to(const hora_net_desc* net, const hora_pred_desc* p, const hora_pred_desc* q,
                          int32_t backend, hora_stats* stats, int32_t* result);
 
 /* Successor pipeline on host buffers, for differential testing against a CPU implementation.
@@ -182,14 +194,14 @@ int32_t hora_gb_leads_to(const hora_net_desc* net, const hora_pred_desc* p, cons
  * out_ord[k] emission ordinal within its source, out_locs, out_ints, out_zones. *out_n receives the
  * successor count; when it exceeds cap only the first cap are written and HORA_E_OVERFLOW is
  * returned. */
-int32_t hora_gb_expand(const hora_net_desc* net, int32_t n, const int32_t* locs, const int32_t* ints,
+HORA_GB_API int32_t hora_gb_expand(const hora_net_desc* net, int32_t n, const int32_t* locs, const int32_t* ints,
                        const int32_t* zones, const int32_t* L, const int32_t* U, const uint8_t* qmask,
                        int32_t emode, int64_t cap, int32_t* out_src, int32_t* out_ord,
                        int32_t* out_locs, int32_t* out_ints, int32_t* out_zones, int64_t* out_n);
 
 /* Deadlock predicate on host buffers (state_has_deadlock, src/reachability/deadlock.cpp:74-270):
  * out[k] = 1 iff state k contains a deadlocked valuation. */
-int32_t hora_gb_has_deadlock(const hora_net_desc* net, int32_t n, const int32_t* locs,
+HORA_GB_API int32_t hora_gb_has_deadlock(const hora_net_desc* net, int32_t n, const int32_t* locs,
                              const int32_t* ints, const int32_t* zones, int32_t* out);
 
 /* ---- batched form ----------------------------------------------------------------------------- */
@@ -198,7 +210,7 @@ int32_t hora_gb_has_deadlock(const hora_net_desc* net, int32_t n, const int32_t*
  * result in the single-query convention of the query's kind (reach: reachable; deadlock: deadlock
  * reachable; leads-to: holds); stats (may be null) one record per instance. Returns HORA_OK when
  * every instance ran; per-instance failures are reported in stats[k].status and verdicts[k] = -1. */
-int32_t hora_gb_batch_run(int32_t n, const hora_net_desc* nets, const hora_query_desc* queries,
+HORA_GB_API int32_t hora_gb_batch_run(int32_t n, const hora_net_desc* nets, const hora_query_desc* queries,
                           int32_t* verdicts, hora_stats* stats);
 
 /* ---- serving form ------------------------------------------------------------------------------ */
@@ -207,18 +219,18 @@ typedef struct hora_server hora_server;
 
 /* budget_bytes: device memory the passed/waiting stores of admitted requests may hold together;
  * max_inflight: instances interleaved on the device at once. */
-int32_t hora_gb_server_create(uint64_t budget_bytes, int32_t max_inflight, hora_server** out);
+HORA_GB_API int32_t hora_gb_server_create(uint64_t budget_bytes, int32_t max_inflight, hora_server** out);
 /* Queue a request; the descriptors are copied. *ticket identifies it. A request whose own store
  * estimate exceeds the whole budget is rejected with HORA_E_BUDGET. */
-int32_t hora_gb_server_submit(hora_server* s, const hora_net_desc* net, const hora_query_desc* q,
+HORA_GB_API int32_t hora_gb_server_submit(hora_server* s, const hora_net_desc* net, const hora_query_desc* q,
                               int64_t* ticket);
 /* Advance the device by one interleaved step over every admitted request, admitting queued ones as
  * slots and budget free up. *active receives the number still queued or running. */
-int32_t hora_gb_server_step(hora_server* s, int32_t* active);
+HORA_GB_API int32_t hora_gb_server_step(hora_server* s, int32_t* active);
 /* Fetch a finished request: *done = 1 and verdict/stats filled once it has finished. */
-int32_t hora_gb_server_poll(hora_server* s, int64_t ticket, int32_t* done, int32_t* verdict,
+HORA_GB_API int32_t hora_gb_server_poll(hora_server* s, int64_t ticket, int32_t* done, int32_t* verdict,
                             hora_stats* stats);
-int32_t hora_gb_server_destroy(hora_server* s);
+HORA_GB_API int32_t hora_gb_server_destroy(hora_server* s);
 
 #ifdef __cplusplus
 }

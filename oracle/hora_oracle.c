@@ -213,6 +213,10 @@ typedef struct {
   int keybits;
   int has_urgent_chan;
   int has_diag;
+  /* optional restriction to !q (leads-to): at states matching q's discrete part the successor
+     must stay outside q's clock region, which is a single atom (convex complement) */
+  const hora_pred_desc* avoid;   /* q, or NULL */
+  int32_t avoid_neg[3];          /* complement of q's clock atom */
 } Model;
 
 static int ceil_log2(long n) { int b = 0; while ((1L << b) < n) ++b; return b; }
@@ -492,12 +496,21 @@ static void reset_inactive(const Model* m, const int32_t* locs, int32_t* z, cons
 }
 /* close_succ_zone without the avoid-set (semantics.hpp:522-568). Returns 0 when the target
  * invariant is unsatisfiable; the caller tests emptiness. */
+static int ints_ok(const int32_t* atoms, int na, const int32_t* ints);
+static int disc_match(const hora_pred_desc* t, const int32_t* locs, const int32_t* ints);
+/* Restrict z to the complement of q where q's discrete part holds; 0 when nothing is left. */
+static int avoid_cut(const Model* m, int32_t* z, const int32_t* tl, const int32_t* ti) {
+  if (!m->avoid || !disc_match(m->avoid, tl, ti)) return 1;
+  if (m->avoid->nclk == 0) return 0;   /* a purely discrete q: the whole state is in q */
+  return orc_dbm_constrain(z, m->dim, m->avoid_neg[0], m->avoid_neg[1], m->avoid_neg[2]);
+}
 static int close_succ_zone(const Model* m, const int32_t* tl, const int32_t* ti, int32_t* z,
                            const uint8_t* qmask, const int32_t* L, const int32_t* U, int emode) {
   if (!apply_inv(m, z, tl)) return 0;
+  if (!avoid_cut(m, z, tl, ti)) return 0;
   int c, u;
   frozen_flags(m, tl, ti, &c, &u);
-  if (!c && !u) { orc_dbm_delay(z, m->dim); apply_inv(m, z, tl); }
+  if (!c && !u) { orc_dbm_delay(z, m->dim); apply_inv(m, z, tl); avoid_cut(m, z, tl, ti); }
   reset_inactive(m, tl, z, qmask);
   if (emode == 1) orc_dbm_extrap_lu_plus(z, m->dim, L, U);
   return 1;
@@ -1059,6 +1072,9 @@ static int goal_hit(const Model* m, const Goal* g, const int32_t* locs, const in
   return apply_cons(z, m->dim, t->clk_cond, 0, t->nclk);
 }
 
+static double g_time_limit = 0.0;   /* seconds; 0 = none. Bounds a CPU-baseline sample. */
+void orc_set_time_limit(double seconds) { g_time_limit = seconds; }
+
 static double now_s(void) {
   struct timespec ts; clock_gettime(CLOCK_MONOTONIC, &ts);
   return ts.tv_sec + ts.tv_nsec * 1e-9;
@@ -1185,6 +1201,7 @@ static int32_t run_reach(const hora_net_desc* net, const Goal* goal, int collaps
       memcpy(fr, out, sizeof(FItem) * nfr);
       free(out); free(heads); free(start);
     }
+    if (g_time_limit > 0 && now_s() - t0 > g_time_limit) { S0.levels = level; S0.status = HORA_E_TIMEOUT; goto done; }
     /* adaptive switch to Extra_LU+ (engine.cpp:2178-2184) */
     if (emode == 0 && S.nkeys && (double)S.nlive >= 4.0 * (double)S.nkeys) { emode = 1; S0.extrapolating = 1; }
     S0.levels = level;
@@ -1195,6 +1212,7 @@ done:
   S0.keys = (uint64_t)S.nkeys;
   S0.expanded = S0.explored;
   S0.seconds = now_s() - t0;
+  S0.probes += 0;
   if (st) *st = S0;
   free(fr); free(B.locs); free(B.ints); free(B.zones);
   store_free(&S);
@@ -1224,8 +1242,308 @@ int32_t orc_initial_state(const hora_net_desc* net, const uint8_t* qmask, int32_
   return ok;
 }
 
+/* ============================================================================================
+ * Leads-to, p --> q  (leads_to_clocks / leads_to_otf, src/liveness/api.cpp:655-733)
+ *
+ * p --> q fails iff some reachable state satisfying p and not q starts a maximal run that never
+ * satisfies q. This restatement decides that with the same three ingredients as the reference's
+ * backward sweep (src/liveness/fixpoint.cpp:48-977): the region of !q-states, the end-of-run set
+ * (stop_set, src/liveness/construction.cpp:1200-1239), and the greatest fixpoint
+ * W = W /\ (NoSucc \/ Pre(W)):
+ *
+ *  1. the reachable states, explored with the deadlock-sound a_M bisimulation bounds (every query
+ *     constant folded in), give the roots: their p-part, cut to !q;
+ *  2. from the roots, the exact zone graph of the network restricted to !q (q's clock atom is a
+ *     single constraint, so its complement is convex and is adjoined to the invariant exactly
+ *     where q's discrete part holds) is built with Extra_M+ for finiteness and exact-zone
+ *     deduplication, so the graph is post-stable: every valuation of a node has a predecessor in
+ *     each of its source nodes;
+ *  3. on that graph, node-level emptiness of W is exact: W starts as every node and repeatedly
+ *     loses the nodes with no stop valuation and no successor left in W.
+ * ============================================================================================ */
+static int disc_match(const hora_pred_desc* t, const int32_t* locs, const int32_t* ints) {
+  for (int k = 0; k < t->nloc; ++k) if (locs[t->loc_req[2 * k]] != t->loc_req[2 * k + 1]) return 0;
+  return ints_ok(t->int_cond, t->nint, ints);
+}
+static int has_upper_invariant(const Model* m, const int32_t* locs) {
+  const hora_net_desc* n = m->n;
+  for (int p = 0; p < n->nprocs; ++p) {
+    const int gl = m->loc_base[p] + locs[p];
+    for (int c = n->loc_inv_off[gl]; c < n->loc_inv_off[gl + 1]; ++c)
+      if (n->cons[3 * c] > 0 && n->cons[3 * c + 1] == 0 && n->cons[3 * c + 2] < ORC_INF) return 1;
+  }
+  return 0;
+}
+static int all_unbounded(const int32_t* z, int dim) {
+  for (int i = 1; i < dim; ++i) if (z[i * dim] != ORC_INF) return 0;
+  return 1;
+}
+/* time_diverges (construction.cpp:1097-1136): every clock unbounded after a delay inside the
+ * invariant -- and, when `restricted`, inside !q as well. */
+static int time_diverges(const Model* m, const int32_t* locs, const int32_t* ints, const int32_t* zone, int restricted) {
+  const int dim = m->dim;
+  if (m->n->nclocks == 0 || has_upper_invariant(m, locs)) return 0;
+  int c, u;
+  frozen_flags(m, locs, ints, &c, &u);
+  if (c || u) return 0;
+  int32_t z[64 * 64];
+  memcpy(z, zone, sizeof(int32_t) * dim * dim);
+  orc_dbm_delay(z, dim);
+  if (!apply_inv(m, z, locs) || orc_dbm_empty(z, dim) || !all_unbounded(z, dim)) return 0;
+  if (restricted && m->avoid && disc_match(m->avoid, locs, ints)) {
+    memcpy(z, zone, sizeof(int32_t) * dim * dim);
+    if (!avoid_cut(m, z, locs, ints)) return 0;
+    orc_dbm_delay(z, dim);
+    if (!apply_inv(m, z, locs) || !avoid_cut(m, z, locs, ints) || orc_dbm_empty(z, dim)) return 0;
+    return all_unbounded(z, dim);
+  }
+  return 1;
+}
+/* orig_time_open (construction.cpp:1163-1177): can time run away here in the unrestricted system? */
+static int orig_time_open(const Model* m, const int32_t* locs, const int32_t* ints) {
+  const int dim = m->dim;
+  if (m->n->nclocks == 0 || has_upper_invariant(m, locs)) return 0;
+  int c, u;
+  frozen_flags(m, locs, ints, &c, &u);
+  if (c || u) return 0;
+  int32_t z[64 * 64];
+  for (int i = 0; i < dim; ++i)
+    for (int j = 0; j < dim; ++j) z[i * dim + j] = (i == j || i == 0) ? ORC_ZERO_LE : ORC_INF;
+  orc_dbm_delay(z, dim);
+  if (!apply_inv(m, z, locs)) return 0;
+  return all_unbounded(z, dim);
+}
+
+/* Exact-zone dedup insert: returns the node holding zone z under key k (new or existing). */
+static int store_find_or_add_exact(Store* S, uint64_t k, const int32_t* z, int level, int* is_new) {
+  if ((uint64_t)(S->nkeys + 1) * 10 >= (S->smask + 1) * 7) store_grow(S);
+  const uint64_t si = slot_of(S, k);
+  *is_new = 0;
+  if (S->shead[si] == -2) {
+    S->skey[si] = k;
+    S->shead[si] = store_node(S, z, level, -1);
+    S->nkeys++;
+    *is_new = 1;
+    return S->shead[si];
+  }
+  for (int i = S->shead[si]; i >= 0; i = S->next[i])
+    if (memcmp(S->zones + (size_t)i * S->d2, z, sizeof(int32_t) * S->d2) == 0) return i;
+  const int id = store_node(S, z, level, S->shead[si]);
+  S->shead[si] = id;
+  *is_new = 1;
+  return id;
+}
+
+typedef struct { int* a; int n, cap; } IVec;
+static void iv_push(IVec* v, int x) {
+  if (v->n == v->cap) { v->cap = v->cap ? v->cap * 2 : 256; v->a = (int*)realloc(v->a, sizeof(int) * v->cap); }
+  v->a[v->n++] = x;
+}
+
+typedef struct { IVec* succ_keys_unused; int count; } CountCtx;
+static void count_emit(void* c, const int32_t* l, const int32_t* i, const int32_t* z) {
+  (void)l; (void)i; (void)z;
+  ((CountCtx*)c)->count++;
+}
+
 int32_t orc_leads_to(const hora_net_desc* net, const hora_pred_desc* p, const hora_pred_desc* q,
                      hora_stats* st, int32_t* result) {
-  (void)net; (void)p; (void)q; (void)st; (void)result;
-  return HORA_E_NOT_SUPPORTED;
+  double t0 = now_s();
+  if (q->nclk > 1) return HORA_E_NOT_SUPPORTED;   /* !q must be convex: at most one clock atom */
+  Model m;
+  int rc = model_build(net, &m);
+  if (rc) { model_free(&m); return rc; }
+  if (m.keybits > 63 || m.has_diag) { model_free(&m); return HORA_E_NOT_SUPPORTED; }
+  const int dim = m.dim, d2 = dim * dim, np = net->nprocs, ni = net->nints;
+  /* bounds: query constants folded in, then collapsed to a_M (L = U = max) */
+  uint8_t qmask[64] = {0};
+  int32_t Lq[64], Uq[64];
+  for (int c = 0; c < dim; ++c) Lq[c] = Uq[c] = ORC_ALU_NEG_INF;
+  const hora_pred_desc* preds[2] = {p, q};
+  for (int w = 0; w < 2; ++w)
+    for (int k = 0; k < preds[w]->nclk; ++k) {
+      const int i = preds[w]->clk_cond[3 * k], j = preds[w]->clk_cond[3 * k + 1];
+      const int v = r_bound(preds[w]->clk_cond[3 * k + 2]);
+      if (i > 0) qmask[i] = 1;
+      if (j > 0) qmask[j] = 1;
+      const int a = v < 0 ? -v : v;
+      const int x = i > 0 ? i : j;
+      m.L[x] = imax(m.L[x], a); m.U[x] = imax(m.U[x], a);
+      Lq[x] = imax(Lq[x], a); Uq[x] = imax(Uq[x], a);
+    }
+  for (int c = 0; c < dim; ++c) { m.L[c] = m.U[c] = imax(m.L[c], m.U[c]); Lq[c] = Uq[c] = imax(Lq[c], Uq[c]); }
+  for (int k = 0; k < m.nlocs_total * dim; ++k) m.Lloc[k] = m.Uloc[k] = imax(m.Lloc[k], m.Uloc[k]);
+  m.L[0] = m.U[0] = 0;
+  hora_stats S0;
+  memset(&S0, 0, sizeof S0);
+  int32_t locs[64], ints[64], zone[64 * 64], z2[64 * 64], Ls[64], Us[64];
+  /* ---- phase 1: reachable states under a_M subsumption ---- */
+  Store R;
+  store_init(&R, d2);
+  SuccBuf B = {0};
+  B.np = np; B.ni = ni; B.d2 = d2;
+  FItem* fr = NULL; int nfr = 0, capfr = 0;
+  int emode = 0;
+  for (int pp = 0; pp < np; ++pp) locs[pp] = net->proc_init[pp];
+  for (int v = 0; v < ni; ++v) ints[v] = net->int_init[v];
+  orc_dbm_init(zone, dim);
+  int violated = 0;
+  if (close_succ_zone(&m, locs, ints, zone, qmask, m.L, m.U, 0) && !orc_dbm_empty(zone, dim)) {
+    const uint64_t k0 = key_encode(&m, locs, ints);
+    int id = store_add(&R, k0, zone, 0, dim, m.L, m.U, NULL);
+    capfr = 16; fr = (FItem*)malloc(sizeof(FItem) * capfr);
+    fr[0].key = k0; fr[0].node = id; nfr = 1;
+  }
+  int level = 0;
+  while (nfr > 0) {
+    S0.explored += nfr;
+    ++level;
+    B.n = 0;
+    for (int f = 0; f < nfr; ++f) {
+      key_decode(&m, fr[f].key, locs, ints);
+      successors(&m, locs, ints, R.zones + (size_t)fr[f].node * d2, m.L, m.U, qmask, emode, sb_emit, &B);
+    }
+    S0.generated += B.n;
+    for (int b = 0; b < B.n; ++b) {
+      const int32_t* sl = B.locs + (size_t)b * np;
+      const uint64_t k = key_encode(&m, sl, B.ints + (size_t)b * ni);
+      for (int c = 1; c < dim; ++c) {
+        int32_t lv = ORC_ALU_NEG_INF;
+        for (int pp = 0; pp < np; ++pp) lv = imax(lv, m.Lloc[(m.loc_base[pp] + sl[pp]) * dim + c]);
+        Ls[c] = Us[c] = imax(lv, Lq[c]);
+      }
+      Ls[0] = Us[0] = 0;
+      int id = store_add(&R, k, B.zones + (size_t)b * d2, level, dim, Ls, Us, NULL);
+      if (id >= 0) R.stouch[slot_of(&R, k)] = level;
+    }
+    nfr = 0;
+    for (uint64_t i = 0; i <= R.smask; ++i) {
+      if (R.shead[i] == -2 || R.stouch[i] != level) continue;
+      for (int nd = R.shead[i]; nd >= 0; nd = R.next[nd]) {
+        if (R.dead[nd] || R.level[nd] != level) continue;
+        if (nfr == capfr) { capfr = capfr ? capfr * 2 : 16; fr = (FItem*)realloc(fr, sizeof(FItem) * capfr); }
+        fr[nfr].key = R.skey[i]; fr[nfr].node = nd; nfr++;
+      }
+    }
+    if (emode == 0 && R.nkeys && (double)R.nlive >= 4.0 * (double)R.nkeys) emode = 1;
+  }
+  /* ---- roots: the p-part of every stored zone, cut to !q ---- */
+  m.avoid = q;
+  if (q->nclk == 1) {
+    m.avoid_neg[0] = q->clk_cond[1]; m.avoid_neg[1] = q->clk_cond[0]; m.avoid_neg[2] = r_negate(q->clk_cond[2]);
+  }
+  Store G;
+  store_init(&G, d2);
+  IVec roots = {0}, efrom = {0}, eto = {0};
+  nfr = 0;
+  for (uint64_t i = 0; i <= R.smask; ++i) {
+    if (R.shead[i] == -2) continue;
+    key_decode(&m, R.skey[i], locs, ints);
+    if (!disc_match(p, locs, ints)) continue;
+    for (int nd = R.shead[i]; nd >= 0; nd = R.next[nd]) {
+      if (R.dead[nd]) continue;
+      memcpy(z2, R.zones + (size_t)nd * d2, sizeof(int32_t) * d2);
+      if (!apply_cons(z2, dim, p->clk_cond, 0, p->nclk)) continue;
+      if (!avoid_cut(&m, z2, locs, ints) || orc_dbm_empty(z2, dim)) continue;
+      int is_new;
+      const int id = store_find_or_add_exact(&G, R.skey[i], z2, 0, &is_new);
+      if (is_new) {
+        iv_push(&roots, id);
+        if (nfr == capfr) { capfr = capfr ? capfr * 2 : 16; fr = (FItem*)realloc(fr, sizeof(FItem) * capfr); }
+        fr[nfr].key = R.skey[i]; fr[nfr].node = id; nfr++;
+      }
+    }
+  }
+  store_free(&R);
+  /* ---- phase 2: exact zone graph of the !q-restricted network from the roots ---- */
+  IVec nodekey_unused = {0};
+  (void)nodekey_unused;
+  uint64_t* nkey = NULL; int nkcap = 0;
+  level = 0;
+  while (nfr > 0) {
+    S0.explored += nfr;
+    ++level;
+    FItem* nxt = NULL; int nn = 0, capn = 0;
+    for (int f = 0; f < nfr; ++f) {
+      key_decode(&m, fr[f].key, locs, ints);
+      B.n = 0;
+      successors(&m, locs, ints, G.zones + (size_t)fr[f].node * d2, m.L, m.U, qmask, 1, sb_emit, &B);
+      S0.generated += B.n;
+      for (int b = 0; b < B.n; ++b) {
+        const uint64_t k = key_encode(&m, B.locs + (size_t)b * np, B.ints + (size_t)b * ni);
+        int is_new;
+        const int id = store_find_or_add_exact(&G, k, B.zones + (size_t)b * d2, level, &is_new);
+        iv_push(&efrom, fr[f].node);
+        iv_push(&eto, id);
+        if (is_new) {
+          if (nn == capn) { capn = capn ? capn * 2 : 16; nxt = (FItem*)realloc(nxt, sizeof(FItem) * capn); }
+          nxt[nn].key = k; nxt[nn].node = id; nn++;
+        }
+      }
+    }
+    free(fr);
+    fr = nxt; nfr = nn; capfr = capn;
+  }
+  /* node keys, for the stop sets */
+  nkcap = G.nn;
+  nkey = (uint64_t*)malloc(sizeof(uint64_t) * (nkcap ? nkcap : 1));
+  for (uint64_t i = 0; i <= G.smask; ++i)
+    if (G.shead[i] != -2)
+      for (int nd = G.shead[i]; nd >= 0; nd = G.next[nd]) nkey[nd] = G.skey[i];
+  /* ---- stop sets (stop_set, construction.cpp:1200-1239) ---- */
+  char* stop = (char*)calloc(G.nn ? G.nn : 1, 1);
+  char* inW = (char*)malloc(G.nn ? G.nn : 1);
+  const hora_pred_desc* av = m.avoid;
+  for (int u = 0; u < G.nn; ++u) {
+    key_decode(&m, nkey[u], locs, ints);
+    const int32_t* zu = G.zones + (size_t)u * d2;
+    m.avoid = NULL;   /* deadlock and any-successor are judged in the unrestricted network */
+    if (q->nclk == 0) {
+      CountCtx cc = {NULL, 0};
+      successors(&m, locs, ints, zu, m.L, m.U, qmask, 1, count_emit, &cc);
+      stop[u] = cc.count == 0 || time_diverges(&m, locs, ints, zu, 0) || state_has_deadlock(&m, locs, ints, zu);
+    } else {
+      m.avoid = av;
+      if (time_diverges(&m, locs, ints, zu, 1)) stop[u] = 1;
+      else if (orig_time_open(&m, locs, ints)) stop[u] = 0;
+      else { m.avoid = NULL; stop[u] = state_has_deadlock(&m, locs, ints, zu) ? 1 : 0; }
+    }
+    m.avoid = av;
+    inW[u] = 1;
+  }
+  /* ---- greatest fixpoint over the graph (CSR by source) ---- */
+  int* off = (int*)calloc(G.nn + 1, sizeof(int));
+  int* dst = (int*)malloc(sizeof(int) * (efrom.n ? efrom.n : 1));
+  for (int e = 0; e < efrom.n; ++e) off[efrom.a[e] + 1]++;
+  for (int u = 0; u < G.nn; ++u) off[u + 1] += off[u];
+  {
+    int* fill = (int*)calloc(G.nn ? G.nn : 1, sizeof(int));
+    for (int e = 0; e < efrom.n; ++e) dst[off[efrom.a[e]] + fill[efrom.a[e]]++] = eto.a[e];
+    free(fill);
+  }
+  for (int changed = 1; changed;) {
+    changed = 0;
+    S0.gfp_iters++;
+    for (int u = 0; u < G.nn; ++u) {
+      if (!inW[u] || stop[u]) continue;
+      int any = 0;
+      for (int e = off[u]; e < off[u + 1] && !any; ++e) any = inW[dst[e]];
+      if (!any) { inW[u] = 0; changed = 1; }
+    }
+  }
+  for (int r = 0; r < roots.n && !violated; ++r) violated = inW[roots.a[r]];
+  S0.stored = (uint64_t)G.nn;
+  S0.keys = (uint64_t)G.nkeys;
+  S0.levels = (uint64_t)level;
+  S0.pre_calls = (uint64_t)efrom.n;
+  S0.expanded = S0.explored;
+  S0.seconds = now_s() - t0;
+  if (st) *st = S0;
+  *result = !violated;
+  free(off); free(dst); free(stop); free(inW); free(nkey);
+  free(roots.a); free(efrom.a); free(eto.a); free(fr);
+  free(B.locs); free(B.ints); free(B.zones);
+  store_free(&G);
+  model_free(&m);
+  return HORA_OK;
 }

@@ -67,6 +67,11 @@ int32_t orc_deadlock_reachable(const hora_net_desc* net, hora_stats* st, int32_t
 int32_t orc_leads_to(const hora_net_desc* net, const hora_pred_desc* p, const hora_pred_desc* q,
                      hora_stats* st, int32_t* result);
 
+/* Stop whole-query runs after the first BFS level that ends past `seconds` (0 = no limit); the run
+ * then reports status HORA_E_TIMEOUT with the counters reached so far. Used to bound the CPU
+ * baseline sample. */
+void orc_set_time_limit(double seconds);
+
 /* Initial symbolic state of the reach route (initial_symbolic_state,
  * src/reachability/engine.cpp:1322-1335): fills locs[nprocs], ints[nints], zone[dim*dim]. Returns 0
  * when the initial invariant is unsatisfiable. */

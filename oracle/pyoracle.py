@@ -56,7 +56,13 @@ def lib():
         L.orc_leads_to.argtypes = [VP, VP, VP, VP, P32]; L.orc_leads_to.restype = I32
         L.orc_initial_state.argtypes = [VP, ctypes.POINTER(ctypes.c_uint8), P32, P32, P32]
         L.orc_initial_state.restype = I32
+        L.orc_set_time_limit.argtypes = [ctypes.c_double]
+        L.orc_set_time_limit.restype = None
     return _lib
+
+
+def set_time_limit(seconds: float):
+    lib().orc_set_time_limit(float(seconds))
 
 
 def _p(a: np.ndarray):
@@ -206,7 +212,7 @@ def deadlock_reachable(net: Network):
     na = NetArrays(net)
     st = Stats(); res = ctypes.c_int32(0)
     rc = lib().orc_deadlock_reachable(ctypes.addressof(na.desc), ctypes.byref(st), ctypes.byref(res))
-    if rc:
+    if rc or st.status not in (0, 5):
         raise RuntimeError(f"oracle deadlock_reachable status {rc}")
     return bool(res.value), st.as_dict()
 

@@ -1,0 +1,495 @@
+// host.cu -- model compilation, device upload, dimension dispatch and the C ABI of libhora_gb300.so.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "host.h"
+#include "dbm_tile.cuh"
+
+namespace hgb {
+
+static inline int raw_bound(int r) { return r >> 1; }
+static int ceil_log2(long long n) { int b = 0; while ((1LL << b) < n) ++b; return b; }
+
+// ---------------------------------------------------------------------------------------------
+// compile_net: validation, the re-indexing of the descriptor, and the static analyses of
+// src/model/network.cpp (compute_bounds :59-85, compute_loc_bounds :105-182, compute_active
+// :184-232), plus the query constants of reach_engine (src/reachability/engine.cpp:1417-1455).
+// ---------------------------------------------------------------------------------------------
+int compile_net(const hora_net_desc* n, int kind, const hora_pred_desc* target, HostNet& H, std::string& err) {
+  if (!n) { err = "null network"; return HORA_E_INVALID; }
+  if (n->nprocs <= 0 || n->nclocks < 0 || n->nints < 0 || n->nchans < 0 || n->nedges < 0) {
+    err = "negative or empty sizes in the network descriptor";
+    return HORA_E_INVALID;
+  }
+  if (n->nclocks + 1 > kMaxDim || n->nclocks + 1 < kMinDim) {
+    err = "clock count outside [1, 16]";
+    return HORA_E_NOT_SUPPORTED;
+  }
+  if (n->nprocs > kMaxProcs || n->nints > kMaxInts) { err = "more than 16 processes or integers"; return HORA_E_NOT_SUPPORTED; }
+  H = HostNet{};
+  H.kind = kind;
+  H.nclocks = n->nclocks; H.dim = n->nclocks + 1; H.nprocs = n->nprocs; H.nints = n->nints;
+  H.nchans = n->nchans; H.nedges = n->nedges;
+  const int dim = H.dim, np = H.nprocs;
+  H.loc_base.resize(np);
+  int tot = 0;
+  for (int p = 0; p < np; ++p) {
+    if (n->proc_nlocs[p] <= 0 || n->proc_init[p] < 0 || n->proc_init[p] >= n->proc_nlocs[p]) {
+      err = "bad location count or initial location";
+      return HORA_E_INVALID;
+    }
+    H.loc_base[p] = tot;
+    tot += n->proc_nlocs[p];
+  }
+  H.nlocs = tot;
+  H.chan_flags.assign(n->chan_flags, n->chan_flags + n->nchans);
+  for (int c : H.chan_flags) if (c & 2) H.has_urgent_chan = 1;
+  H.int_lo.assign(n->int_lo, n->int_lo + n->nints);
+  H.int_init.assign(n->int_init, n->int_init + n->nints);
+  for (int v = 0; v < n->nints; ++v)
+    if (n->int_hi[v] < n->int_lo[v] || n->int_init[v] < n->int_lo[v] || n->int_init[v] > n->int_hi[v]) {
+      err = "bad integer range";
+      return HORA_E_INVALID;
+    }
+  H.proc_init.assign(n->proc_init, n->proc_init + np);
+  H.loc_flags.assign(n->loc_flags, n->loc_flags + tot);
+  H.loc_inv_off.assign(n->loc_inv_off, n->loc_inv_off + tot + 1);
+  const int ne = n->nedges;
+  const int ncons = ne ? n->edge_guard_off[ne] : H.loc_inv_off[tot];
+  H.cons.assign(n->cons, n->cons + 3 * std::max(ncons, H.loc_inv_off[tot]));
+  for (size_t c = 0; c < H.cons.size() / 3; ++c) {
+    const int i = H.cons[3 * c], j = H.cons[3 * c + 1];
+    if (i < 0 || j < 0 || i > H.nclocks || j > H.nclocks) { err = "clock index out of range"; return HORA_E_INVALID; }
+    if (i > 0 && j > 0) { err = "diagonal clock constraint"; return HORA_E_NOT_SUPPORTED; }
+  }
+  H.edge_tgt.resize(ne); H.edge_chan.resize(ne); H.edge_dir.resize(ne);
+  H.edge_guard_off.assign(n->edge_guard_off, n->edge_guard_off + ne + 1);
+  H.edge_iguard_off.assign(n->edge_iguard_off, n->edge_iguard_off + ne + 1);
+  H.edge_reset_off.assign(n->edge_reset_off, n->edge_reset_off + ne + 1);
+  H.edge_iupd_off.assign(n->edge_iupd_off, n->edge_iupd_off + ne + 1);
+  if (ne) {
+    H.iatoms.assign(n->iatoms, n->iatoms + 3 * n->edge_iguard_off[ne]);
+    H.resets.assign(n->resets, n->resets + n->edge_reset_off[ne]);
+    H.iupds.assign(n->iupds, n->iupds + 2 * n->edge_iupd_off[ne]);
+  }
+  for (int r : H.resets) if (r <= 0 || r > H.nclocks) { err = "reset of a non-clock"; return HORA_E_INVALID; }
+  for (size_t a = 0; a < H.iatoms.size() / 3; ++a)
+    if (H.iatoms[3 * a] < 0 || H.iatoms[3 * a] >= n->nints || H.iatoms[3 * a + 1] < 0 || H.iatoms[3 * a + 1] > 5) {
+      err = "bad integer guard"; return HORA_E_INVALID;
+    }
+  for (size_t u = 0; u < H.iupds.size() / 2; ++u) {
+    const int v = H.iupds[2 * u], val = H.iupds[2 * u + 1];
+    if (v < 0 || v >= n->nints || val < n->int_lo[v] || val > n->int_hi[v]) { err = "integer update out of range"; return HORA_E_INVALID; }
+  }
+  // outgoing edges per (global) location, in edge order
+  H.eloc_off.assign(tot + 1, 0);
+  H.eloc.assign(std::max(ne, 1), 0);
+  int last_proc = 0;
+  for (int e = 0; e < ne; ++e) {
+    const int p = n->edge_proc[e];
+    if (p < last_proc || p >= np || n->edge_src[e] < 0 || n->edge_src[e] >= n->proc_nlocs[p] ||
+        n->edge_tgt[e] < 0 || n->edge_tgt[e] >= n->proc_nlocs[p]) {
+      err = "edges must be grouped by process, with locations in range";
+      return HORA_E_INVALID;
+    }
+    last_proc = p;
+    if (n->edge_chan[e] >= n->nchans || (n->edge_chan[e] >= 0 && n->edge_dir[e] != 1 && n->edge_dir[e] != -1)) {
+      err = "bad channel on an edge";
+      return HORA_E_INVALID;
+    }
+    H.edge_tgt[e] = n->edge_tgt[e];
+    H.edge_chan[e] = n->edge_chan[e];
+    H.edge_dir[e] = n->edge_chan[e] >= 0 ? n->edge_dir[e] : 0;
+    H.eloc_off[H.loc_base[p] + n->edge_src[e] + 1]++;
+  }
+  for (int l = 0; l < tot; ++l) H.eloc_off[l + 1] += H.eloc_off[l];
+  {
+    std::vector<int> fill(tot, 0);
+    for (int e = 0; e < ne; ++e) {
+      const int gl = H.loc_base[n->edge_proc[e]] + n->edge_src[e];
+      H.eloc[H.eloc_off[gl] + fill[gl]++] = e;
+    }
+  }
+  // global Extra_LU bounds
+  H.L.assign(dim, 0);
+  H.U.assign(dim, 0);
+  auto scan_global = [&](int c0, int c1) {
+    for (int c = c0; c < c1; ++c) {
+      const int i = H.cons[3 * c], j = H.cons[3 * c + 1], v = raw_bound(H.cons[3 * c + 2]);
+      if (i > 0 && j == 0) H.U[i] = std::max(H.U[i], v);
+      else if (i == 0 && j > 0) H.L[j] = std::max(H.L[j], -v);
+    }
+  };
+  for (int l = 0; l < tot; ++l) scan_global(H.loc_inv_off[l], H.loc_inv_off[l + 1]);
+  for (int e = 0; e < ne; ++e) scan_global(H.edge_guard_off[e], H.edge_guard_off[e + 1]);
+  H.L[0] = H.U[0] = 0;
+  // per-location a_LU bounds: a backward least fixpoint inside each process
+  H.Lloc.assign((size_t)tot * dim, kAluNegInf);
+  H.Uloc.assign((size_t)tot * dim, kAluNegInf);
+  std::vector<int> Lc(dim), Uc(dim);
+  auto scan_loc = [&](int c0, int c1) {
+    for (int c = c0; c < c1; ++c) {
+      const int i = H.cons[3 * c], j = H.cons[3 * c + 1], v = raw_bound(H.cons[3 * c + 2]);
+      if (i > 0 && j == 0) Uc[i] = std::max(Uc[i], v);
+      else if (i == 0 && j > 0) Lc[j] = std::max(Lc[j], -v);
+    }
+  };
+  for (int p = 0; p < np; ++p) {
+    const int base = H.loc_base[p], nl = n->proc_nlocs[p];
+    for (bool changed = true; changed;) {
+      changed = false;
+      for (int l = 0; l < nl; ++l) {
+        std::fill(Lc.begin(), Lc.end(), kAluNegInf);
+        std::fill(Uc.begin(), Uc.end(), kAluNegInf);
+        scan_loc(H.loc_inv_off[base + l], H.loc_inv_off[base + l + 1]);
+        for (int k = H.eloc_off[base + l]; k < H.eloc_off[base + l + 1]; ++k) {
+          const int e = H.eloc[k];
+          scan_loc(H.edge_guard_off[e], H.edge_guard_off[e + 1]);
+          unsigned long long rst = 0;
+          for (int q = H.edge_reset_off[e]; q < H.edge_reset_off[e + 1]; ++q) rst |= 1ull << H.resets[q];
+          const int tg = base + H.edge_tgt[e];
+          for (int c = 1; c < dim; ++c)
+            if (!((rst >> c) & 1)) {
+              Lc[c] = std::max(Lc[c], H.Lloc[(size_t)tg * dim + c]);
+              Uc[c] = std::max(Uc[c], H.Uloc[(size_t)tg * dim + c]);
+            }
+        }
+        for (int c = 1; c < dim; ++c) {
+          int& lo = H.Lloc[(size_t)(base + l) * dim + c];
+          int& up = H.Uloc[(size_t)(base + l) * dim + c];
+          if (Lc[c] > lo) { lo = Lc[c]; changed = true; }
+          if (Uc[c] > up) { up = Uc[c]; changed = true; }
+        }
+      }
+    }
+  }
+  // active clocks
+  H.act.assign(tot, 0);
+  for (int p = 0; p < np; ++p) {
+    const int base = H.loc_base[p], nl = n->proc_nlocs[p];
+    for (bool changed = true; changed;) {
+      changed = false;
+      for (int l = 0; l < nl; ++l) {
+        unsigned long long A = 0;
+        auto rd = [&](int c0, int c1) {
+          for (int c = c0; c < c1; ++c) {
+            if (H.cons[3 * c] > 0) A |= 1ull << H.cons[3 * c];
+            if (H.cons[3 * c + 1] > 0) A |= 1ull << H.cons[3 * c + 1];
+          }
+        };
+        rd(H.loc_inv_off[base + l], H.loc_inv_off[base + l + 1]);
+        for (int k = H.eloc_off[base + l]; k < H.eloc_off[base + l + 1]; ++k) {
+          const int e = H.eloc[k];
+          rd(H.edge_guard_off[e], H.edge_guard_off[e + 1]);
+          unsigned long long r = 0;
+          for (int q = H.edge_reset_off[e]; q < H.edge_reset_off[e + 1]; ++q) r |= 1ull << H.resets[q];
+          A |= H.act[base + H.edge_tgt[e]] & ~r;
+        }
+        A &= ~1ull;
+        if (A & ~H.act[base + l]) { H.act[base + l] |= A; changed = true; }
+      }
+    }
+  }
+  // discrete key layout (DiscKeyCodecT, src/reachability/engine.cpp:967-1026)
+  H.kshift.resize(np + n->nints);
+  H.kwidth.resize(np + n->nints);
+  int off = 0;
+  for (int p = 0; p < np; ++p) { H.kshift[p] = off; H.kwidth[p] = ceil_log2(n->proc_nlocs[p]); off += H.kwidth[p]; }
+  for (int v = 0; v < n->nints; ++v) {
+    H.kshift[np + v] = off;
+    H.kwidth[np + v] = ceil_log2((long long)n->int_hi[v] - n->int_lo[v] + 1);
+    off += H.kwidth[np + v];
+  }
+  H.keybits = off;
+  if (off > 63) { err = "discrete key wider than 63 bits"; return HORA_E_NOT_SUPPORTED; }
+  // query constants
+  H.Lq.assign(dim, kAluNegInf);
+  H.Uq.assign(dim, kAluNegInf);
+  if (kind == HORA_Q_DEADLOCK) {
+    // a_M bounds: L = U = max(L, U) per clock (deadlock_reachable, src/reachability/engine.cpp:2376-2384)
+    for (int c = 0; c < dim; ++c) H.L[c] = H.U[c] = std::max(H.L[c], H.U[c]);
+    for (size_t k = 0; k < H.Lloc.size(); ++k) H.Lloc[k] = H.Uloc[k] = std::max(H.Lloc[k], H.Uloc[k]);
+  }
+  if (kind == HORA_Q_REACH && target) {
+    H.t_never = target->never;
+    for (int k = 0; k < target->nloc; ++k) {
+      const int p = target->loc_req[2 * k], l = target->loc_req[2 * k + 1];
+      if (p < 0 || p >= np || l < 0 || l >= n->proc_nlocs[p]) { err = "target location out of range"; return HORA_E_INVALID; }
+    }
+    H.t_loc.assign(target->loc_req, target->loc_req + 2 * target->nloc);
+    H.t_int.assign(target->int_cond, target->int_cond + 3 * target->nint);
+    H.t_clk.assign(target->clk_cond, target->clk_cond + 3 * target->nclk);
+    for (int k = 0; k < target->nclk; ++k) {
+      const int i = H.t_clk[3 * k], j = H.t_clk[3 * k + 1], v = raw_bound(H.t_clk[3 * k + 2]);
+      if (i < 0 || j < 0 || i > H.nclocks || j > H.nclocks) { err = "target clock out of range"; return HORA_E_INVALID; }
+      if (i > 0) H.qmask |= 1ull << i;
+      if (j > 0) H.qmask |= 1ull << j;
+      if (i > 0 && j == 0) { H.U[i] = std::max(H.U[i], v); H.Uq[i] = std::max(H.Uq[i], v); }
+      else if (i == 0 && j > 0) { H.L[j] = std::max(H.L[j], -v); H.Lq[j] = std::max(H.Lq[j], -v); }
+      else if (i > 0 && j > 0) { err = "diagonal target constraint"; return HORA_E_NOT_SUPPORTED; }
+    }
+    H.L[0] = H.U[0] = 0;
+  }
+  return HORA_OK;
+}
+
+DeviceNets::~DeviceNets() {
+  for (void* b : blobs) cudaFree(b);
+  if (views) cudaFree(views);
+  if (ok) cudaFree(ok);
+}
+
+int upload_nets(const std::vector<const HostNet*>& nets, int inst_shift, DeviceNets& out, std::string& err) {
+  const int ninst = (int)nets.size();
+  out.host_views.resize(ninst);
+  std::vector<int> okv(ninst, 1);
+  for (int k = 0; k < ninst; ++k) {
+    const HostNet& H = *nets[k];
+    std::vector<int32_t> blob;
+    std::vector<size_t> offs;
+    auto add = [&](const std::vector<int32_t>& v) {
+      while (blob.size() % 4) blob.push_back(0);   // 16-byte alignment for every array
+      offs.push_back(blob.size());
+      blob.insert(blob.end(), v.begin(), v.end());
+      if (v.empty()) blob.push_back(0);
+    };
+    std::vector<int32_t> act32(H.act.size() * 2);
+    std::memcpy(act32.data(), H.act.data(), H.act.size() * 8);
+    const std::vector<int32_t>* arrs[] = {&H.chan_flags, &H.int_lo, &H.int_init, &H.proc_init, &H.loc_base,
+                                          &H.loc_flags, &H.loc_inv_off, &H.eloc_off, &H.eloc, &H.edge_tgt,
+                                          &H.edge_chan, &H.edge_dir, &H.edge_guard_off, &H.edge_iguard_off,
+                                          &H.edge_reset_off, &H.edge_iupd_off, &H.cons, &H.iatoms, &H.resets,
+                                          &H.iupds, &H.Lloc, &H.Uloc, &act32, &H.kshift, &H.kwidth, &H.L, &H.U,
+                                          &H.Lq, &H.Uq, &H.t_loc, &H.t_int, &H.t_clk};
+    for (auto* a : arrs) add(*a);
+    void* d = nullptr;
+    cudaError_t e = cudaMalloc(&d, blob.size() * 4);
+    if (e != cudaSuccess) { err = std::string("CUDA: cudaMalloc: ") + cudaGetErrorString(e); return HORA_E_NOMEM; }
+    out.blobs.push_back(d);
+    out.blob_bytes.push_back(blob.size() * 4);
+    e = cudaMemcpy(d, blob.data(), blob.size() * 4, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) { err = std::string("CUDA: cudaMemcpy: ") + cudaGetErrorString(e); return HORA_E_CUDA; }
+    const int32_t* b = static_cast<const int32_t*>(d);
+    size_t q = 0;
+    NetView& V = out.host_views[k];
+    V.nclocks = H.nclocks; V.dim = H.dim; V.nprocs = H.nprocs; V.nints = H.nints; V.nchans = H.nchans;
+    V.nedges = H.nedges; V.nlocs = H.nlocs; V.has_urgent_chan = H.has_urgent_chan; V.kind = H.kind;
+    V.inst_shift = inst_shift;
+    V.chan_flags = b + offs[q++]; V.int_lo = b + offs[q++]; V.int_init = b + offs[q++]; V.proc_init = b + offs[q++];
+    V.loc_base = b + offs[q++]; V.loc_flags = b + offs[q++]; V.loc_inv_off = b + offs[q++];
+    V.eloc_off = b + offs[q++]; V.eloc = b + offs[q++]; V.edge_tgt = b + offs[q++]; V.edge_chan = b + offs[q++];
+    V.edge_dir = b + offs[q++]; V.edge_guard_off = b + offs[q++]; V.edge_iguard_off = b + offs[q++];
+    V.edge_reset_off = b + offs[q++]; V.edge_iupd_off = b + offs[q++]; V.cons = b + offs[q++];
+    V.iatoms = b + offs[q++]; V.resets = b + offs[q++]; V.iupds = b + offs[q++]; V.Lloc = b + offs[q++];
+    V.Uloc = b + offs[q++];
+    V.act = reinterpret_cast<const unsigned long long*>(b + offs[q++]);
+    V.kshift = b + offs[q++]; V.kwidth = b + offs[q++]; V.L = b + offs[q++]; V.U = b + offs[q++];
+    V.Lq = b + offs[q++]; V.Uq = b + offs[q++];
+    V.qmask = H.qmask;
+    V.t_never = H.t_never;
+    V.t_nloc = (int)H.t_loc.size() / 2; V.t_nint = (int)H.t_int.size() / 3; V.t_nclk = (int)H.t_clk.size() / 3;
+    V.t_loc = b + offs[q++]; V.t_int = b + offs[q++]; V.t_clk = b + offs[q++];
+  }
+  cudaError_t e = cudaMalloc(&out.views, sizeof(NetView) * std::max(ninst, 1));
+  if (e == cudaSuccess) e = cudaMemcpy(out.views, out.host_views.data(), sizeof(NetView) * ninst, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMalloc(&out.ok, sizeof(int) * std::max(ninst, 1));
+  if (e == cudaSuccess) e = cudaMemcpy(out.ok, okv.data(), sizeof(int) * ninst, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) { err = std::string("CUDA: ") + cudaGetErrorString(e); return HORA_E_CUDA; }
+  return HORA_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+// dimension dispatch
+// ---------------------------------------------------------------------------------------------
+#define HGB_FOR_DIMS(X) X(2) X(3) X(4) X(5) X(6) X(7) X(8) X(9) X(10) X(11) X(12) X(13) X(14) X(15) X(16) X(17)
+#define HGB_DECL(D)                                                                                         \
+  extern template int run_group<D>(const std::vector<const HostNet*>&, std::vector<InstResult>&,           \
+                                   const RunOptions&, std::string&);                                       \
+  extern template int run_expand<D>(const HostNet&, int, const int*, const int*, const int*, int, int64_t, \
+                                    int*, int*, int*, int*, int*, int64_t*, std::string&);                 \
+  extern template int run_has_deadlock<D>(const HostNet&, int, const int*, const int*, const int*, int*,   \
+                                          std::string&);
+HGB_FOR_DIMS(HGB_DECL)
+
+static int dispatch_group(int dim, const std::vector<const HostNet*>& nets, std::vector<InstResult>& res,
+                          const RunOptions& o, std::string& err) {
+  switch (dim) {
+#define HGB_CASE(D) case D: return run_group<D>(nets, res, o, err);
+    HGB_FOR_DIMS(HGB_CASE)
+#undef HGB_CASE
+  }
+  err = "unsupported DBM dimension";
+  return HORA_E_NOT_SUPPORTED;
+}
+
+}  // namespace hgb
+
+// =============================================================================================
+// C ABI
+// =============================================================================================
+using namespace hgb;
+
+static thread_local std::string g_last_error;
+
+static int32_t fail(int32_t rc, const std::string& msg) {
+  g_last_error = msg;
+  return rc;
+}
+static void stats_out(hora_stats* dst, const hora_stats& src) { if (dst) *dst = src; }
+
+static int32_t ensure_device() {
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) return fail(HORA_E_NO_DEVICE, "no CUDA device visible");
+  return HORA_OK;
+}
+
+extern "C" {
+
+const char* hora_gb_last_error(void) { return g_last_error.c_str(); }
+int32_t hora_gb_abi_version(void) { return HORA_GB_ABI_VERSION; }
+
+int32_t hora_gb_device_count(int32_t* count) {
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (count) *count = (e == cudaSuccess) ? n : 0;
+  return HORA_OK;
+}
+
+static int32_t run_single(const hora_net_desc* net, int kind, const hora_pred_desc* target, int32_t backend,
+                          hora_stats* stats, const volatile int32_t* cancel, int32_t* result) {
+  g_last_error.clear();
+  if (!result) return fail(HORA_E_INVALID, "null result pointer");
+  if (backend != HORA_BACKEND_CUDA) return fail(HORA_E_NOT_SUPPORTED, "this library implements the cuda backend only");
+  HostNet H;
+  std::string err;
+  int rc = compile_net(net, kind, target, H, err);
+  if (rc) return fail(rc, err);
+  if ((rc = ensure_device())) return rc;
+  std::vector<const HostNet*> v{&H};
+  std::vector<InstResult> res;
+  RunOptions o;
+  o.cancel = cancel;
+  rc = dispatch_group(H.dim, v, res, o, err);
+  if (!res.empty()) stats_out(stats, res[0].st);
+  if (rc) return fail(rc, err);
+  *result = res[0].verdict;
+  return HORA_OK;
+}
+
+int32_t hora_gb_reachable_net(const hora_net_desc* net, const hora_pred_desc* target, int32_t backend,
+                              hora_stats* stats, int32_t* result) {
+  if (!target) return fail(HORA_E_INVALID, "null target");
+  return run_single(net, HORA_Q_REACH, target, backend, stats, nullptr, result);
+}
+
+int32_t hora_gb_deadlock_reachable(const hora_net_desc* net, int32_t backend, hora_stats* stats,
+                                   const volatile int32_t* cancel, int32_t* result) {
+  return run_single(net, HORA_Q_DEADLOCK, nullptr, backend, stats, cancel, result);
+}
+
+int32_t hora_gb_leads_to(const hora_net_desc* net, const hora_pred_desc* p, const hora_pred_desc* q,
+                         int32_t backend, hora_stats* stats, int32_t* result) {
+  (void)net; (void)p; (void)q; (void)backend; (void)stats; (void)result;
+  return fail(HORA_E_NOT_SUPPORTED, "leads-to is not available in this build");
+}
+
+int32_t hora_gb_expand(const hora_net_desc* net, int32_t n, const int32_t* locs, const int32_t* ints,
+                       const int32_t* zones, const int32_t* L, const int32_t* U, const uint8_t* qmask,
+                       int32_t emode, int64_t cap, int32_t* out_src, int32_t* out_ord, int32_t* out_locs,
+                       int32_t* out_ints, int32_t* out_zones, int64_t* out_n) {
+  g_last_error.clear();
+  if (n < 0 || !out_n) return fail(HORA_E_INVALID, "bad arguments");
+  HostNet H;
+  std::string err;
+  int rc = compile_net(net, HORA_Q_REACH, nullptr, H, err);
+  if (rc) return fail(rc, err);
+  if ((rc = ensure_device())) return rc;
+  if (L && U) {
+    H.L.assign(L, L + H.dim);
+    H.U.assign(U, U + H.dim);
+  }
+  H.qmask = 0;
+  if (qmask)
+    for (int c = 1; c < H.dim; ++c) if (qmask[c]) H.qmask |= 1ull << c;
+  if (n == 0) { *out_n = 0; return HORA_OK; }
+  switch (H.dim) {
+#define HGB_CASE(D) case D: rc = run_expand<D>(H, n, locs, ints, zones, emode, cap, out_src, out_ord, out_locs, out_ints, out_zones, out_n, err); break;
+    HGB_FOR_DIMS(HGB_CASE)
+#undef HGB_CASE
+    default: return fail(HORA_E_NOT_SUPPORTED, "unsupported DBM dimension");
+  }
+  if (rc && rc != HORA_E_OVERFLOW) return fail(rc, err);
+  return rc;
+}
+
+int32_t hora_gb_has_deadlock(const hora_net_desc* net, int32_t n, const int32_t* locs, const int32_t* ints,
+                             const int32_t* zones, int32_t* out) {
+  g_last_error.clear();
+  if (n < 0 || !out) return fail(HORA_E_INVALID, "bad arguments");
+  HostNet H;
+  std::string err;
+  int rc = compile_net(net, HORA_Q_DEADLOCK, nullptr, H, err);
+  if (rc) return fail(rc, err);
+  if ((rc = ensure_device())) return rc;
+  if (n == 0) return HORA_OK;
+  switch (H.dim) {
+#define HGB_CASE(D) case D: rc = run_has_deadlock<D>(H, n, locs, ints, zones, out, err); break;
+    HGB_FOR_DIMS(HGB_CASE)
+#undef HGB_CASE
+    default: return fail(HORA_E_NOT_SUPPORTED, "unsupported DBM dimension");
+  }
+  if (rc) return fail(rc, err);
+  return HORA_OK;
+}
+
+int32_t hora_gb_batch_run(int32_t n, const hora_net_desc* nets, const hora_query_desc* queries, int32_t* verdicts,
+                          hora_stats* stats) {
+  g_last_error.clear();
+  if (n < 0 || (n > 0 && (!nets || !queries || !verdicts))) return fail(HORA_E_INVALID, "bad arguments");
+  int rc = ensure_device();
+  if (rc) return rc;
+  std::vector<HostNet> H(n);
+  std::map<int, std::vector<int>> by_dim;
+  for (int k = 0; k < n; ++k) {
+    verdicts[k] = -1;
+    std::string err;
+    const hora_query_desc& q = queries[k];
+    int r = HORA_OK;
+    if (q.kind == HORA_Q_LEADSTO) r = HORA_E_NOT_SUPPORTED;
+    else r = compile_net(&nets[k], q.kind, q.kind == HORA_Q_REACH ? &q.p : nullptr, H[k], err);
+    if (stats) { std::memset(&stats[k], 0, sizeof(hora_stats)); stats[k].status = r; }
+    if (r == HORA_OK) by_dim[H[k].dim].push_back(k);
+  }
+  std::string err;
+  int first_err = HORA_OK;
+  for (auto& kv : by_dim) {
+    std::vector<const HostNet*> v;
+    for (int k : kv.second) v.push_back(&H[k]);
+    std::vector<InstResult> res;
+    RunOptions o;
+    const int r = dispatch_group(kv.first, v, res, o, err);
+    for (size_t q = 0; q < kv.second.size(); ++q) {
+      const int k = kv.second[q];
+      if (q < res.size()) {
+        if (stats) stats[k] = res[q].st;
+        verdicts[k] = r == HORA_OK ? res[q].verdict : -1;
+      }
+      if (stats && r) stats[k].status = r;
+    }
+    if (r && !first_err) { first_err = r; g_last_error = err; }
+  }
+  return first_err == HORA_E_CUDA ? HORA_E_CUDA : HORA_OK;
+}
+
+// ---- serving form: implemented in server.cu ----
+
+}  // extern "C"

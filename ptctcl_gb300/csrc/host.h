@@ -1,0 +1,71 @@
+// host.h -- host-side model compilation and the per-dimension engine entry points.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/hora_gb300.h"
+#include "engine.cuh"
+
+namespace hgb {
+
+// One (network, query) instance compiled for the device: the descriptor's arrays re-indexed, the
+// static analyses of src/model/network.cpp applied, and the query's constants folded in.
+struct HostNet {
+  int kind = 0;
+  int nclocks = 0, dim = 0, nprocs = 0, nints = 0, nchans = 0, nedges = 0, nlocs = 0;
+  int keybits = 0;
+  int has_urgent_chan = 0;
+  int t_never = 0;
+  unsigned long long qmask = 0;
+  std::vector<int32_t> chan_flags, int_lo, int_init, proc_init, loc_base, loc_flags, loc_inv_off, eloc_off,
+      eloc, edge_tgt, edge_chan, edge_dir, edge_guard_off, edge_iguard_off, edge_reset_off, edge_iupd_off, cons,
+      iatoms, resets, iupds, Lloc, Uloc, kshift, kwidth, L, U, Lq, Uq, t_loc, t_int, t_clk;
+  std::vector<unsigned long long> act;
+};
+
+// Compile `net` for query `kind` (HORA_Q_*); `target` is the reach target (may be null).
+// Returns HORA_OK, HORA_E_INVALID or HORA_E_NOT_SUPPORTED with a message in `err`.
+int compile_net(const hora_net_desc* net, int kind, const hora_pred_desc* target, HostNet& out, std::string& err);
+
+// Device copy of one or more compiled instances: a blob per instance and the NetView array.
+struct DeviceNets {
+  std::vector<void*> blobs;
+  std::vector<size_t> blob_bytes;
+  NetView* views = nullptr;   // device array
+  std::vector<NetView> host_views;
+  int* ok = nullptr;          // device array of per-instance "runnable" flags
+  ~DeviceNets();
+};
+int upload_nets(const std::vector<const HostNet*>& nets, int inst_shift, DeviceNets& out, std::string& err);
+
+// Result of one instance.
+struct InstResult {
+  int status = HORA_OK;
+  int verdict = 0;            // goal reached (reach: target reachable; deadlock: deadlock reachable)
+  hora_stats st{};
+};
+
+struct RunOptions {
+  int blocks = 0;             // grid cap for the level kernels (0: derived from the SM count)
+  const volatile int32_t* cancel = nullptr;
+  size_t succ_cap0 = 1 << 16; // initial successor-buffer capacity
+};
+
+// Run a group of instances that share the DBM dimension D (one level-synchronous BFS over all of
+// them). Implemented per D in the generated units.
+template <int D>
+int run_group(const std::vector<const HostNet*>& nets, std::vector<InstResult>& res, const RunOptions& o,
+              std::string& err);
+template <int D>
+int run_expand(const HostNet& net, int n, const int* locs, const int* ints, const int* zones, int emode,
+               int64_t cap, int* out_src, int* out_ord, int* out_locs, int* out_ints, int* out_zones, int64_t* out_n,
+               std::string& err);
+template <int D>
+int run_has_deadlock(const HostNet& net, int n, const int* locs, const int* ints, const int* zones, int* out,
+                     std::string& err);
+
+constexpr int kMinDim = 2;
+constexpr int kMaxDim = 17;
+
+}  // namespace hgb

@@ -1,0 +1,498 @@
+// level_kernels_impl.cuh -- bodies of the level kernels. Included once per DBM dimension by the
+// generated translation units (dim_<D>.cu), which instantiate hgb::Level<D>.
+#pragma once
+#include "level_kernels.cuh"
+
+namespace hgb {
+
+constexpr int kBlock = 128;   // threads per block: 4 warps, each holding floor(32/D) tiles
+
+template <int D>
+__device__ __forceinline__ long long tile_id() {
+  constexpr int TPW = 32 / D;
+  const int lane = threadIdx.x & 31;
+  return ((long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * TPW + lane / D;
+}
+template <int D>
+__device__ __forceinline__ long long tile_count() {
+  return (long long)gridDim.x * (blockDim.x >> 5) * (32 / D);
+}
+__device__ __forceinline__ unsigned long long key_part(unsigned long long hk, int inst_shift) {
+  return hk & ((1ull << inst_shift) - 1);
+}
+
+// Find or insert a hash key (atomic CAS, linear probing). Returns the slot, or -1 if the table
+// is full; *inserted tells a fresh key from an existing one. Called by one lane.
+inline __device__ long long slot_find_insert(const Store& st, unsigned long long hk, bool* inserted) {
+  unsigned long long h = hash_mix(hk) & st.hmask;
+  *inserted = false;
+  for (unsigned long long probe = 0; probe <= st.hmask; ++probe) {
+    const unsigned long long k = st.hkey[h];
+    if (k == hk) return (long long)h;
+    if (k == kEmptyKey) {
+      const unsigned long long prev = atomicCAS(&st.hkey[h], kEmptyKey, hk);
+      if (prev == kEmptyKey) { *inserted = true; return (long long)h; }
+      if (prev == hk) return (long long)h;
+    }
+    h = (h + 1) & st.hmask;
+  }
+  return -1;
+}
+
+// ---------------------------------------------------------------------------------------------
+// init: the initial symbolic state of every instance (initial_symbolic_state,
+// src/reachability/engine.cpp:1322-1335), its goal test, and its insertion at level 0.
+// ---------------------------------------------------------------------------------------------
+template <int D>
+__global__ void __launch_bounds__(kBlock) k_init(const NetView* nets, int ninst, const int* ok, Store st,
+                                                 Front out, InstState is, Ctl* ctl) {
+  Tile<D> t;
+  if (!make_tile(t, threadIdx.x & 31)) return;
+  DlScratch<D> S;
+  for (long long w = tile_id<D>(); w < ninst; w += tile_count<D>()) {
+    const int inst = (int)w;
+    if (!ok[inst]) continue;
+    const NetView& N = nets[inst];
+    int locs[kMaxProcs], ints[kMaxInts];
+    for (int p = 0; p < N.nprocs; ++p) locs[p] = N.proc_init[p];
+    for (int v = 0; v < N.nints; ++v) ints[v] = N.int_init[v];
+    int z[D];
+    init_zero(z);
+    if (!close_succ(N, t, z, locs, ints, 0) || is_empty(t, z)) {   // no initial state at all
+      if (t.i == 0) is.done[inst] = 1;
+      continue;
+    }
+    bool hit = false;
+    if (N.kind == 0) hit = target_hit(N, t, z, locs, ints);
+    else if (N.kind == 1) {
+      const int r = state_has_deadlock(N, t, locs, ints, z, S);
+      if (r < 0) { if (t.i == 0) atomicMax(&ctl->err, 4u); continue; }
+      hit = r == 1;
+    }
+    if (hit) {
+      if (t.i == 0) { is.found[inst] = 1; is.done[inst] = 1; atomicOr(&ctl->found, 1u); }
+      continue;
+    }
+    const unsigned long long hk = key_encode(N, locs, ints) | ((unsigned long long)inst << N.inst_shift);
+    long long slot = 0, node = 0;
+    if (t.i == 0) {
+      bool ins;
+      slot = slot_find_insert(st, hk, &ins);
+      if (slot >= 0) node = (long long)atomicAdd(&ctl->nnodes, 1ull);
+    }
+    slot = (long long)t.shfl64((unsigned long long)slot, 0);
+    node = (long long)t.shfl64((unsigned long long)node, 0);
+    if (slot < 0) { if (t.i == 0) atomicMax(&ctl->err, 4u); continue; }
+    store_rows(t, z, st.nzone + node * D * D);
+    if (t.i == 0) {
+      st.nnext[node] = -1; st.nlevel[node] = 0; st.ndead[node] = 0; st.ninst[node] = inst;
+      st.head[slot] = (int)node;
+      const unsigned long long f = atomicAdd(&ctl->nfront, 1ull);
+      out.key[f] = hk; out.node[f] = (int)node; out.rank[f] = 0; out.inst[f] = inst;
+      is.nkeys[inst] = 1; is.nlive[inst] = 1; is.nfront[inst] = 1;
+      atomicAdd(&ctl->nkeys, 1ull);
+      atomicAdd(&ctl->nslots, 1ull);
+      atomicAdd((unsigned long long*)&ctl->nlive, 1ull);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// expand: successors of every frontier state
+// ---------------------------------------------------------------------------------------------
+template <int D>
+__global__ void __launch_bounds__(kBlock) k_expand(const NetView* nets, InstState is, Front fr, int nfront,
+                                                   Store st, Succ sc, Ctl* ctl) {
+  Tile<D> t;
+  if (!make_tile(t, threadIdx.x & 31)) return;
+  for (long long f = tile_id<D>(); f < nfront; f += tile_count<D>()) {
+    const int inst = fr.inst[f];
+    if (is.done[inst]) continue;
+    const NetView& N = nets[inst];
+    const unsigned long long hk = fr.key[f];
+    int locs[kMaxProcs], ints[kMaxInts];
+    key_decode(N, key_part(hk, N.inst_shift), locs, ints);
+    int src[D];
+    load_rows(t, src, st.nzone + (long long)fr.node[f] * D * D);
+    const int emode = is.emode[inst];
+    int ord = 0;
+    bool hit = false;
+    const bool ok = for_each_successor(N, t, locs, ints, src, emode, [&](const int* tl, const int* ti, const int (&z)[D]) {
+      unsigned long long idx = 0;
+      if (t.i == 0) idx = atomicAdd(&ctl->nsucc, 1ull);
+      idx = t.shfl64(idx, 0);
+      if ((long long)idx < sc.cap) {
+        store_rows(t, z, sc.zone + (long long)idx * D * D);
+        if (t.i == 0) {
+          sc.key[idx] = key_encode(N, tl, ti) | ((unsigned long long)inst << N.inst_shift);
+          sc.parent[idx] = (int)f;
+          sc.ord[idx] = ord;
+        }
+      } else if (t.i == 0) {
+        ctl->overflow = 1;
+      }
+      ++ord;
+      if (N.kind == 0 && !hit) hit = target_hit(N, t, z, tl, ti);
+    });
+    if (t.i == 0) {
+      if (!ok) atomicMax(&ctl->err, 4u);
+      if (ord) atomicAdd(&is.generated[inst], (unsigned long long)ord);
+      if (hit) { is.found[inst] = 1; atomicOr(&ctl->found, 1u); }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// probe: drop successors a stored zone simulates; group the rest by hash slot
+// ---------------------------------------------------------------------------------------------
+template <int D>
+__global__ void __launch_bounds__(kBlock) k_probe(const NetView* nets, InstState is, Succ sc, Store st, Ctl* ctl,
+                                                  long long nsucc) {
+  Tile<D> t;
+  if (!make_tile(t, threadIdx.x & 31)) return;
+  const int ishift = nets[0].inst_shift;
+  for (long long s = tile_id<D>(); s < nsucc; s += tile_count<D>()) {
+    const unsigned long long hk = sc.key[s];
+    const int inst = (int)(hk >> ishift);
+    if (is.found[inst] || is.done[inst]) { if (t.i == 0) sc.slot[s] = -1; continue; }
+    const NetView& N = nets[inst];
+    int locs[kMaxProcs], ints[kMaxInts];
+    key_decode(N, key_part(hk, ishift), locs, ints);
+    int Ly, U[D];
+    key_bounds(N, t, locs, Ly, U);
+    int z[D], z0[D];
+    load_rows(t, z, sc.zone + s * D * D);
+#pragma unroll
+    for (int x = 0; x < D; ++x) z0[x] = t.shfl(z[x], 0);
+    long long slot = 0;
+    int inserted = 0;
+    if (t.i == 0) {
+      bool ins;
+      slot = slot_find_insert(st, hk, &ins);
+      inserted = ins;   // keys are counted when their first zone is stored (merge), not here
+      if (ins) atomicAdd(&ctl->nslots, 1ull);
+    }
+    slot = (long long)t.shfl64((unsigned long long)slot, 0);
+    inserted = t.shfl(inserted, 0);
+    if (slot < 0) { if (t.i == 0) { atomicMax(&ctl->err, 4u); sc.slot[s] = -1; } continue; }
+    bool killed = false;
+    unsigned long long nprobe = 0;
+    if (!inserted) {
+      for (int n = __ldg(st.head + slot); n >= 0; n = __ldg(st.nnext + n)) {
+        if (__ldg(st.ndead + n)) continue;
+        int zp[D];
+        load_rows(t, zp, st.nzone + (long long)n * D * D);
+        ++nprobe;
+        if (alu_le(t, z, zp, z0, Ly, U)) { killed = true; break; }
+      }
+    }
+    if (t.i == 0) {
+      if (nprobe) atomicAdd(&ctl->probes, nprobe);
+      if (killed) {
+        sc.slot[s] = -1;
+      } else {
+        const unsigned r = atomicAdd(&st.pend[slot], 1u);
+        if (r == 0) sc.touched[atomicAdd(&ctl->ntouched, 1ull)] = (int)slot;
+        sc.slot[s] = (int)slot;
+        sc.rank[s] = (int)r;
+        sc.surv[atomicAdd(&ctl->nsurv, 1ull)] = (int)s;
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// deadlock: the goal test of the deadlock query, on the probe's survivors
+// ---------------------------------------------------------------------------------------------
+template <int D>
+__global__ void __launch_bounds__(kBlock) k_deadlock(const NetView* nets, InstState is, Succ sc, Ctl* ctl,
+                                                     long long nsurv) {
+  Tile<D> t;
+  if (!make_tile(t, threadIdx.x & 31)) return;
+  DlScratch<D> S;
+  const int ishift = nets[0].inst_shift;
+  for (long long w = tile_id<D>(); w < nsurv; w += tile_count<D>()) {
+    const int s = sc.surv[w];
+    const unsigned long long hk = sc.key[s];
+    const int inst = (int)(hk >> ishift);
+    const NetView& N = nets[inst];
+    if (N.kind != 1 || is.found[inst]) continue;
+    int locs[kMaxProcs], ints[kMaxInts];
+    key_decode(N, key_part(hk, ishift), locs, ints);
+    int z[D];
+    load_rows(t, z, sc.zone + (long long)s * D * D);
+    const int r = state_has_deadlock(N, t, locs, ints, z, S);
+    if (t.i == 0) {
+      if (r < 0) atomicMax(&ctl->err, 4u);
+      else if (r == 1) { is.found[inst] = 1; atomicOr(&ctl->found, 1u); }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// group: one contiguous segment of survivors per touched slot
+// ---------------------------------------------------------------------------------------------
+static __global__ void k_seg_alloc(Succ sc, Store st, Ctl* ctl, long long ntouched) {
+  for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < ntouched; j += (long long)gridDim.x * blockDim.x) {
+    const int s = sc.touched[j];
+    st.pend_base[s] = (unsigned)atomicAdd(&ctl->seg_alloc, (unsigned long long)st.pend[s]);
+  }
+}
+static __global__ void k_seg_scatter(Succ sc, Store st, long long nsucc) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nsucc; i += (long long)gridDim.x * blockDim.x) {
+    const int s = sc.slot[i];
+    if (s < 0) continue;
+    sc.seg[st.pend_base[s] + sc.rank[i]] = (int)i;
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// merge: NetPassedT::add folds (passed_set.hpp:287-444) per key, in canonical order
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ bool order_less(const Front& fr, const Succ& sc, int a, int b) {
+  const int pa = sc.parent[a], pb = sc.parent[b];
+  const unsigned long long ka = fr.key[pa], kb = fr.key[pb];
+  if (ka != kb) return ka < kb;
+  const int ra = fr.rank[pa], rb = fr.rank[pb];
+  if (ra != rb) return ra < rb;
+  return sc.ord[a] < sc.ord[b];
+}
+
+template <int D>
+__global__ void __launch_bounds__(kBlock) k_merge(const NetView* nets, InstState is, Front fr, Succ sc, Store st,
+                                                  Front out, Ctl* ctl, long long ntouched, int level) {
+  Tile<D> t;
+  if (!make_tile(t, threadIdx.x & 31)) return;
+  const int ishift = nets[0].inst_shift;
+  for (long long j = tile_id<D>(); j < ntouched; j += tile_count<D>()) {
+    const int s = sc.touched[j];
+    const unsigned n = st.pend[s];
+    const unsigned base = st.pend_base[s];
+    const unsigned long long hk = st.hkey[s];
+    const int inst = (int)(hk >> ishift);
+    if (is.found[inst] || is.done[inst]) { t.sync(); if (t.i == 0) st.pend[s] = 0; continue; }
+    const NetView& N = nets[inst];
+    // canonical order: rank every pending survivor by (parent key, parent rank, ordinal)
+    for (unsigned e = t.i; e < n; e += D) {
+      const int a = sc.seg[base + e];
+      unsigned r = 0;
+      for (unsigned q = 0; q < n; ++q) r += order_less(fr, sc, sc.seg[base + q], a) ? 1u : 0u;
+      sc.sorted[base + r] = a;
+    }
+    t.sync();
+    int locs[kMaxProcs], ints[kMaxInts];
+    key_decode(N, key_part(hk, ishift), locs, ints);
+    int Ly, U[D];
+    key_bounds(N, t, locs, Ly, U);
+    long long dlive = 0;
+    unsigned long long nprobe = 0;
+    for (unsigned q = 0; q < n; ++q) {
+      const int a = ((volatile int*)sc.sorted)[base + q];
+      int z[D], z0[D];
+      load_rows(t, z, sc.zone + (long long)a * D * D);
+#pragma unroll
+      for (int x = 0; x < D; ++x) z0[x] = t.shfl(z[x], 0);
+      // (1)+(2): dropped if a stored zone simulates it
+      bool drop = false;
+      for (int m = ((volatile int*)st.head)[s]; m >= 0; m = ((volatile int*)st.nnext)[m]) {
+        if (((volatile int*)st.ndead)[m]) continue;
+        int zp[D];
+        load_rows_rw(t, zp, st.nzone + (long long)m * D * D);
+        ++nprobe;
+        if (alu_le(t, z, zp, z0, Ly, U)) { drop = true; break; }
+      }
+      if (drop) continue;
+      // (3): retire stored zones the new one simulates
+      for (int m = ((volatile int*)st.head)[s]; m >= 0; m = ((volatile int*)st.nnext)[m]) {
+        if (((volatile int*)st.ndead)[m]) continue;
+        int zp[D], zp0[D];
+        load_rows_rw(t, zp, st.nzone + (long long)m * D * D);
+#pragma unroll
+        for (int x = 0; x < D; ++x) zp0[x] = t.shfl(zp[x], 0);
+        if (alu_le(t, zp, z, zp0, Ly, U)) {
+          t.sync();
+          if (t.i == 0) ((volatile int*)st.ndead)[m] = 1;
+          --dlive;
+          t.sync();
+        }
+      }
+      // (4): convex-union absorb within the newest kMergeScan live zones, restarting after each
+      for (bool merged = true; merged;) {
+        merged = false;
+        int seen = 0;
+        for (int m = ((volatile int*)st.head)[s]; m >= 0 && seen < kMergeScan; m = ((volatile int*)st.nnext)[m]) {
+          if (((volatile int*)st.ndead)[m]) continue;
+          ++seen;
+          int zp[D];
+          load_rows_rw(t, zp, st.nzone + (long long)m * D * D);
+          if (try_union(t, z, zp)) {
+            t.sync();
+            if (t.i == 0) ((volatile int*)st.ndead)[m] = 1;
+            --dlive;
+            t.sync();
+            merged = true;
+            break;
+          }
+        }
+      }
+      // (5): prepend
+      long long node = 0;
+      if (t.i == 0) node = (long long)atomicAdd(&ctl->nnodes, 1ull);
+      node = (long long)t.shfl64((unsigned long long)node, 0);
+      store_rows(t, z, st.nzone + node * D * D);
+      t.sync();
+      if (t.i == 0) {
+        const int old_head = ((volatile int*)st.head)[s];
+        if (old_head < 0) { atomicAdd(&ctl->nkeys, 1ull); atomicAdd(&is.nkeys[inst], 1ull); }
+        st.nnext[node] = old_head;
+        st.nlevel[node] = level;
+        st.ndead[node] = 0;
+        st.ninst[node] = inst;
+        __threadfence_block();
+        ((volatile int*)st.head)[s] = (int)node;
+      }
+      ++dlive;
+      t.sync();
+    }
+    // this key's zones stored at this level enter the next frontier, in chain order
+    if (t.i == 0) {
+      int r = 0;
+      for (int m = ((volatile int*)st.head)[s]; m >= 0; m = ((volatile int*)st.nnext)[m]) {
+        if (((volatile int*)st.ndead)[m] || ((volatile int*)st.nlevel)[m] != level) continue;
+        const unsigned long long f = atomicAdd(&ctl->nfront, 1ull);
+        out.key[f] = hk; out.node[f] = m; out.rank[f] = r++; out.inst[f] = inst;
+      }
+      if (r) atomicAdd(&is.nfront[inst], (unsigned long long)r);
+      if (dlive) {
+        atomicAdd((unsigned long long*)&ctl->nlive, (unsigned long long)dlive);
+        atomicAdd((unsigned long long*)&is.nlive[inst], (unsigned long long)dlive);
+      }
+      if (nprobe) atomicAdd(&ctl->probes, nprobe);
+      st.pend[s] = 0;
+    }
+    t.sync();
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// host-buffer entry points: successors and deadlock test of explicit states
+// ---------------------------------------------------------------------------------------------
+template <int D>
+__global__ void __launch_bounds__(kBlock) k_expand_plain(const NetView* nets, const int* locs_in, const int* ints_in,
+                                                         const int* zones, int n, int emode,
+                                                         unsigned long long* okey, int* osrc, int* oord, int* olocs,
+                                                         int* oints, int* ozones, long long cap, Ctl* ctl) {
+  Tile<D> t;
+  if (!make_tile(t, threadIdx.x & 31)) return;
+  const NetView& N = nets[0];
+  for (long long f = tile_id<D>(); f < n; f += tile_count<D>()) {
+    int locs[kMaxProcs], ints[kMaxInts];
+    for (int p = 0; p < N.nprocs; ++p) locs[p] = locs_in[f * N.nprocs + p];
+    for (int v = 0; v < N.nints; ++v) ints[v] = ints_in[f * N.nints + v];
+    int src[D];
+    load_rows(t, src, zones + f * D * D);
+    int ord = 0;
+    const bool ok = for_each_successor(N, t, locs, ints, src, emode, [&](const int* tl, const int* ti, const int (&z)[D]) {
+      unsigned long long idx = 0;
+      if (t.i == 0) idx = atomicAdd(&ctl->nsucc, 1ull);
+      idx = t.shfl64(idx, 0);
+      if ((long long)idx < cap) {
+        store_rows(t, z, ozones + (long long)idx * D * D);
+        if (t.i == 0) {
+          okey[idx] = ((unsigned long long)f << 32) | (unsigned)ord;
+          osrc[idx] = (int)f;
+          oord[idx] = ord;
+          for (int p = 0; p < N.nprocs; ++p) olocs[idx * N.nprocs + p] = tl[p];
+          for (int v = 0; v < N.nints; ++v) oints[idx * N.nints + v] = ti[v];
+        }
+      } else if (t.i == 0) {
+        ctl->overflow = 1;
+      }
+      ++ord;
+    });
+    if (!ok && t.i == 0) atomicMax(&ctl->err, 4u);
+  }
+}
+
+template <int D>
+__global__ void __launch_bounds__(kBlock) k_has_deadlock(const NetView* nets, const int* locs_in, const int* ints_in,
+                                                         const int* zones, int n, int* out, Ctl* ctl) {
+  Tile<D> t;
+  if (!make_tile(t, threadIdx.x & 31)) return;
+  DlScratch<D> S;
+  const NetView& N = nets[0];
+  for (long long f = tile_id<D>(); f < n; f += tile_count<D>()) {
+    int locs[kMaxProcs], ints[kMaxInts];
+    for (int p = 0; p < N.nprocs; ++p) locs[p] = locs_in[f * N.nprocs + p];
+    for (int v = 0; v < N.nints; ++v) ints[v] = ints_in[f * N.nints + v];
+    int z[D];
+    load_rows(t, z, zones + f * D * D);
+    const int r = is_empty(t, z) ? 0 : state_has_deadlock(N, t, locs, ints, z, S);
+    if (t.i == 0) {
+      out[f] = r;
+      if (r < 0) atomicMax(&ctl->err, 4u);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------------------------
+inline int grid_for(long long items, int tiles_per_block, int max_blocks) {
+  long long b = (items + tiles_per_block - 1) / tiles_per_block;
+  if (b < 1) b = 1;
+  if (b > max_blocks) b = max_blocks;
+  return (int)b;
+}
+
+template <int D>
+void Level<D>::init(const NetView* nets, int ninst, const int* ok, Store st, Front out, InstState is, Ctl* ctl,
+                    cudaStream_t s) {
+  constexpr int TPB = (kBlock / 32) * (32 / D);
+  k_init<D><<<grid_for(ninst, TPB, 4096), kBlock, 0, s>>>(nets, ninst, ok, st, out, is, ctl);
+}
+template <int D>
+void Level<D>::expand(const NetView* nets, InstState is, Front fr, int nfront, Store st, Succ sc, Ctl* ctl,
+                      int blocks, cudaStream_t s) {
+  constexpr int TPB = (kBlock / 32) * (32 / D);
+  k_expand<D><<<grid_for(nfront, TPB, blocks), kBlock, 0, s>>>(nets, is, fr, nfront, st, sc, ctl);
+}
+template <int D>
+void Level<D>::probe(const NetView* nets, InstState is, Succ sc, Store st, Ctl* ctl, long long nsucc, int blocks,
+                     cudaStream_t s) {
+  constexpr int TPB = (kBlock / 32) * (32 / D);
+  k_probe<D><<<grid_for(nsucc, TPB, blocks), kBlock, 0, s>>>(nets, is, sc, st, ctl, nsucc);
+}
+template <int D>
+void Level<D>::deadlock(const NetView* nets, InstState is, Succ sc, Ctl* ctl, long long nsurv, int blocks,
+                        cudaStream_t s) {
+  constexpr int TPB = (kBlock / 32) * (32 / D);
+  k_deadlock<D><<<grid_for(nsurv, TPB, blocks), kBlock, 0, s>>>(nets, is, sc, ctl, nsurv);
+}
+template <int D>
+void Level<D>::group(Succ sc, Store st, Ctl* ctl, long long nsucc, long long ntouched, cudaStream_t s) {
+  k_seg_alloc<<<grid_for(ntouched, 256, 1024), 256, 0, s>>>(sc, st, ctl, ntouched);
+  k_seg_scatter<<<grid_for(nsucc, 256, 4096), 256, 0, s>>>(sc, st, nsucc);
+}
+template <int D>
+void Level<D>::merge(const NetView* nets, InstState is, Front fr, Succ sc, Store st, Front out, Ctl* ctl,
+                     long long ntouched, int level, int blocks, cudaStream_t s) {
+  constexpr int TPB = (kBlock / 32) * (32 / D);
+  k_merge<D><<<grid_for(ntouched, TPB, blocks), kBlock, 0, s>>>(nets, is, fr, sc, st, out, ctl, ntouched, level);
+}
+template <int D>
+void Level<D>::expand_plain(const NetView* nets, const int* locs, const int* ints, const int* zones, int n, int emode,
+                            unsigned long long* okey, int* osrc, int* oord, int* olocs, int* oints, int* ozones,
+                            long long cap, Ctl* ctl, cudaStream_t s) {
+  constexpr int TPB = (kBlock / 32) * (32 / D);
+  k_expand_plain<D><<<grid_for(n, TPB, 4096), kBlock, 0, s>>>(nets, locs, ints, zones, n, emode, okey, osrc, oord,
+                                                                olocs, oints, ozones, cap, ctl);
+}
+template <int D>
+void Level<D>::has_deadlock(const NetView* nets, const int* locs, const int* ints, const int* zones, int n, int* out,
+                            Ctl* ctl, cudaStream_t s) {
+  constexpr int TPB = (kBlock / 32) * (32 / D);
+  k_has_deadlock<D><<<grid_for(n, TPB, 4096), kBlock, 0, s>>>(nets, locs, ints, zones, n, out, ctl);
+}
+
+}  // namespace hgb

@@ -1,0 +1,180 @@
+"""Python face of the engine, mirroring the reference's query entry points.
+
+Names and argument meanings follow include/hora/reachability.hpp (``reachable_net``),
+include/hora/liveness.hpp (``deadlock_reachable``, ``leads_to_clocks``) and
+include/hora/query.hpp (``check_network_query``). Every call goes through libhora_gb300.so; there
+is no Python or CPU fallback, and a missing library or device raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import enum
+from dataclasses import dataclass, field
+from typing import List, Optional, Sequence, Tuple
+
+import numpy as np
+
+from . import capi
+from .model import (Network, Pred, NetArrays, PredArrays, QueryArrays, Stats, QueryDesc, NetDesc,
+                    Q_REACH, Q_DEADLOCK, Q_LEADSTO)
+
+
+class Backend(enum.IntEnum):
+    """enum class Backend { Seq, Omp, Cuda, Metal } (include/hora/reach.hpp:21)."""
+    Seq = 0
+    Omp = 1
+    Cuda = 2
+    Metal = 3
+
+
+@dataclass
+class ReachStats:
+    """ReachStats (include/hora/reach.hpp:10-19) plus the engine's own counters."""
+    explored: int = 0
+    generated: int = 0
+    expanded: int = 0
+    stored: int = 0
+    keys: int = 0
+    levels: int = 0
+    probes: int = 0
+    kernel_launches: int = 0
+    seconds: float = 0.0
+    device_seconds: float = 0.0
+    extrapolating: bool = False
+    status: int = 0
+    h2d_bytes: int = 0
+    d2h_bytes: int = 0
+    kernels: dict = field(default_factory=dict)   # family -> {"seconds", "calls"}
+
+    def fill(self, st: Stats):
+        for k in ("explored", "generated", "expanded", "stored", "keys", "levels", "probes",
+                  "kernel_launches", "seconds", "device_seconds", "status", "h2d_bytes", "d2h_bytes"):
+            setattr(self, k, getattr(st, k))
+        self.extrapolating = bool(st.extrapolating)
+        self.kernels = {n: {"seconds": st.kernel_seconds[i], "calls": int(st.kernel_calls[i])}
+                        for i, n in enumerate(Stats.KERNELS)}
+        return self
+
+
+def reachable_net(net: Network, target: Pred, backend: Backend = Backend.Cuda,
+                  stats: Optional[ReachStats] = None) -> bool:
+    """E<> target: is a symbolic state matching `target` reachable?"""
+    L = capi.load()
+    na, ta = NetArrays(net), PredArrays(target)
+    st = Stats()
+    res = ctypes.c_int32(0)
+    rc = L.hora_gb_reachable_net(ctypes.addressof(na.desc), ctypes.addressof(ta.desc), int(backend),
+                                 ctypes.byref(st), ctypes.byref(res))
+    if stats is not None:
+        stats.fill(st)
+    capi.check(rc, "reachable_net")
+    return bool(res.value)
+
+
+def deadlock_reachable(net: Network, backend: Backend = Backend.Cuda, stats: Optional[ReachStats] = None,
+                       cancel: Optional[ctypes.c_int32] = None) -> bool:
+    """Is a state containing a deadlocked valuation reachable?  (A[] not deadlock == not this.)"""
+    L = capi.load()
+    na = NetArrays(net)
+    st = Stats()
+    res = ctypes.c_int32(0)
+    rc = L.hora_gb_deadlock_reachable(ctypes.addressof(na.desc), int(backend), ctypes.byref(st),
+                                      ctypes.byref(cancel) if cancel is not None else None, ctypes.byref(res))
+    if stats is not None:
+        stats.fill(st)
+    capi.check(rc, "deadlock_reachable")
+    return bool(res.value)
+
+
+def leads_to_clocks(net: Network, p: Pred, q: Pred, backend: Backend = Backend.Cuda,
+                    stats: Optional[ReachStats] = None) -> bool:
+    """p --> q, both sides conjunctions that may carry clock atoms."""
+    L = capi.load()
+    na, pa, qa = NetArrays(net), PredArrays(p), PredArrays(q)
+    st = Stats()
+    res = ctypes.c_int32(0)
+    rc = L.hora_gb_leads_to(ctypes.addressof(na.desc), ctypes.addressof(pa.desc), ctypes.addressof(qa.desc),
+                            int(backend), ctypes.byref(st), ctypes.byref(res))
+    if stats is not None:
+        stats.fill(st)
+    capi.check(rc, "leads_to")
+    return bool(res.value)
+
+
+def check_network_query(net: Network, kind: int, p: Pred, q: Optional[Pred] = None, negate: bool = False,
+                        backend: Backend = Backend.Cuda, stats: Optional[ReachStats] = None) -> bool:
+    """Route one lowered query (check_network_query, src/query/dispatch.cpp:109-607).
+
+    ``kind`` is Q_REACH (E<> p; ``negate`` gives A[] not p), Q_DEADLOCK (``negate`` gives
+    A[] not deadlock) or Q_LEADSTO (p --> q). Returns whether the formula is satisfied.
+    """
+    if kind == Q_REACH:
+        r = reachable_net(net, p, backend, stats)
+    elif kind == Q_DEADLOCK:
+        r = deadlock_reachable(net, backend, stats)
+    elif kind == Q_LEADSTO:
+        r = leads_to_clocks(net, p, q or Pred(), backend, stats)
+    else:
+        raise ValueError(kind)
+    return (not r) if negate else r
+
+
+def expand(net: Network, locs, ints, zones, L, U, qmask=None, emode: int = 0, cap: Optional[int] = None):
+    """Successor pipeline on explicit states (hora_gb_expand): dict of arrays in emission order."""
+    lib = capi.load()
+    na = NetArrays(net)
+    dim, np_, ni = net.dim, len(net.procs), len(net.ints)
+    locs = np.ascontiguousarray(locs, np.int32).reshape(-1, np_)
+    n = locs.shape[0]
+    ints = np.ascontiguousarray(ints, np.int32).reshape(n, ni) if ni else np.zeros((n, 1), np.int32)
+    zones = np.ascontiguousarray(zones, np.int32).reshape(n, dim, dim)
+    L = np.ascontiguousarray(L, np.int32)
+    U = np.ascontiguousarray(U, np.int32)
+    qm = np.zeros(dim, np.uint8) if qmask is None else np.ascontiguousarray(qmask, np.uint8)
+    cap = cap or max(16, n * 64)
+    while True:
+        o_src = np.zeros(cap, np.int32); o_ord = np.zeros(cap, np.int32)
+        o_locs = np.zeros((cap, np_), np.int32); o_ints = np.zeros((cap, max(ni, 1)), np.int32)
+        o_z = np.zeros((cap, dim, dim), np.int32)
+        out_n = ctypes.c_int64(0)
+        rc = lib.hora_gb_expand(ctypes.addressof(na.desc), n, capi.p32(locs), capi.p32(ints), capi.p32(zones),
+                                capi.p32(L), capi.p32(U), qm.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)), emode,
+                                cap, capi.p32(o_src), capi.p32(o_ord), capi.p32(o_locs), capi.p32(o_ints),
+                                capi.p32(o_z), ctypes.byref(out_n))
+        if rc == capi.E_OVERFLOW:
+            cap = int(out_n.value)
+            continue
+        capi.check(rc, "expand")
+        k = int(out_n.value)
+        return {"src": o_src[:k], "ord": o_ord[:k], "locs": o_locs[:k], "ints": o_ints[:k, :ni], "zones": o_z[:k]}
+
+
+def has_deadlock(net: Network, locs, ints, zones) -> np.ndarray:
+    lib = capi.load()
+    na = NetArrays(net)
+    dim, np_, ni = net.dim, len(net.procs), len(net.ints)
+    locs = np.ascontiguousarray(locs, np.int32).reshape(-1, np_)
+    n = locs.shape[0]
+    ints = np.ascontiguousarray(ints, np.int32).reshape(n, ni) if ni else np.zeros((n, 1), np.int32)
+    zones = np.ascontiguousarray(zones, np.int32).reshape(n, dim, dim)
+    out = np.zeros(n, np.int32)
+    rc = lib.hora_gb_has_deadlock(ctypes.addressof(na.desc), n, capi.p32(locs), capi.p32(ints), capi.p32(zones),
+                                  capi.p32(out))
+    capi.check(rc, "has_deadlock")
+    return out.astype(bool)
+
+
+def batch_run(items: Sequence[Tuple[Network, int, Pred, Pred]]):
+    """Run (network, kind, p, q) instances together; returns (verdicts, [stats dict])."""
+    lib = capi.load()
+    n = len(items)
+    nas = [NetArrays(it[0]) for it in items]
+    qas = [QueryArrays(it[1], it[2], it[3]) for it in items]
+    nets = (NetDesc * max(n, 1))(*[a.desc for a in nas])
+    qs = (QueryDesc * max(n, 1))(*[a.desc for a in qas])
+    verdicts = np.zeros(max(n, 1), np.int32)
+    stats = (Stats * max(n, 1))()
+    rc = lib.hora_gb_batch_run(n, ctypes.addressof(nets), ctypes.addressof(qs), capi.p32(verdicts),
+                               ctypes.addressof(stats))
+    capi.check(rc, "batch_run")
+    return verdicts[:n].tolist(), [stats[k].as_dict() for k in range(n)]

@@ -218,10 +218,16 @@ class Stats(ctypes.Structure):
                 ("pre_calls", ctypes.c_uint64), ("gfp_iters", ctypes.c_uint64),
                 ("kernel_launches", ctypes.c_uint64), ("seconds", ctypes.c_double),
                 ("device_seconds", ctypes.c_double), ("extrapolating", ctypes.c_int32),
-                ("status", ctypes.c_int32)]
+                ("status", ctypes.c_int32), ("kernel_seconds", ctypes.c_double * 6),
+                ("kernel_calls", ctypes.c_uint64 * 6), ("h2d_bytes", ctypes.c_uint64),
+                ("d2h_bytes", ctypes.c_uint64)]
+    KERNELS = ("expand", "probe", "deadlock", "group", "merge", "other")
 
     def as_dict(self):
-        return {k: getattr(self, k) for k, _ in self._fields_}
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k not in ("kernel_seconds", "kernel_calls")}
+        d["kernel_seconds"] = {n: self.kernel_seconds[i] for i, n in enumerate(self.KERNELS)}
+        d["kernel_calls"] = {n: int(self.kernel_calls[i]) for i, n in enumerate(self.KERNELS)}
+        return d
 
 
 def _i32(a) -> np.ndarray:

@@ -241,7 +241,7 @@ def main(ref: str):
     tables = sorted(f for f in os.listdir(os.path.join(ref, "tests/uppaal-differential")) if f.endswith(".txt"))
     for tab in tables:
         for line in open(os.path.join(ref, "tests/uppaal-differential", tab)):
-            cols = [c.strip() for c in line.split("|")]
+            cols = [c.strip() for c in line.split("|", 3)]
             if len(cols) < 4 or cols[0] != "ok":
                 continue
             v = cols[1].split()

@@ -1,0 +1,70 @@
+"""CPU-side checks of the C ABI: the library loads, exports every declared entry point, and rejects
+bad or out-of-scope input before touching a device."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from ptctcl_gb300 import capi
+from ptctcl_gb300.model import NetArrays, PredArrays, Stats, Pred, Network, Process, Location, Edge, c_le
+from golden_util import load_model
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    syms = set()
+    for f in os.listdir(os.path.join(ROOT, "include")):
+        if f.endswith(".h"):
+            syms |= set(re.findall(r"HORA_GB_API\s+[\w\s\*]+?\b(hora_gb_\w+)\s*\(", open(os.path.join(ROOT, "include", f)).read()))
+    return syms
+
+
+def test_library_exports_every_declared_symbol():
+    lib = capi.load()
+    syms = declared_symbols()
+    assert syms >= set(capi.EXPORTS) - {"hora_gb_run_no_alloc"}
+    for s in syms:
+        assert hasattr(lib, s), s
+    assert lib.hora_gb_abi_version() == 1
+
+
+def test_invalid_and_unsupported_inputs_are_rejected_without_a_device():
+    lib = capi.load()
+    res = ctypes.c_int32(7)
+    st = Stats()
+    # backend other than CUDA: the caller keeps its own engine
+    net = load_model("fischer4")
+    na, ta = NetArrays(net), PredArrays(Pred([(0, 3)]))
+    rc = lib.hora_gb_reachable_net(ctypes.addressof(na.desc), ctypes.addressof(ta.desc), capi.BACKEND_OMP,
+                                   ctypes.byref(st), ctypes.byref(res))
+    assert rc == capi.E_NOT_SUPPORTED
+    # diagonal constraint: out of scope, like the reference's CUDA factory
+    diag = Network(2, [Process("P", [Location("A", [(1, 2, (3 << 1) | 1)])], [], 0)])
+    na2 = NetArrays(diag)
+    rc = lib.hora_gb_reachable_net(ctypes.addressof(na2.desc), ctypes.addressof(ta.desc), capi.BACKEND_CUDA,
+                                   ctypes.byref(st), ctypes.byref(res))
+    assert rc == capi.E_NOT_SUPPORTED and "diagonal" in capi.last_error()
+    # target location out of range
+    bad = PredArrays(Pred([(0, 99)]))
+    rc = lib.hora_gb_reachable_net(ctypes.addressof(na.desc), ctypes.addressof(bad.desc), capi.BACKEND_CUDA,
+                                   ctypes.byref(st), ctypes.byref(res))
+    assert rc == capi.E_INVALID
+    # more than 16 clocks
+    wide = Network(17, [Process("P", [Location("A", [c_le(17, 3)])], [], 0)])
+    na3 = NetArrays(wide)
+    rc = lib.hora_gb_deadlock_reachable(ctypes.addressof(na3.desc), capi.BACKEND_CUDA, ctypes.byref(st), None,
+                                        ctypes.byref(res))
+    assert rc == capi.E_NOT_SUPPORTED
+
+
+@pytest.mark.skipif(capi.device_count() > 0, reason="needs a machine without a CUDA device")
+def test_no_device_is_an_error_not_a_fallback():
+    lib = capi.load()
+    net = load_model("fischer4")
+    na, ta = NetArrays(net), PredArrays(Pred([(0, 3)]))
+    res = ctypes.c_int32(0)
+    rc = lib.hora_gb_reachable_net(ctypes.addressof(na.desc), ctypes.addressof(ta.desc), capi.BACKEND_CUDA, None,
+                                   ctypes.byref(res))
+    assert rc == capi.E_NO_DEVICE

@@ -1,0 +1,133 @@
+"""GPU parity: the CUDA engine against the CPU oracle, through the C ABI.
+
+* successor pipeline: bit-exact successor DBMs, target locations/integers and emission order per
+  source state (exact zones and Extra_LU+), on states sampled from every configuration shape;
+* deadlock predicate: identical answer per state;
+* whole queries: identical verdicts, and -- because both engines insert each level in the same
+  canonical order -- identical explored / generated / stored / key / level counts;
+* the reference's recorded verdicts (tests/golden) on the GPU.
+"""
+import numpy as np
+import pytest
+
+from oracle import pyoracle
+from ptctcl_gb300 import engine
+from ptctcl_gb300.engine import Backend, ReachStats
+from ptctcl_gb300.generator import config_instance
+from ptctcl_gb300.model import Pred
+from golden_util import load_model, verdict_rows
+from states import sample_states
+
+pytestmark = pytest.mark.gpu
+
+# config-4 seeds whose whole query the single-threaded oracle finishes in well under a second
+C4_SMALL = [0, 1, 2, 3, 4, 5, 8, 9, 12, 13, 14, 18, 19, 22, 23, 25, 26]
+NETS = [("c1", 1, s) for s in range(6)] + [("c2", 2, s) for s in (0, 3, 10, 23)] + \
+       [("c3", 3, s) for s in range(3)] + [("c4", 4, s) for s in C4_SMALL[:8] + [6, 10, 17, 21]]
+
+
+def _net(cfg, seed):
+    return config_instance(cfg, seed)[0]
+
+
+@pytest.mark.parametrize("name,cfg,seed", NETS, ids=[f"{n}-{s}" for n, _, s in NETS])
+@pytest.mark.parametrize("emode", [0, 1])
+def test_expand_bit_exact(name, cfg, seed, emode):
+    net = _net(cfg, seed)
+    smp = sample_states(net, nmax=120, depth=5)
+    if smp is None:
+        pytest.skip("no initial state")
+    locs, ints, zones, L, U = smp
+    want = pyoracle.expand(net, locs, ints, zones, L, U, None, emode)
+    got = engine.expand(net, locs, ints, zones, L, U, None, emode)
+    assert len(got["src"]) == len(want["src"])
+    for k in ("src", "ord", "locs", "ints", "zones"):
+        np.testing.assert_array_equal(got[k], want[k], err_msg=k)
+
+
+@pytest.mark.parametrize("name,cfg,seed", NETS, ids=[f"{n}-{s}" for n, _, s in NETS])
+def test_deadlock_predicate(name, cfg, seed):
+    net = _net(cfg, seed)
+    smp = sample_states(net, nmax=120, depth=5)
+    if smp is None:
+        pytest.skip("no initial state")
+    locs, ints, zones, _, _ = smp
+    want = pyoracle.has_deadlock(net, locs, ints, zones)
+    got = engine.has_deadlock(net, locs, ints, zones)
+    np.testing.assert_array_equal(got, want)
+
+
+COUNT_KEYS = ("explored", "generated", "stored", "keys", "levels")
+
+
+def _compare(got, gst, want, wst):
+    assert got == want
+    for k in COUNT_KEYS:
+        assert getattr(gst, k) == wst[k], (k, getattr(gst, k), wst[k])
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_reach_config1(seed):
+    net, kind, p, q = config_instance(1, seed)
+    want, wst = pyoracle.reachable_net(net, p)
+    st = ReachStats()
+    got = engine.reachable_net(net, p, Backend.Cuda, st)
+    _compare(got, st, want, wst)
+
+
+@pytest.mark.parametrize("seed", [0, 3, 4, 9, 10, 14, 16, 23, 145])
+def test_deadlock_config2(seed):
+    net = config_instance(2, seed)[0]
+    want, wst = pyoracle.deadlock_reachable(net)
+    st = ReachStats()
+    got = engine.deadlock_reachable(net, Backend.Cuda, st)
+    _compare(got, st, want, wst)
+
+
+@pytest.mark.parametrize("seed", C4_SMALL)
+def test_mixed_config4(seed):
+    net, kind, p, q = config_instance(4, seed)
+    if kind == 2:
+        pytest.skip("leads-to")
+    st = ReachStats()
+    if kind == 0:
+        want, wst = pyoracle.reachable_net(net, p)
+        got = engine.reachable_net(net, p, Backend.Cuda, st)
+    else:
+        want, wst = pyoracle.deadlock_reachable(net)
+        got = engine.deadlock_reachable(net, Backend.Cuda, st)
+    _compare(got, st, want, wst)
+
+
+ROWS = verdict_rows(kinds=(0, 1))
+
+
+@pytest.mark.parametrize("model,formula,kind,p,q,result", ROWS, ids=[f"{r[0]}:{r[1]}" for r in ROWS])
+def test_reference_verdicts_gpu(model, formula, kind, p, q, result):
+    net = load_model(model)
+    st = ReachStats()
+    if kind == 0:
+        got = engine.reachable_net(net, p, Backend.Cuda, st)
+        want, wst = pyoracle.reachable_net(net, p)
+    else:
+        got = engine.deadlock_reachable(net, Backend.Cuda, st)
+        want, wst = pyoracle.deadlock_reachable(net)
+    assert got == result
+    _compare(got, st, want, wst)
+
+
+def test_batch_matches_single():
+    items = []
+    for seed in C4_SMALL:
+        net, kind, p, q = config_instance(4, seed)
+        if kind != 2:
+            items.append((net, kind, p, q))
+    verdicts, stats = engine.batch_run(items)
+    for (net, kind, p, q), v, s in zip(items, verdicts, stats):
+        if kind == 0:
+            want, wst = pyoracle.reachable_net(net, p)
+        else:
+            want, wst = pyoracle.deadlock_reachable(net)
+        assert v == int(want)
+        for k in COUNT_KEYS:
+            assert s[k] == wst[k], (k, s[k], wst[k])
