@@ -53,6 +53,16 @@ struct NetView {
   const int* t_loc;
   const int* t_int;
   const int* t_clk;
+  // leads-to: restriction of the successor pipeline to !q, and p's conjunction
+  int av_on;                   // 1: cut successors to !q where q's discrete part holds
+  int av_nloc, av_nint, av_nclk;
+  const int* av_loc;
+  const int* av_int;
+  int av_neg[3];               // complement of q's single clock atom
+  int p_nloc, p_nint, p_nclk;
+  const int* p_loc;
+  const int* p_int;
+  const int* p_clk;
 };
 
 // Device-side counters, read back with a single copy. The first block is reset at every level.
@@ -68,10 +78,11 @@ struct Ctl {
   unsigned long long nnodes;     // passed-store nodes allocated
   unsigned long long nkeys;      // distinct keys holding at least one stored zone
   unsigned long long nslots;     // occupied hash slots
+  unsigned long long nedges;     // graph edges recorded (leads-to graph mode)
   unsigned long long probes;     // stored zones read by the probe and the merge
   long long nlive;               // live passed-store zones
   unsigned int err;              // HORA_E_* raised on the device (table full, escape overflow)
-  unsigned int pad;
+  unsigned int flag;             // set by a fixpoint pass that changed something
 };
 constexpr unsigned long long kCtlLevelBytes = 5 * 8 + 2 * 4;
 

@@ -129,16 +129,36 @@ template <int D>
 __device__ __forceinline__ void apply_resets(const NetView& N, const Tile<D>& t, int (&r)[D], int e) {
   for (int q = N.edge_reset_off[e]; q < N.edge_reset_off[e + 1]; ++q) reset(t, r, N.resets[q]);
 }
-// close_succ_zone without an avoid set (semantics.hpp:522-568). False when the target invariant
-// is unsatisfiable; the caller tests emptiness afterwards.
+__device__ __forceinline__ bool pred_disc(const int* loc, int nloc, const int* ia, int nint, const int* locs,
+                                          const int* ints) {
+  for (int k = 0; k < nloc; ++k)
+    if (locs[loc[2 * k]] != loc[2 * k + 1]) return false;
+  return iatoms_ok(ia, nint, ints);
+}
+// Leads-to restriction to !q: where q's discrete part holds, cut the zone to the complement of
+// q's clock atom (a single constraint, so the complement is convex and the cut exact). False when
+// nothing is left -- including everywhere q is purely discrete.
+template <int D>
+__device__ __forceinline__ bool avoid_cut(const NetView& N, const Tile<D>& t, int (&r)[D], const int* tl,
+                                          const int* ti) {
+  if (!N.av_on || !pred_disc(N.av_loc, N.av_nloc, N.av_int, N.av_nint, tl, ti)) return true;
+  if (N.av_nclk == 0) return false;
+  return constrain(t, r, N.av_neg[0], N.av_neg[1], N.av_neg[2]);
+}
+
+// close_succ_zone (semantics.hpp:522-568), with the leads-to restriction adjoined to the target
+// invariant when it is on. False when the target invariant is unsatisfiable; the caller tests
+// emptiness afterwards.
 template <int D>
 __device__ bool close_succ(const NetView& N, const Tile<D>& t, int (&r)[D], const int* tl, const int* ti, int emode) {
   if (!apply_inv(N, t, r, tl)) return false;
+  if (!avoid_cut(N, t, r, tl, ti)) return false;
   bool c, u;
   frozen_flags(N, tl, ti, c, u);
   if (!c && !u) {
     delay(t, r);
     apply_inv(N, t, r, tl);
+    avoid_cut(N, t, r, tl, ti);
   }
   // reset_inactive (semantics.hpp:186-215)
   unsigned long long a = N.qmask;
@@ -571,6 +591,57 @@ __device__ int state_has_deadlock(const NetView& N, const Tile<D>& t, const int*
     }
   }
   return 0;
+}
+
+// ---------------------------------------------------------------------------------------------
+// End-of-run tests of the leads-to sweep (src/liveness/construction.cpp:1097-1177)
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ bool has_upper_invariant(const NetView& N, const int* locs) {
+  for (int p = 0; p < N.nprocs; ++p) {
+    const int gl = N.loc_base[p] + locs[p];
+    for (int c = N.loc_inv_off[gl]; c < N.loc_inv_off[gl + 1]; ++c)
+      if (N.cons[3 * c] > 0 && N.cons[3 * c + 1] == 0 && N.cons[3 * c + 2] < kInf) return true;
+  }
+  return false;
+}
+// time_diverges: every clock unbounded after a delay inside the invariant (and, `restricted`,
+// inside !q too).
+template <int D>
+__device__ bool time_diverges(const NetView& N, const Tile<D>& t, const int* locs, const int* ints,
+                              const int (&zone)[D], bool restricted) {
+  if (N.nclocks == 0 || has_upper_invariant(N, locs)) return false;
+  bool c, u;
+  frozen_flags(N, locs, ints, c, u);
+  if (c || u) return false;
+  int z[D];
+#pragma unroll
+  for (int j = 0; j < D; ++j) z[j] = zone[j];
+  delay(t, z);
+  if (!apply_inv(N, t, z, locs) || is_empty(t, z)) return false;
+  if (!t.all(t.i == 0 || z[0] >= kInf)) return false;
+  if (restricted && N.av_on && pred_disc(N.av_loc, N.av_nloc, N.av_int, N.av_nint, locs, ints)) {
+#pragma unroll
+    for (int j = 0; j < D; ++j) z[j] = zone[j];
+    if (!avoid_cut(N, t, z, locs, ints)) return false;
+    delay(t, z);
+    if (!apply_inv(N, t, z, locs) || !avoid_cut(N, t, z, locs, ints) || is_empty(t, z)) return false;
+    return t.all(t.i == 0 || z[0] >= kInf);
+  }
+  return true;
+}
+// orig_time_open: can time run away at these locations in the unrestricted system?
+template <int D>
+__device__ bool orig_time_open(const NetView& N, const Tile<D>& t, const int* locs, const int* ints) {
+  if (N.nclocks == 0 || has_upper_invariant(N, locs)) return false;
+  bool c, u;
+  frozen_flags(N, locs, ints, c, u);
+  if (c || u) return false;
+  int z[D];
+#pragma unroll
+  for (int j = 0; j < D; ++j) z[j] = (j == t.i || t.i == 0) ? kZeroLe : kInf;
+  delay(t, z);
+  if (!apply_inv(N, t, z, locs)) return false;
+  return t.all(t.i == 0 || z[0] >= kInf);
 }
 
 // ---------------------------------------------------------------------------------------------

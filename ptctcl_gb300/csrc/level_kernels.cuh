@@ -20,6 +20,12 @@ struct Store {
   int* nlevel;                // [ncap]
   int* ndead;                 // [ncap]
   int* ninst;                 // [ncap]
+  unsigned long long* nkey;   // [ncap] hash key of the node's discrete state
+};
+struct Edges {                // zone-graph edges (leads-to graph mode)
+  int* src;
+  int* dst;
+  long long cap;
 };
 struct Succ {                 // successors of the current level
   unsigned long long* key;    // hash key
@@ -53,17 +59,27 @@ struct InstState {            // per-instance device state (one entry per instan
 
 template <int D>
 struct Level {
+  // mode: 0 = a_LU subsumption store (reach, deadlock, leads-to phase 1),
+  //       1 = exact-zone graph store with edges (leads-to phase 2)
   static void init(const NetView* nets, int ninst, const int* inst_dim_ok, Store st, Front out, InstState is,
                    Ctl* ctl, cudaStream_t s);
-  static void expand(const NetView* nets, InstState is, Front fr, int nfront, Store st, Succ sc, Ctl* ctl,
-                     int blocks, cudaStream_t s);
-  static void probe(const NetView* nets, InstState is, Succ sc, Store st, Ctl* ctl, long long nsucc,
+  static void expand(const NetView* nets, InstState is, Front fr, int nfront, const int* src_zone, Succ sc, Ctl* ctl,
+                     int roots, int blocks, cudaStream_t s);
+  static void probe(const NetView* nets, InstState is, Succ sc, Store st, Ctl* ctl, long long nsucc, int mode,
                     int blocks, cudaStream_t s);
   static void deadlock(const NetView* nets, InstState is, Succ sc, Ctl* ctl, long long nsurv, int blocks,
                        cudaStream_t s);
   static void group(Succ sc, Store st, Ctl* ctl, long long nsucc, long long ntouched, cudaStream_t s);
   static void merge(const NetView* nets, InstState is, Front fr, Succ sc, Store st, Front out, Ctl* ctl,
-                    long long ntouched, int level, int blocks, cudaStream_t s);
+                    long long ntouched, int level, int mode, Edges ed, int record, int blocks, cudaStream_t s);
+  // leads-to: phase-1 nodes whose discrete state satisfies p, as a frontier
+  static void collect_p(const NetView* nets, Store st, long long nnodes, Front out, Ctl* ctl, cudaStream_t s);
+  // leads-to: end-of-run flags and the greatest-fixpoint sweep over the recorded graph
+  static void stop(const NetView* nets, Store st, long long nnodes, int* stop, Ctl* ctl, int blocks, cudaStream_t s);
+  static void gfp_pass(Edges ed, long long nedges, long long nnodes, const int* stop, int* W, int* F, Ctl* ctl,
+                       cudaStream_t s);
+  static void gfp_verdict(const NetView* nets, Store st, long long nnodes, const int* W, InstState is, Ctl* ctl,
+                          cudaStream_t s);
   // Host-buffer successor pipeline (hora_gb_expand): states given as frontier + node zones.
   static void expand_plain(const NetView* nets, const int* locs, const int* ints, const int* zones, int n,
                            int emode, unsigned long long* okey, int* osrc, int* oord, int* olocs, int* oints,

@@ -85,7 +85,7 @@ __global__ void __launch_bounds__(kBlock) k_init(const NetView* nets, int ninst,
     if (slot < 0) { if (t.i == 0) atomicMax(&ctl->err, 4u); continue; }
     store_rows(t, z, st.nzone + node * D * D);
     if (t.i == 0) {
-      st.nnext[node] = -1; st.nlevel[node] = 0; st.ndead[node] = 0; st.ninst[node] = inst;
+      st.nnext[node] = -1; st.nlevel[node] = 0; st.ndead[node] = 0; st.ninst[node] = inst; st.nkey[node] = hk;
       st.head[slot] = (int)node;
       const unsigned long long f = atomicAdd(&ctl->nfront, 1ull);
       out.key[f] = hk; out.node[f] = (int)node; out.rank[f] = 0; out.inst[f] = inst;
@@ -102,7 +102,7 @@ __global__ void __launch_bounds__(kBlock) k_init(const NetView* nets, int ninst,
 // ---------------------------------------------------------------------------------------------
 template <int D>
 __global__ void __launch_bounds__(kBlock) k_expand(const NetView* nets, InstState is, Front fr, int nfront,
-                                                   Store st, Succ sc, Ctl* ctl) {
+                                                   const int* src_zone, Succ sc, Ctl* ctl, int roots) {
   Tile<D> t;
   if (!make_tile(t, threadIdx.x & 31)) return;
   for (long long f = tile_id<D>(); f < nfront; f += tile_count<D>()) {
@@ -113,11 +113,11 @@ __global__ void __launch_bounds__(kBlock) k_expand(const NetView* nets, InstStat
     int locs[kMaxProcs], ints[kMaxInts];
     key_decode(N, key_part(hk, N.inst_shift), locs, ints);
     int src[D];
-    load_rows(t, src, st.nzone + (long long)fr.node[f] * D * D);
+    load_rows(t, src, src_zone + (long long)fr.node[f] * D * D);
     const int emode = is.emode[inst];
     int ord = 0;
     bool hit = false;
-    const bool ok = for_each_successor(N, t, locs, ints, src, emode, [&](const int* tl, const int* ti, const int (&z)[D]) {
+    auto emit = [&](const int* tl, const int* ti, const int (&z)[D]) {
       unsigned long long idx = 0;
       if (t.i == 0) idx = atomicAdd(&ctl->nsucc, 1ull);
       idx = t.shfl64(idx, 0);
@@ -133,7 +133,15 @@ __global__ void __launch_bounds__(kBlock) k_expand(const NetView* nets, InstStat
       }
       ++ord;
       if (N.kind == 0 && !hit) hit = target_hit(N, t, z, tl, ti);
-    });
+    };
+    bool ok = true;
+    if (roots) {
+      // leads-to roots: the p-part of a phase-1 zone, cut to !q
+      if (apply_cons(t, src, N.p_clk, 0, N.p_nclk) && avoid_cut(N, t, src, locs, ints) && !is_empty(t, src))
+        emit(locs, ints, src);
+    } else {
+      ok = for_each_successor(N, t, locs, ints, src, emode, emit);
+    }
     if (t.i == 0) {
       if (!ok) atomicMax(&ctl->err, 4u);
       if (ord) atomicAdd(&is.generated[inst], (unsigned long long)ord);
@@ -147,7 +155,7 @@ __global__ void __launch_bounds__(kBlock) k_expand(const NetView* nets, InstStat
 // ---------------------------------------------------------------------------------------------
 template <int D>
 __global__ void __launch_bounds__(kBlock) k_probe(const NetView* nets, InstState is, Succ sc, Store st, Ctl* ctl,
-                                                  long long nsucc) {
+                                                  long long nsucc, int mode) {
   Tile<D> t;
   if (!make_tile(t, threadIdx.x & 31)) return;
   const int ishift = nets[0].inst_shift;
@@ -177,7 +185,7 @@ __global__ void __launch_bounds__(kBlock) k_probe(const NetView* nets, InstState
     if (slot < 0) { if (t.i == 0) { atomicMax(&ctl->err, 4u); sc.slot[s] = -1; } continue; }
     bool killed = false;
     unsigned long long nprobe = 0;
-    if (!inserted) {
+    if (!inserted && mode == 0) {
       for (int n = __ldg(st.head + slot); n >= 0; n = __ldg(st.nnext + n)) {
         if (__ldg(st.ndead + n)) continue;
         int zp[D];
@@ -260,7 +268,8 @@ __device__ __forceinline__ bool order_less(const Front& fr, const Succ& sc, int 
 
 template <int D>
 __global__ void __launch_bounds__(kBlock) k_merge(const NetView* nets, InstState is, Front fr, Succ sc, Store st,
-                                                  Front out, Ctl* ctl, long long ntouched, int level) {
+                                                  Front out, Ctl* ctl, long long ntouched, int level, int mode,
+                                                  Edges ed, int record) {
   Tile<D> t;
   if (!make_tile(t, threadIdx.x & 31)) return;
   const int ishift = nets[0].inst_shift;
@@ -292,6 +301,45 @@ __global__ void __launch_bounds__(kBlock) k_merge(const NetView* nets, InstState
       load_rows(t, z, sc.zone + (long long)a * D * D);
 #pragma unroll
       for (int x = 0; x < D; ++x) z0[x] = t.shfl(z[x], 0);
+      if (mode == 1) {
+        // exact-zone graph: find the identical zone or store a new node, then record the edge
+        int hit = -1;
+        for (int m = ((volatile int*)st.head)[s]; m >= 0; m = ((volatile int*)st.nnext)[m]) {
+          int zp[D];
+          load_rows_rw(t, zp, st.nzone + (long long)m * D * D);
+          bool eq = true;
+#pragma unroll
+          for (int j = 0; j < D; ++j) eq &= zp[j] == z[j];
+          if (t.all(eq)) { hit = m; break; }
+        }
+        if (hit < 0) {
+          long long node = 0;
+          if (t.i == 0) node = (long long)atomicAdd(&ctl->nnodes, 1ull);
+          node = (long long)t.shfl64((unsigned long long)node, 0);
+          store_rows(t, z, st.nzone + node * D * D);
+          t.sync();
+          if (t.i == 0) {
+            const int old_head = ((volatile int*)st.head)[s];
+            if (old_head < 0) { atomicAdd(&ctl->nkeys, 1ull); atomicAdd(&is.nkeys[inst], 1ull); }
+            st.nnext[node] = old_head;
+            st.nlevel[node] = level;
+            st.ndead[node] = 0;
+            st.ninst[node] = inst;
+            st.nkey[node] = hk;
+            __threadfence_block();
+            ((volatile int*)st.head)[s] = (int)node;
+          }
+          ++dlive;
+          hit = (int)node;
+          t.sync();
+        }
+        if (record && t.i == 0) {
+          const unsigned long long e = atomicAdd(&ctl->nedges, 1ull);
+          if ((long long)e < ed.cap) { ed.src[e] = fr.node[sc.parent[a]]; ed.dst[e] = hit; }
+          else atomicMax(&ctl->err, 4u);
+        }
+        continue;
+      }
       // (1)+(2): dropped if a stored zone simulates it
       bool drop = false;
       for (int m = ((volatile int*)st.head)[s]; m >= 0; m = ((volatile int*)st.nnext)[m]) {
@@ -348,6 +396,7 @@ __global__ void __launch_bounds__(kBlock) k_merge(const NetView* nets, InstState
         st.nlevel[node] = level;
         st.ndead[node] = 0;
         st.ninst[node] = inst;
+        st.nkey[node] = hk;
         __threadfence_block();
         ((volatile int*)st.head)[s] = (int)node;
       }
@@ -372,6 +421,90 @@ __global__ void __launch_bounds__(kBlock) k_merge(const NetView* nets, InstState
     }
     t.sync();
   }
+}
+
+// ---------------------------------------------------------------------------------------------
+// leads-to: roots, end-of-run flags, greatest fixpoint
+// ---------------------------------------------------------------------------------------------
+// Phase-1 nodes whose discrete state satisfies p become the root frontier (one thread per node).
+static __global__ void k_collect_p(const NetView* nets, Store st, long long nnodes, Front out, Ctl* ctl) {
+  const int ishift = nets[0].inst_shift;
+  for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < nnodes; n += (long long)gridDim.x * blockDim.x) {
+    if (st.ndead[n]) continue;
+    const unsigned long long hk = st.nkey[n];
+    const int inst = (int)(hk >> ishift);
+    const NetView& N = nets[inst];
+    if (N.kind != 2) continue;
+    int locs[kMaxProcs], ints[kMaxInts];
+    key_decode(N, key_part(hk, ishift), locs, ints);
+    if (!pred_disc(N.p_loc, N.p_nloc, N.p_int, N.p_nint, locs, ints)) continue;
+    const unsigned long long f = atomicAdd(&ctl->nfront, 1ull);
+    out.key[f] = hk; out.node[f] = (int)n; out.rank[f] = 0; out.inst[f] = inst;
+  }
+}
+
+// stop_set (src/liveness/construction.cpp:1200-1239) of every graph node, as a flag: the node holds
+// a valuation whose run may end here.
+template <int D>
+__global__ void __launch_bounds__(kBlock) k_stop(const NetView* nets, Store st, long long nnodes, int* stop, Ctl* ctl) {
+  Tile<D> t;
+  if (!make_tile(t, threadIdx.x & 31)) return;
+  DlScratch<D> S;
+  const int ishift = nets[0].inst_shift;
+  for (long long n = tile_id<D>(); n < nnodes; n += tile_count<D>()) {
+    const unsigned long long hk = st.nkey[n];
+    const int inst = (int)(hk >> ishift);
+    const NetView& N = nets[inst];
+    int locs[kMaxProcs], ints[kMaxInts];
+    key_decode(N, key_part(hk, ishift), locs, ints);
+    int z[D];
+    load_rows(t, z, st.nzone + n * D * D);
+    int r = 0;
+    if (N.av_nclk == 0) {
+      // unrestricted: no successor at all, time divergence, or a deadlocked valuation
+      NetView U = N;
+      U.av_on = 0;
+      int cnt = 0;
+      const bool ok = for_each_successor(U, t, locs, ints, z, 1, [&](const int*, const int*, const int (&)[D]) { ++cnt; });
+      if (!ok) { if (t.i == 0) atomicMax(&ctl->err, 4u); continue; }
+      if (cnt == 0 || time_diverges(N, t, locs, ints, z, false)) r = 1;
+      else {
+        const int d = state_has_deadlock(N, t, locs, ints, z, S);
+        if (d < 0) { if (t.i == 0) atomicMax(&ctl->err, 4u); continue; }
+        r = d;
+      }
+    } else {
+      // restricted: divergence inside !q, or a genuine timelock of the unrestricted system
+      if (time_diverges(N, t, locs, ints, z, true)) r = 1;
+      else if (orig_time_open(N, t, locs, ints)) r = 0;
+      else {
+        const int d = state_has_deadlock(N, t, locs, ints, z, S);
+        if (d < 0) { if (t.i == 0) atomicMax(&ctl->err, 4u); continue; }
+        r = d;
+      }
+    }
+    if (t.i == 0) stop[n] = r;
+  }
+}
+
+// One Jacobi pass of W = W /\ (stop \/ exists edge into W): mark sources with a successor in W...
+static __global__ void k_gfp_mark(Edges ed, long long nedges, const int* W, int* F) {
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nedges; e += (long long)gridDim.x * blockDim.x)
+    if (W[ed.dst[e]]) F[ed.src[e]] = 1;
+}
+// ... then keep a node only if it stops or kept such a successor.
+static __global__ void k_gfp_update(long long nnodes, const int* stop, int* W, int* F, Ctl* ctl) {
+  for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < nnodes; n += (long long)gridDim.x * blockDim.x) {
+    const int w = W[n] && (stop[n] || F[n]);
+    if (w != W[n]) { W[n] = w; ctl->flag = 1; }
+    F[n] = 0;
+  }
+}
+// Violated iff a root (a level-0 node of the graph) survives.
+static __global__ void k_gfp_verdict(const NetView* nets, Store st, long long nnodes, const int* W, InstState is) {
+  const int ishift = nets[0].inst_shift;
+  for (long long n = blockIdx.x * (long long)blockDim.x + threadIdx.x; n < nnodes; n += (long long)gridDim.x * blockDim.x)
+    if (W[n] && st.nlevel[n] == 0) is.found[(int)(st.nkey[n] >> ishift)] = 1;
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -452,16 +585,16 @@ void Level<D>::init(const NetView* nets, int ninst, const int* ok, Store st, Fro
   k_init<D><<<grid_for(ninst, TPB, 4096), kBlock, 0, s>>>(nets, ninst, ok, st, out, is, ctl);
 }
 template <int D>
-void Level<D>::expand(const NetView* nets, InstState is, Front fr, int nfront, Store st, Succ sc, Ctl* ctl,
-                      int blocks, cudaStream_t s) {
+void Level<D>::expand(const NetView* nets, InstState is, Front fr, int nfront, const int* src_zone, Succ sc,
+                      Ctl* ctl, int roots, int blocks, cudaStream_t s) {
   constexpr int TPB = (kBlock / 32) * (32 / D);
-  k_expand<D><<<grid_for(nfront, TPB, blocks), kBlock, 0, s>>>(nets, is, fr, nfront, st, sc, ctl);
+  k_expand<D><<<grid_for(nfront, TPB, blocks), kBlock, 0, s>>>(nets, is, fr, nfront, src_zone, sc, ctl, roots);
 }
 template <int D>
-void Level<D>::probe(const NetView* nets, InstState is, Succ sc, Store st, Ctl* ctl, long long nsucc, int blocks,
-                     cudaStream_t s) {
+void Level<D>::probe(const NetView* nets, InstState is, Succ sc, Store st, Ctl* ctl, long long nsucc, int mode,
+                     int blocks, cudaStream_t s) {
   constexpr int TPB = (kBlock / 32) * (32 / D);
-  k_probe<D><<<grid_for(nsucc, TPB, blocks), kBlock, 0, s>>>(nets, is, sc, st, ctl, nsucc);
+  k_probe<D><<<grid_for(nsucc, TPB, blocks), kBlock, 0, s>>>(nets, is, sc, st, ctl, nsucc, mode);
 }
 template <int D>
 void Level<D>::deadlock(const NetView* nets, InstState is, Succ sc, Ctl* ctl, long long nsurv, int blocks,
@@ -476,9 +609,31 @@ void Level<D>::group(Succ sc, Store st, Ctl* ctl, long long nsucc, long long nto
 }
 template <int D>
 void Level<D>::merge(const NetView* nets, InstState is, Front fr, Succ sc, Store st, Front out, Ctl* ctl,
-                     long long ntouched, int level, int blocks, cudaStream_t s) {
+                     long long ntouched, int level, int mode, Edges ed, int record, int blocks, cudaStream_t s) {
   constexpr int TPB = (kBlock / 32) * (32 / D);
-  k_merge<D><<<grid_for(ntouched, TPB, blocks), kBlock, 0, s>>>(nets, is, fr, sc, st, out, ctl, ntouched, level);
+  k_merge<D><<<grid_for(ntouched, TPB, blocks), kBlock, 0, s>>>(nets, is, fr, sc, st, out, ctl, ntouched, level,
+                                                                mode, ed, record);
+}
+template <int D>
+void Level<D>::collect_p(const NetView* nets, Store st, long long nnodes, Front out, Ctl* ctl, cudaStream_t s) {
+  k_collect_p<<<grid_for(nnodes, 256, 4096), 256, 0, s>>>(nets, st, nnodes, out, ctl);
+}
+template <int D>
+void Level<D>::stop(const NetView* nets, Store st, long long nnodes, int* stop, Ctl* ctl, int blocks, cudaStream_t s) {
+  constexpr int TPB = (kBlock / 32) * (32 / D);
+  k_stop<D><<<grid_for(nnodes, TPB, blocks), kBlock, 0, s>>>(nets, st, nnodes, stop, ctl);
+}
+template <int D>
+void Level<D>::gfp_pass(Edges ed, long long nedges, long long nnodes, const int* stop, int* W, int* F, Ctl* ctl,
+                        cudaStream_t s) {
+  if (nedges > 0) k_gfp_mark<<<grid_for(nedges, 256, 8192), 256, 0, s>>>(ed, nedges, W, F);
+  k_gfp_update<<<grid_for(nnodes, 256, 8192), 256, 0, s>>>(nnodes, stop, W, F, ctl);
+}
+template <int D>
+void Level<D>::gfp_verdict(const NetView* nets, Store st, long long nnodes, const int* W, InstState is, Ctl* ctl,
+                           cudaStream_t s) {
+  (void)ctl;
+  k_gfp_verdict<<<grid_for(nnodes, 256, 8192), 256, 0, s>>>(nets, st, nnodes, W, is);
 }
 template <int D>
 void Level<D>::expand_plain(const NetView* nets, const int* locs, const int* ints, const int* zones, int n, int emode,
