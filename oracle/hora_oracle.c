@@ -1038,6 +1038,36 @@ static int fcmp(const void* a, const void* b) {
   if (x->key != y->key) return x->key < y->key ? -1 : 1;
   return 0;   /* qsort is not stable: ties are resolved by construction below */
 }
+
+/* The next frontier in canonical order: keys touched at `level` ascending, and within a key its
+ * live zones stored at `level` in chain order (newest first). */
+static int collect_frontier(const Store* S, int level, FItem** frp, int* capp) {
+  FItem* fr = *frp;
+  int nfr = 0, capfr = *capp;
+  for (uint64_t i = 0; i <= S->smask; ++i) {
+    if (S->shead[i] == -2 || S->stouch[i] != level) continue;
+    for (int nd = S->shead[i]; nd >= 0; nd = S->next[nd]) {
+      if (S->dead[nd] || S->level[nd] != level) continue;
+      if (nfr == capfr) { capfr = capfr ? capfr * 2 : 16; fr = (FItem*)realloc(fr, sizeof(FItem) * capfr); }
+      fr[nfr].key = S->skey[i]; fr[nfr].node = nd; nfr++;
+    }
+  }
+  /* one slot per key, so each key's entries form one contiguous run: sort the runs by key */
+  int nr = 0;
+  FItem* heads = (FItem*)malloc(sizeof(FItem) * (nfr ? nfr : 1));
+  for (int f = 0; f < nfr; ++f)
+    if (f == 0 || fr[f].key != fr[f - 1].key) { heads[nr].key = fr[f].key; heads[nr].node = f; nr++; }
+  qsort(heads, nr, sizeof(FItem), fcmp);
+  FItem* out = (FItem*)malloc(sizeof(FItem) * (nfr ? nfr : 1));
+  int o = 0;
+  for (int r = 0; r < nr; ++r)
+    for (int f = heads[r].node; f < nfr && fr[f].key == heads[r].key; ++f) out[o++] = fr[f];
+  if (nfr) memcpy(fr, out, sizeof(FItem) * nfr);
+  free(out); free(heads);
+  *frp = fr; *capp = capfr;
+  return nfr;
+}
+
 typedef struct {
   int32_t* locs; int32_t* ints; int32_t* zones;
   int n, cap, np, ni, d2;
@@ -1175,32 +1205,7 @@ static int32_t run_reach(const hora_net_desc* net, const Goal* goal, int collaps
       if (id >= 0) S.stouch[slot_of(&S, k)] = level;
     }
     /* next frontier: touched keys ascending, chain order within a key */
-    nfr = 0;
-    for (uint64_t i = 0; i <= S.smask; ++i) {
-      if (S.shead[i] == -2 || S.stouch[i] != level) continue;
-      for (int nd = S.shead[i]; nd >= 0; nd = S.next[nd]) {
-        if (S.dead[nd] || S.level[nd] != level) continue;
-        if (nfr == capfr) { capfr = capfr ? capfr * 2 : 16; fr = (FItem*)realloc(fr, sizeof(FItem) * capfr); }
-        fr[nfr].key = S.skey[i]; fr[nfr].node = nd; nfr++;
-      }
-    }
-    /* stable sort by key: collect per-key runs are contiguous already (one slot per key), so
-       sorting whole runs by key keeps the chain order inside each run */
-    {
-      /* sort run heads, then rebuild */
-      int nr = 0;
-      FItem* heads = (FItem*)malloc(sizeof(FItem) * (nfr ? nfr : 1));
-      int* start = (int*)malloc(sizeof(int) * (nfr + 1));
-      for (int f = 0; f < nfr; ++f)
-        if (f == 0 || fr[f].key != fr[f - 1].key) { heads[nr].key = fr[f].key; heads[nr].node = f; nr++; }
-      qsort(heads, nr, sizeof(FItem), fcmp);
-      FItem* out = (FItem*)malloc(sizeof(FItem) * (nfr ? nfr : 1));
-      int o = 0;
-      for (int r = 0; r < nr; ++r)
-        for (int f = heads[r].node; f < nfr && fr[f].key == heads[r].key; ++f) out[o++] = fr[f];
-      memcpy(fr, out, sizeof(FItem) * nfr);
-      free(out); free(heads); free(start);
-    }
+    nfr = collect_frontier(&S, level, &fr, &capfr);
     if (g_time_limit > 0 && now_s() - t0 > g_time_limit) { S0.levels = level; S0.status = HORA_E_TIMEOUT; goto done; }
     /* adaptive switch to Extra_LU+ (engine.cpp:2178-2184) */
     if (emode == 0 && S.nkeys && (double)S.nlive >= 4.0 * (double)S.nkeys) { emode = 1; S0.extrapolating = 1; }
@@ -1395,7 +1400,9 @@ int32_t orc_leads_to(const hora_net_desc* net, const hora_pred_desc* p, const ho
     fr[0].key = k0; fr[0].node = id; nfr = 1;
   }
   int level = 0;
+  int timed_out = 0;
   while (nfr > 0) {
+    if (g_time_limit > 0 && now_s() - t0 > g_time_limit) { timed_out = 1; break; }
     S0.explored += nfr;
     ++level;
     B.n = 0;
@@ -1416,15 +1423,7 @@ int32_t orc_leads_to(const hora_net_desc* net, const hora_pred_desc* p, const ho
       int id = store_add(&R, k, B.zones + (size_t)b * d2, level, dim, Ls, Us, NULL);
       if (id >= 0) R.stouch[slot_of(&R, k)] = level;
     }
-    nfr = 0;
-    for (uint64_t i = 0; i <= R.smask; ++i) {
-      if (R.shead[i] == -2 || R.stouch[i] != level) continue;
-      for (int nd = R.shead[i]; nd >= 0; nd = R.next[nd]) {
-        if (R.dead[nd] || R.level[nd] != level) continue;
-        if (nfr == capfr) { capfr = capfr ? capfr * 2 : 16; fr = (FItem*)realloc(fr, sizeof(FItem) * capfr); }
-        fr[nfr].key = R.skey[i]; fr[nfr].node = nd; nfr++;
-      }
-    }
+    nfr = collect_frontier(&R, level, &fr, &capfr);
     if (emode == 0 && R.nkeys && (double)R.nlive >= 4.0 * (double)R.nkeys) emode = 1;
   }
   /* ---- roots: the p-part of every stored zone, cut to !q ---- */
@@ -1460,7 +1459,8 @@ int32_t orc_leads_to(const hora_net_desc* net, const hora_pred_desc* p, const ho
   (void)nodekey_unused;
   uint64_t* nkey = NULL; int nkcap = 0;
   level = 0;
-  while (nfr > 0) {
+  while (nfr > 0 && !timed_out) {
+    if (g_time_limit > 0 && now_s() - t0 > g_time_limit) { timed_out = 1; break; }
     S0.explored += nfr;
     ++level;
     FItem* nxt = NULL; int nn = 0, capn = 0;
@@ -1484,17 +1484,17 @@ int32_t orc_leads_to(const hora_net_desc* net, const hora_pred_desc* p, const ho
     free(fr);
     fr = nxt; nfr = nn; capfr = capn;
   }
-  /* node keys, for the stop sets */
-  nkcap = G.nn;
+  /* node keys, for the stop sets (a timed-out run skips the sweep: its verdict is not used) */
+  nkcap = timed_out ? 0 : G.nn;
   nkey = (uint64_t*)malloc(sizeof(uint64_t) * (nkcap ? nkcap : 1));
   for (uint64_t i = 0; i <= G.smask; ++i)
     if (G.shead[i] != -2)
-      for (int nd = G.shead[i]; nd >= 0; nd = G.next[nd]) nkey[nd] = G.skey[i];
+      for (int nd = G.shead[i]; nd >= 0 && nkcap; nd = G.next[nd]) nkey[nd] = G.skey[i];
   /* ---- stop sets (stop_set, construction.cpp:1200-1239) ---- */
   char* stop = (char*)calloc(G.nn ? G.nn : 1, 1);
   char* inW = (char*)malloc(G.nn ? G.nn : 1);
   const hora_pred_desc* av = m.avoid;
-  for (int u = 0; u < G.nn; ++u) {
+  for (int u = 0; u < nkcap; ++u) {
     key_decode(&m, nkey[u], locs, ints);
     const int32_t* zu = G.zones + (size_t)u * d2;
     m.avoid = NULL;   /* deadlock and any-successor are judged in the unrestricted network */
@@ -1521,7 +1521,7 @@ int32_t orc_leads_to(const hora_net_desc* net, const hora_pred_desc* p, const ho
     for (int e = 0; e < efrom.n; ++e) dst[off[efrom.a[e]] + fill[efrom.a[e]]++] = eto.a[e];
     free(fill);
   }
-  for (int changed = 1; changed;) {
+  for (int changed = !timed_out; changed;) {
     changed = 0;
     S0.gfp_iters++;
     for (int u = 0; u < G.nn; ++u) {
@@ -1531,13 +1531,14 @@ int32_t orc_leads_to(const hora_net_desc* net, const hora_pred_desc* p, const ho
       if (!any) { inW[u] = 0; changed = 1; }
     }
   }
-  for (int r = 0; r < roots.n && !violated; ++r) violated = inW[roots.a[r]];
+  for (int r = 0; r < roots.n && !violated && !timed_out; ++r) violated = inW[roots.a[r]];
   S0.stored = (uint64_t)G.nn;
   S0.keys = (uint64_t)G.nkeys;
   S0.levels = (uint64_t)level;
   S0.pre_calls = (uint64_t)efrom.n;
   S0.expanded = S0.explored;
   S0.seconds = now_s() - t0;
+  if (timed_out) S0.status = HORA_E_TIMEOUT;
   if (st) *st = S0;
   *result = !violated;
   free(off); free(dst); free(stop); free(inW); free(nkey);

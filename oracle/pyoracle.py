@@ -222,6 +222,6 @@ def leads_to(net: Network, p: Pred, q: Pred):
     st = Stats(); res = ctypes.c_int32(0)
     rc = lib().orc_leads_to(ctypes.addressof(na.desc), ctypes.addressof(pa.desc), ctypes.addressof(qa.desc),
                             ctypes.byref(st), ctypes.byref(res))
-    if rc:
+    if rc or st.status not in (0, 5):
         raise RuntimeError(f"oracle leads_to status {rc}")
     return bool(res.value), st.as_dict()

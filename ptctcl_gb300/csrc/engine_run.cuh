@@ -98,322 +98,478 @@ struct KTimer {
 enum { KT_EXPAND = 0, KT_PROBE = 1, KT_DEADLOCK = 2, KT_GROUP = 3, KT_MERGE = 4, KT_OTHER = 5 };
 
 template <int D>
-struct GroupBuffers {
-  DBuf hkey, head, pend, pend_base;                         // hash table
-  DBuf nzone, nnext, nlevel, ndead, ninst;                  // nodes
-  DBuf skey, sparent, sord, sslot, srank, szone, ssurv, sseg, ssorted, stouched;   // successors
-  DBuf fkey[2], fnode[2], frank[2], finst[2];               // frontiers
-  DBuf ctl, nets_ok;
-  DBuf emode, done, found, generated, gen_backup, nlive, nkeys, nfront, probes;
+struct StoreBufs {
+  DBuf hkey, head, pend, pend_base;           // hash table
+  DBuf nzone, nnext, nlevel, ndead, ninst, nkey;  // nodes
   unsigned long long hcap = 0;
-  long long ncap = 0, scap = 0, fcapb[2] = {0, 0};
+  long long ncap = 0;
 };
 
+// The level-synchronous engine over a group of instances sharing the DBM dimension D. Store 0 is
+// the a_LU passed store of reach / deadlock / leads-to phase 1; store 1 is the exact-zone graph of
+// leads-to phase 2.
 template <int D>
-int run_group(const std::vector<const HostNet*>& nets, std::vector<InstResult>& res, const RunOptions& o,
-              std::string& err) {
-  const auto t_start = std::chrono::steady_clock::now();
-  constexpr long long Z2 = (long long)D * D;
-  const int ninst = (int)nets.size();
-  res.assign(ninst, InstResult{});
-  int instbits = 0;
-  while ((1 << instbits) < ninst) ++instbits;
-  const int inst_shift = 63 - instbits;
-  for (int k = 0; k < ninst; ++k)
-    if (nets[k]->keybits > inst_shift) { err = "discrete key too wide for the batch"; return HORA_E_NOT_SUPPORTED; }
-
-  cudaStream_t s;
-  HGB_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
-  struct StreamGuard { cudaStream_t s; ~StreamGuard() { cudaStreamDestroy(s); } } sg{s};
-  int dev = 0, nsm = 0;
-  HGB_CUDA(cudaGetDevice(&dev));
-  HGB_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-  const int blocks = o.blocks > 0 ? o.blocks : nsm * 16;
-
+struct Engine {
+  static constexpr long long Z2 = (long long)D * D;
+  std::vector<const HostNet*> nets;
+  int ninst = 0, inst_shift = 63;
+  RunOptions o;
+  std::string& err;
+  cudaStream_t s = nullptr;
+  int blocks = 0;
   DeviceNets dn;
-  {
-    int rc = upload_nets(nets, inst_shift, dn, err);
-    if (rc) return rc;
-  }
-  GroupBuffers<D> B;
-  // --- initial sizes
-  B.hcap = 1ull << 16;
-  while (B.hcap < 4ull * ninst) B.hcap <<= 1;
-  B.ncap = std::max<long long>(1 << 14, 2LL * ninst);
-  B.scap = (long long)std::max<size_t>(o.succ_cap0, 4 * (size_t)ninst);
-  B.fcapb[0] = B.fcapb[1] = std::max<long long>(1 << 14, 2LL * ninst);
-  auto alloc_table = [&](DBuf& k, DBuf& h, DBuf& p, DBuf& pb, unsigned long long cap) -> cudaError_t {
-    cudaError_t e;
-    if ((e = k.alloc(cap * 8)) || (e = h.alloc(cap * 4)) || (e = p.alloc(cap * 4)) || (e = pb.alloc(cap * 4))) return e;
-    if ((e = cudaMemsetAsync(k.p, 0xff, cap * 8, s)) || (e = cudaMemsetAsync(h.p, 0xff, cap * 4, s)) ||
-        (e = cudaMemsetAsync(p.p, 0, cap * 4, s)))
-      return e;
-    return cudaSuccess;
-  };
-  HGB_CUDA(alloc_table(B.hkey, B.head, B.pend, B.pend_base, B.hcap));
-  HGB_CUDA(B.nzone.alloc(B.ncap * Z2 * 4));
-  HGB_CUDA(B.nnext.alloc(B.ncap * 4));
-  HGB_CUDA(B.nlevel.alloc(B.ncap * 4));
-  HGB_CUDA(B.ndead.alloc(B.ncap * 4));
-  HGB_CUDA(B.ninst.alloc(B.ncap * 4));
-  auto alloc_succ = [&](long long cap) -> cudaError_t {
-    cudaError_t e;
-    if ((e = B.skey.alloc(cap * 8)) || (e = B.sparent.alloc(cap * 4)) || (e = B.sord.alloc(cap * 4)) ||
-        (e = B.sslot.alloc(cap * 4)) || (e = B.srank.alloc(cap * 4)) || (e = B.szone.alloc(cap * Z2 * 4)) ||
-        (e = B.ssurv.alloc(cap * 4)) || (e = B.sseg.alloc(cap * 4)) || (e = B.ssorted.alloc(cap * 4)) ||
-        (e = B.stouched.alloc(cap * 4)))
-      return e;
-    return cudaSuccess;
-  };
-  HGB_CUDA(alloc_succ(B.scap));
-  for (int b = 0; b < 2; ++b) {
-    HGB_CUDA(B.fkey[b].alloc(B.fcapb[b] * 8));
-    HGB_CUDA(B.fnode[b].alloc(B.fcapb[b] * 4));
-    HGB_CUDA(B.frank[b].alloc(B.fcapb[b] * 4));
-    HGB_CUDA(B.finst[b].alloc(B.fcapb[b] * 4));
-  }
-  HGB_CUDA(B.ctl.alloc(sizeof(Ctl)));
-  HGB_CUDA(cudaMemsetAsync(B.ctl.p, 0, sizeof(Ctl), s));
-  const size_t ni4 = (size_t)ninst * 4, ni8 = (size_t)ninst * 8;
-  HGB_CUDA(B.emode.alloc(ni4)); HGB_CUDA(B.done.alloc(ni4)); HGB_CUDA(B.found.alloc(ni4));
-  HGB_CUDA(B.generated.alloc(ni8)); HGB_CUDA(B.gen_backup.alloc(ni8)); HGB_CUDA(B.nlive.alloc(ni8));
-  HGB_CUDA(B.nkeys.alloc(ni8)); HGB_CUDA(B.nfront.alloc(ni8)); HGB_CUDA(B.probes.alloc(ni8));
-  for (DBuf* b : {&B.emode, &B.done, &B.found, &B.generated, &B.nlive, &B.nkeys, &B.nfront, &B.probes})
-    HGB_CUDA(cudaMemsetAsync(b->p, 0, b->bytes, s));
+  StoreBufs<D> S[2];
+  DBuf skey, sparent, sord, sslot, srank, szone, ssurv, sseg, ssorted, stouched;
+  long long scap = 0;
+  DBuf fkey[2], fnode[2], frank[2], finst[2];
+  long long fcapb[2] = {0, 0};
+  DBuf esrc, edst;
+  long long ecap = 0;
+  DBuf ctl, emode, done, found, generated, gen_backup, nlive, nkeys, nfront, probes;
+  Ctl hctl{};
+  KTimer kt;
+  unsigned long long launches = 0, h2d = 0, d2h = 0;
+  std::vector<int> h_done, h_emode;
+  std::vector<unsigned> h_found;
+  std::vector<unsigned long long> h_nfront, h_nkeys, h_gen, explored, levels;
+  std::vector<long long> h_nlive;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  std::chrono::steady_clock::time_point t_start;
 
-  auto store = [&]() {
+  Engine(const std::vector<const HostNet*>& n, const RunOptions& opt, std::string& e) : nets(n), o(opt), err(e) {}
+  ~Engine() {
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    if (s) cudaStreamDestroy(s);
+  }
+
+  Store store(int k) {
+    StoreBufs<D>& B = S[k];
     Store st;
     st.hkey = B.hkey.template as<unsigned long long>(); st.head = B.head.template as<int>();
     st.pend = B.pend.template as<unsigned>(); st.pend_base = B.pend_base.template as<unsigned>();
     st.hmask = B.hcap - 1;
     st.nzone = B.nzone.template as<int>(); st.nnext = B.nnext.template as<int>();
     st.nlevel = B.nlevel.template as<int>(); st.ndead = B.ndead.template as<int>(); st.ninst = B.ninst.template as<int>();
+    st.nkey = B.nkey.template as<unsigned long long>();
     return st;
-  };
-  auto succ = [&]() {
+  }
+  Succ succ() {
     Succ sc;
-    sc.key = B.skey.template as<unsigned long long>(); sc.parent = B.sparent.template as<int>();
-    sc.ord = B.sord.template as<int>(); sc.slot = B.sslot.template as<int>(); sc.rank = B.srank.template as<int>();
-    sc.zone = B.szone.template as<int>(); sc.surv = B.ssurv.template as<int>(); sc.seg = B.sseg.template as<int>();
-    sc.sorted = B.ssorted.template as<int>(); sc.touched = B.stouched.template as<int>(); sc.cap = B.scap;
+    sc.key = skey.template as<unsigned long long>(); sc.parent = sparent.template as<int>();
+    sc.ord = sord.template as<int>(); sc.slot = sslot.template as<int>(); sc.rank = srank.template as<int>();
+    sc.zone = szone.template as<int>(); sc.surv = ssurv.template as<int>(); sc.seg = sseg.template as<int>();
+    sc.sorted = ssorted.template as<int>(); sc.touched = stouched.template as<int>(); sc.cap = scap;
     return sc;
-  };
-  auto front = [&](int b) {
+  }
+  Front front(int b) {
     Front f;
-    f.key = B.fkey[b].template as<unsigned long long>(); f.node = B.fnode[b].template as<int>();
-    f.rank = B.frank[b].template as<int>(); f.inst = B.finst[b].template as<int>();
+    f.key = fkey[b].template as<unsigned long long>(); f.node = fnode[b].template as<int>();
+    f.rank = frank[b].template as<int>(); f.inst = finst[b].template as<int>();
     return f;
-  };
-  InstState is;
-  is.emode = B.emode.template as<int>(); is.done = B.done.template as<int>(); is.found = B.found.template as<unsigned>();
-  is.generated = B.generated.template as<unsigned long long>(); is.nlive = B.nlive.template as<long long>();
-  is.nkeys = B.nkeys.template as<unsigned long long>(); is.nfront = B.nfront.template as<unsigned long long>();
-  is.probes = B.probes.template as<unsigned long long>();
-  Ctl* dctl = B.ctl.template as<Ctl>();
-  Ctl hctl;
-  unsigned long long launches = 0, h2d = 0, d2h = 0;
-  for (const HostNet* hn : nets) (void)hn;
-  for (size_t k = 0; k < dn.blob_bytes.size(); ++k) h2d += dn.blob_bytes[k];
-  h2d += sizeof(NetView) * (size_t)ninst;
-  KTimer kt;
-  auto read_ctl = [&]() -> cudaError_t {
-    cudaError_t e = cudaMemcpyAsync(&hctl, dctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s);
-    if (e) return e;
+  }
+  Edges edges() { return Edges{esrc.template as<int>(), edst.template as<int>(), ecap}; }
+  InstState istate() {
+    InstState is;
+    is.emode = emode.template as<int>(); is.done = done.template as<int>(); is.found = found.template as<unsigned>();
+    is.generated = generated.template as<unsigned long long>(); is.nlive = nlive.template as<long long>();
+    is.nkeys = nkeys.template as<unsigned long long>(); is.nfront = nfront.template as<unsigned long long>();
+    is.probes = probes.template as<unsigned long long>();
+    return is;
+  }
+  Ctl* dctl() { return ctl.template as<Ctl>(); }
+
+  int read_ctl() {
+    HGB_CUDA(cudaMemcpyAsync(&hctl, dctl(), sizeof(Ctl), cudaMemcpyDeviceToHost, s));
     d2h += sizeof(Ctl);
-    e = cudaStreamSynchronize(s);
-    kt.collect();
-    return e;
-  };
-  // per-instance host mirrors
-  std::vector<int> h_done(ninst, 0), h_emode(ninst, 0);
-  std::vector<unsigned> h_found(ninst, 0);
-  std::vector<unsigned long long> h_nfront(ninst, 0), h_nkeys(ninst, 0), h_gen(ninst, 0);
-  std::vector<long long> h_nlive(ninst, 0);
-  std::vector<unsigned long long> explored(ninst, 0), levels(ninst, 0);
-
-  cudaEvent_t ev0, ev1;
-  HGB_CUDA(cudaEventCreate(&ev0));
-  HGB_CUDA(cudaEventCreate(&ev1));
-  struct EvGuard { cudaEvent_t a, b; ~EvGuard() { cudaEventDestroy(a); cudaEventDestroy(b); } } eg{ev0, ev1};
-  HGB_CUDA(cudaEventRecord(ev0, s));
-
-  // --- level 0
-  kt.begin(s);
-  Level<D>::init(dn.views, ninst, dn.ok, store(), front(0), is, dctl, s);
-  kt.end(s, KT_OTHER);
-  ++launches;
-  HGB_CUDA(cudaGetLastError());
-  HGB_CUDA(read_ctl());
-  if (hctl.err) { err = "device error in init"; return (int)hctl.err; }
-  HGB_CUDA(cudaMemcpyAsync(h_found.data(), is.found, ni4, cudaMemcpyDeviceToHost, s));
-  HGB_CUDA(cudaMemcpyAsync(h_done.data(), is.done, ni4, cudaMemcpyDeviceToHost, s));
-  HGB_CUDA(cudaStreamSynchronize(s));
-  long long nfront = (long long)hctl.nfront;
-  int cur = 0;
-  int level = 0;
-  int status = HORA_OK;
-  while (nfront > 0) {
-    if (o.cancel && *o.cancel) { status = HORA_E_CANCELLED; break; }
-    ++level;
-    // per-instance frontier sizes of this level
-    HGB_CUDA(cudaMemcpyAsync(h_nfront.data(), is.nfront, ni8, cudaMemcpyDeviceToHost, s));
-    HGB_CUDA(cudaMemsetAsync(is.nfront, 0, ni8, s));
     HGB_CUDA(cudaStreamSynchronize(s));
+    kt.collect();
+    return HORA_OK;
+  }
+  int alloc_store(int k, unsigned long long hcap, long long ncap) {
+    StoreBufs<D>& B = S[k];
+    B.hcap = hcap;
+    B.ncap = ncap;
+    HGB_CUDA(B.hkey.alloc(hcap * 8)); HGB_CUDA(B.head.alloc(hcap * 4)); HGB_CUDA(B.pend.alloc(hcap * 4));
+    HGB_CUDA(B.pend_base.alloc(hcap * 4));
+    HGB_CUDA(cudaMemsetAsync(B.hkey.p, 0xff, hcap * 8, s));
+    HGB_CUDA(cudaMemsetAsync(B.head.p, 0xff, hcap * 4, s));
+    HGB_CUDA(cudaMemsetAsync(B.pend.p, 0, hcap * 4, s));
+    HGB_CUDA(B.nzone.alloc(ncap * Z2 * 4)); HGB_CUDA(B.nnext.alloc(ncap * 4)); HGB_CUDA(B.nlevel.alloc(ncap * 4));
+    HGB_CUDA(B.ndead.alloc(ncap * 4)); HGB_CUDA(B.ninst.alloc(ncap * 4)); HGB_CUDA(B.nkey.alloc(ncap * 8));
+    return HORA_OK;
+  }
+  int alloc_succ(long long cap) {
+    scap = cap;
+    HGB_CUDA(skey.alloc(cap * 8)); HGB_CUDA(sparent.alloc(cap * 4)); HGB_CUDA(sord.alloc(cap * 4));
+    HGB_CUDA(sslot.alloc(cap * 4)); HGB_CUDA(srank.alloc(cap * 4)); HGB_CUDA(szone.alloc(cap * Z2 * 4));
+    HGB_CUDA(ssurv.alloc(cap * 4)); HGB_CUDA(sseg.alloc(cap * 4)); HGB_CUDA(ssorted.alloc(cap * 4));
+    HGB_CUDA(stouched.alloc(cap * 4));
+    return HORA_OK;
+  }
+  int alloc_front(int b, long long cap) {
+    fcapb[b] = cap;
+    HGB_CUDA(fkey[b].alloc(cap * 8)); HGB_CUDA(fnode[b].alloc(cap * 4));
+    HGB_CUDA(frank[b].alloc(cap * 4)); HGB_CUDA(finst[b].alloc(cap * 4));
+    return HORA_OK;
+  }
+  // Room in store k's hash table for `extra` more keys (load factor at most 1/2).
+  int ensure_hash(int k, unsigned long long extra) {
+    StoreBufs<D>& B = S[k];
+    if ((hctl.nslots + extra) * 2 <= B.hcap) return HORA_OK;
+    unsigned long long ncap = B.hcap;
+    while ((hctl.nslots + extra) * 2 > ncap) ncap <<= 1;
+    DBuf k2, h2, p2, pb2;
+    HGB_CUDA(k2.alloc(ncap * 8)); HGB_CUDA(h2.alloc(ncap * 4)); HGB_CUDA(p2.alloc(ncap * 4)); HGB_CUDA(pb2.alloc(ncap * 4));
+    HGB_CUDA(cudaMemsetAsync(k2.p, 0xff, ncap * 8, s));
+    HGB_CUDA(cudaMemsetAsync(h2.p, 0xff, ncap * 4, s));
+    HGB_CUDA(cudaMemsetAsync(p2.p, 0, ncap * 4, s));
+    kt.begin(s);
+    k_rehash<<<1024, 256, 0, s>>>(B.hkey.template as<unsigned long long>(), B.head.template as<int>(), B.hcap,
+                                 k2.template as<unsigned long long>(), h2.template as<int>(), ncap - 1, &dctl()->err);
+    kt.end(s, KT_OTHER);
+    ++launches;
+    HGB_CUDA(cudaGetLastError());
+    HGB_CUDA(cudaStreamSynchronize(s));
+    kt.collect();
+    std::swap(B.hkey.p, k2.p); std::swap(B.hkey.bytes, k2.bytes);
+    std::swap(B.head.p, h2.p); std::swap(B.head.bytes, h2.bytes);
+    std::swap(B.pend.p, p2.p); std::swap(B.pend.bytes, p2.bytes);
+    std::swap(B.pend_base.p, pb2.p); std::swap(B.pend_base.bytes, pb2.bytes);
+    B.hcap = ncap;
+    return HORA_OK;
+  }
+  int ensure_nodes(int k, long long extra) {
+    StoreBufs<D>& B = S[k];
+    if ((long long)hctl.nnodes + extra <= B.ncap) return HORA_OK;
+    long long nc = B.ncap;
+    while ((long long)hctl.nnodes + extra > nc) nc *= 2;
+    const size_t used = hctl.nnodes;
+    HGB_CUDA(B.nzone.grow(nc * Z2 * 4, used * Z2 * 4, s));
+    HGB_CUDA(B.nnext.grow(nc * 4, used * 4, s));
+    HGB_CUDA(B.nlevel.grow(nc * 4, used * 4, s));
+    HGB_CUDA(B.ndead.grow(nc * 4, used * 4, s));
+    HGB_CUDA(B.ninst.grow(nc * 4, used * 4, s));
+    HGB_CUDA(B.nkey.grow(nc * 8, used * 8, s));
+    B.ncap = nc;
+    return HORA_OK;
+  }
+  int ensure_edges(long long need) {
+    if (need <= ecap) return HORA_OK;
+    long long c = std::max<long long>(ecap, 1 << 16);
+    while (c < need) c *= 2;
+    const size_t used = (size_t)std::min<unsigned long long>(hctl.nedges, (unsigned long long)ecap);
+    HGB_CUDA(esrc.grow(c * 4, used * 4, s));
+    HGB_CUDA(edst.grow(c * 4, used * 4, s));
+    ecap = c;
+    return HORA_OK;
+  }
+
+  int setup() {
+    t_start = std::chrono::steady_clock::now();
+    ninst = (int)nets.size();
+    int instbits = 0;
+    while ((1 << instbits) < ninst) ++instbits;
+    inst_shift = 63 - instbits;
     for (int k = 0; k < ninst; ++k)
-      if (!h_done[k] && h_nfront[k]) { explored[k] += h_nfront[k]; levels[k] = level; }
-    // ---- expand (re-run with a larger buffer on overflow; expand writes nothing persistent)
-    for (;;) {
-      HGB_CUDA(cudaMemsetAsync(dctl, 0, kCtlLevelBytes, s));
-      HGB_CUDA(cudaMemcpyAsync(B.gen_backup.p, is.generated, ni8, cudaMemcpyDeviceToDevice, s));
-      kt.begin(s);
-      Level<D>::expand(dn.views, is, front(cur), (int)nfront, store(), succ(), dctl, blocks, s);
-      kt.end(s, KT_EXPAND);
-      ++launches;
-      HGB_CUDA(cudaGetLastError());
-      HGB_CUDA(read_ctl());
-      if (!hctl.overflow) break;
-      const long long need = (long long)(hctl.nsucc + hctl.nsucc / 4 + 1024);
-      HGB_CUDA(cudaMemcpyAsync(is.generated, B.gen_backup.p, ni8, cudaMemcpyDeviceToDevice, s));
-      B.scap = need;
-      HGB_CUDA(alloc_succ(B.scap));
-    }
-    if (hctl.err) { status = (int)hctl.err; err = "device error in expand"; break; }
-    const long long nsucc = (long long)hctl.nsucc;
-    if (hctl.found) {
-      HGB_CUDA(cudaMemcpyAsync(h_found.data(), is.found, ni4, cudaMemcpyDeviceToHost, s));
+      if (nets[k]->keybits > inst_shift) { err = "discrete key too wide for the batch"; return HORA_E_NOT_SUPPORTED; }
+    HGB_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    int dev = 0, nsm = 0;
+    HGB_CUDA(cudaGetDevice(&dev));
+    HGB_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    blocks = o.blocks > 0 ? o.blocks : nsm * 16;
+    int rc = upload_nets(nets, inst_shift, dn, err);
+    if (rc) return rc;
+    for (size_t k = 0; k < dn.blob_bytes.size(); ++k) h2d += dn.blob_bytes[k];
+    h2d += sizeof(NetView) * (size_t)ninst;
+    unsigned long long hcap = 1ull << 16;
+    while (hcap < 4ull * ninst) hcap <<= 1;
+    if ((rc = alloc_store(0, hcap, std::max<long long>(1 << 14, 2LL * ninst)))) return rc;
+    if ((rc = alloc_succ((long long)std::max<size_t>(o.succ_cap0, 4 * (size_t)ninst)))) return rc;
+    for (int b = 0; b < 2; ++b)
+      if ((rc = alloc_front(b, std::max<long long>(1 << 14, 2LL * ninst)))) return rc;
+    HGB_CUDA(ctl.alloc(sizeof(Ctl)));
+    HGB_CUDA(cudaMemsetAsync(ctl.p, 0, sizeof(Ctl), s));
+    const size_t ni4 = (size_t)ninst * 4, ni8 = (size_t)ninst * 8;
+    HGB_CUDA(emode.alloc(ni4)); HGB_CUDA(done.alloc(ni4)); HGB_CUDA(found.alloc(ni4));
+    HGB_CUDA(generated.alloc(ni8)); HGB_CUDA(gen_backup.alloc(ni8)); HGB_CUDA(nlive.alloc(ni8));
+    HGB_CUDA(nkeys.alloc(ni8)); HGB_CUDA(nfront.alloc(ni8)); HGB_CUDA(probes.alloc(ni8));
+    for (DBuf* b : {&emode, &done, &found, &generated, &nlive, &nkeys, &nfront, &probes})
+      HGB_CUDA(cudaMemsetAsync(b->p, 0, b->bytes, s));
+    h_done.assign(ninst, 0); h_emode.assign(ninst, 0); h_found.assign(ninst, 0);
+    h_nfront.assign(ninst, 0); h_nkeys.assign(ninst, 0); h_gen.assign(ninst, 0);
+    h_nlive.assign(ninst, 0); explored.assign(ninst, 0); levels.assign(ninst, 0);
+    HGB_CUDA(cudaEventCreate(&ev0));
+    HGB_CUDA(cudaEventCreate(&ev1));
+    HGB_CUDA(cudaEventRecord(ev0, s));
+    return HORA_OK;
+  }
+
+  // Level 0 of store 0: every instance's initial state. Returns the frontier size in *nf.
+  int init(long long* nf) {
+    InstState is = istate();
+    kt.begin(s);
+    Level<D>::init(dn.views_plain, ninst, dn.ok, store(0), front(0), is, dctl(), s);
+    kt.end(s, KT_OTHER);
+    ++launches;
+    HGB_CUDA(cudaGetLastError());
+    int rc = read_ctl();
+    if (rc) return rc;
+    if (hctl.err) { err = "device error in init"; return (int)hctl.err; }
+    HGB_CUDA(cudaMemcpyAsync(h_found.data(), is.found, (size_t)ninst * 4, cudaMemcpyDeviceToHost, s));
+    HGB_CUDA(cudaMemcpyAsync(h_done.data(), is.done, (size_t)ninst * 4, cudaMemcpyDeviceToHost, s));
+    HGB_CUDA(cudaStreamSynchronize(s));
+    *nf = (long long)hctl.nfront;
+    return HORA_OK;
+  }
+
+  // BFS on store k from frontier buffer `cur` until it empties.
+  //  mode 0: a_LU subsumption store with the reach / deadlock goals and the adaptive Extra_LU+;
+  //  mode 1: exact-zone graph store recording edges. With roots_src set, the first step turns the
+  //          frontier's store-0 zones into the graph's level-0 roots instead of expanding them.
+  int run_levels(int k, int mode, int& cur, long long nf, int& level, const int* roots_src) {
+    const size_t ni4 = (size_t)ninst * 4, ni8 = (size_t)ninst * 8;
+    InstState is = istate();
+    int rc;
+    bool roots = roots_src != nullptr;
+    const NetView* V = k == 0 ? dn.views_plain : dn.views;   // the !q restriction is for the graph only
+    while (nf > 0) {
+      if (o.cancel && *o.cancel) return HORA_E_CANCELLED;
+      if (!roots) ++level;
+      HGB_CUDA(cudaMemcpyAsync(h_nfront.data(), is.nfront, ni8, cudaMemcpyDeviceToHost, s));
+      HGB_CUDA(cudaMemsetAsync(is.nfront, 0, ni8, s));
       HGB_CUDA(cudaStreamSynchronize(s));
+      if (!roots)
+        for (int q = 0; q < ninst; ++q)
+          if (!h_done[q] && h_nfront[q]) { explored[q] += h_nfront[q]; levels[q] = level; }
+      // ---- expand; re-run with a larger buffer on overflow (it writes nothing persistent)
+      const int* src = roots ? roots_src : S[k].nzone.template as<int>();
+      for (;;) {
+        HGB_CUDA(cudaMemsetAsync(dctl(), 0, kCtlLevelBytes, s));
+        HGB_CUDA(cudaMemcpyAsync(gen_backup.p, is.generated, ni8, cudaMemcpyDeviceToDevice, s));
+        kt.begin(s);
+        Level<D>::expand(V, is, front(cur), (int)nf, src, succ(), dctl(), roots ? 1 : 0, blocks, s);
+        kt.end(s, KT_EXPAND);
+        ++launches;
+        HGB_CUDA(cudaGetLastError());
+        if ((rc = read_ctl())) return rc;
+        if (!hctl.overflow) break;
+        HGB_CUDA(cudaMemcpyAsync(is.generated, gen_backup.p, ni8, cudaMemcpyDeviceToDevice, s));
+        if ((rc = alloc_succ((long long)(hctl.nsucc + hctl.nsucc / 4 + 1024)))) return rc;
+      }
+      if (hctl.err) { err = "device error in expand"; return (int)hctl.err; }
+      const long long nsucc = (long long)hctl.nsucc;
+      if ((rc = ensure_hash(k, (unsigned long long)nsucc))) return rc;
+      // ---- probe
+      if (nsucc > 0) {
+        kt.begin(s);
+        Level<D>::probe(V, is, succ(), store(k), dctl(), nsucc, mode, blocks, s);
+        kt.end(s, KT_PROBE);
+        ++launches;
+        HGB_CUDA(cudaGetLastError());
+      }
+      if ((rc = read_ctl())) return rc;
+      if (hctl.err) { err = "device error in probe"; return (int)hctl.err; }
+      const long long nsurv = (long long)hctl.nsurv, ntouched = (long long)hctl.ntouched;
+      // ---- deadlock goal on the survivors
+      if (mode == 0) {
+        bool any_dl = false;
+        for (int q = 0; q < ninst; ++q) any_dl |= (nets[q]->kind == HORA_Q_DEADLOCK && !h_done[q]);
+        if (any_dl && nsurv > 0) {
+          kt.begin(s);
+          Level<D>::deadlock(V, is, succ(), dctl(), nsurv, blocks, s);
+          kt.end(s, KT_DEADLOCK);
+          ++launches;
+          HGB_CUDA(cudaGetLastError());
+          if ((rc = read_ctl())) return rc;
+          if (hctl.err) { err = "deadlock test exceeded its escape table"; return (int)hctl.err; }
+        }
+      }
+      // ---- room for the new nodes, the next frontier and the edges
+      if ((rc = ensure_nodes(k, nsurv))) return rc;
+      if (nsurv > fcapb[cur ^ 1]) {
+        long long fc = fcapb[cur ^ 1];
+        while (nsurv > fc) fc *= 2;
+        if ((rc = alloc_front(cur ^ 1, fc))) return rc;
+      }
+      const int record = (mode == 1 && !roots) ? 1 : 0;
+      if (record && (rc = ensure_edges((long long)hctl.nedges + nsucc))) return rc;
+      // ---- group + merge
+      if (ntouched > 0) {
+        kt.begin(s);
+        Level<D>::group(succ(), store(k), dctl(), nsucc, ntouched, s);
+        kt.end(s, KT_GROUP, 2);
+        kt.begin(s);
+        Level<D>::merge(V, is, front(cur), succ(), store(k), front(cur ^ 1), dctl(), ntouched, level, mode,
+                        edges(), record, blocks, s);
+        kt.end(s, KT_MERGE);
+        launches += 3;
+        HGB_CUDA(cudaGetLastError());
+      }
+      if ((rc = read_ctl())) return rc;
+      if (hctl.err) { err = "device error in merge"; return (int)hctl.err; }
+      // ---- end of level: goals and the adaptive extrapolation (store 0 only)
+      if (mode == 0) {
+        HGB_CUDA(cudaMemcpyAsync(h_found.data(), is.found, ni4, cudaMemcpyDeviceToHost, s));
+        HGB_CUDA(cudaMemcpyAsync(h_nlive.data(), is.nlive, ni8, cudaMemcpyDeviceToHost, s));
+        HGB_CUDA(cudaMemcpyAsync(h_nkeys.data(), is.nkeys, ni8, cudaMemcpyDeviceToHost, s));
+        HGB_CUDA(cudaStreamSynchronize(s));
+        bool changed = false;
+        for (int q = 0; q < ninst; ++q) {
+          if (h_done[q]) continue;
+          if (h_found[q]) { h_done[q] = 1; changed = true; continue; }
+          // adaptive switch to Extra_LU+ (src/reachability/engine.cpp:2178-2184)
+          if (h_emode[q] == 0 && h_nkeys[q] && (double)h_nlive[q] >= 4.0 * (double)h_nkeys[q]) { h_emode[q] = 1; changed = true; }
+        }
+        if (changed) {
+          HGB_CUDA(cudaMemcpyAsync(is.done, h_done.data(), ni4, cudaMemcpyHostToDevice, s));
+          HGB_CUDA(cudaMemcpyAsync(is.emode, h_emode.data(), ni4, cudaMemcpyHostToDevice, s));
+          h2d += 2 * ni4;
+        }
+      }
+      nf = (long long)hctl.nfront;
+      cur ^= 1;
+      roots = false;
     }
-    // ---- make room in the hash table for every possible new key
-    if ((hctl.nslots + (unsigned long long)nsucc) * 2 > B.hcap) {
-      unsigned long long ncap = B.hcap;
-      while ((hctl.nslots + (unsigned long long)nsucc) * 2 > ncap) ncap <<= 1;
-      DBuf k2, h2, p2, pb2;
-      HGB_CUDA(alloc_table(k2, h2, p2, pb2, ncap));
+    return HORA_OK;
+  }
+
+  // Leads-to after phase 1: roots, the exact !q graph, stop flags and the greatest fixpoint.
+  int leadsto_phase2(int& cur) {
+    int rc;
+    InstState is = istate();
+    const long long n1 = (long long)hctl.nnodes;
+    // counters of store 1 start from zero; phase 1's stay in the per-instance totals
+    HGB_CUDA(cudaMemsetAsync(&dctl()->nnodes, 0, 8, s));
+    HGB_CUDA(cudaMemsetAsync(&dctl()->nkeys, 0, 8, s));
+    HGB_CUDA(cudaMemsetAsync(&dctl()->nslots, 0, 8, s));
+    HGB_CUDA(cudaMemsetAsync(&dctl()->nlive, 0, 8, s));
+    HGB_CUDA(cudaMemsetAsync(is.nlive, 0, (size_t)ninst * 8, s));
+    HGB_CUDA(cudaMemsetAsync(is.nkeys, 0, (size_t)ninst * 8, s));
+    HGB_CUDA(cudaMemsetAsync(is.nfront, 0, (size_t)ninst * 8, s));
+    std::vector<int> one(ninst, 1);
+    HGB_CUDA(cudaMemcpyAsync(is.emode, one.data(), (size_t)ninst * 4, cudaMemcpyHostToDevice, s));
+    for (int q = 0; q < ninst; ++q) h_emode[q] = 1;
+    unsigned long long hcap = 1ull << 16;
+    if ((rc = alloc_store(1, hcap, std::max<long long>(1 << 14, 2LL * ninst)))) return rc;
+    // the p-nodes of phase 1 as a frontier
+    if (n1 > fcapb[cur]) { if ((rc = alloc_front(cur, n1))) return rc; }
+    HGB_CUDA(cudaMemsetAsync(dctl(), 0, kCtlLevelBytes, s));
+    kt.begin(s);
+    Level<D>::collect_p(dn.views_plain, store(0), n1, front(cur), dctl(), s);
+    kt.end(s, KT_OTHER);
+    ++launches;
+    HGB_CUDA(cudaGetLastError());
+    if ((rc = read_ctl())) return rc;
+    long long nf = (long long)hctl.nfront;
+    int level = 0;
+    if ((rc = run_levels(1, 1, cur, nf, level, S[0].nzone.template as<int>()))) return rc;
+    for (int q = 0; q < ninst; ++q) levels[q] = (unsigned long long)level;
+    // stop flags and the sweep
+    const long long n2 = (long long)hctl.nnodes, ne = (long long)hctl.nedges;
+    DBuf stop, W, F;
+    HGB_CUDA(stop.alloc((size_t)std::max<long long>(n2, 1) * 4));
+    HGB_CUDA(W.alloc((size_t)std::max<long long>(n2, 1) * 4));
+    HGB_CUDA(F.alloc((size_t)std::max<long long>(n2, 1) * 4));
+    HGB_CUDA(cudaMemsetAsync(stop.p, 0, stop.bytes, s));
+    HGB_CUDA(cudaMemsetAsync(F.p, 0, F.bytes, s));
+    std::vector<int> ones((size_t)std::max<long long>(n2, 1), 1);
+    HGB_CUDA(cudaMemcpyAsync(W.p, ones.data(), (size_t)std::max<long long>(n2, 1) * 4, cudaMemcpyHostToDevice, s));
+    if (n2 > 0) {
       kt.begin(s);
-      k_rehash<<<1024, 256, 0, s>>>(B.hkey.template as<unsigned long long>(), B.head.template as<int>(), B.hcap,
-                                   k2.template as<unsigned long long>(), h2.template as<int>(), ncap - 1, &dctl->err);
-      kt.end(s, KT_OTHER);
-      ++launches;
-      HGB_CUDA(cudaGetLastError());
-      HGB_CUDA(cudaStreamSynchronize(s));
-      kt.collect();
-      std::swap(B.hkey.p, k2.p); std::swap(B.hkey.bytes, k2.bytes);
-      std::swap(B.head.p, h2.p); std::swap(B.head.bytes, h2.bytes);
-      std::swap(B.pend.p, p2.p); std::swap(B.pend.bytes, p2.bytes);
-      std::swap(B.pend_base.p, pb2.p); std::swap(B.pend_base.bytes, pb2.bytes);
-      B.hcap = ncap;
-    }
-    // ---- probe
-    if (nsucc > 0) {
-      kt.begin(s);
-      Level<D>::probe(dn.views, is, succ(), store(), dctl, nsucc, blocks, s);
-      kt.end(s, KT_PROBE);
-      ++launches;
-      HGB_CUDA(cudaGetLastError());
-    }
-    HGB_CUDA(read_ctl());
-    if (hctl.err) { status = (int)hctl.err; err = "device error in probe"; break; }
-    const long long nsurv = (long long)hctl.nsurv, ntouched = (long long)hctl.ntouched;
-    // ---- deadlock goal on the survivors
-    bool any_dl = false;
-    for (int k = 0; k < ninst; ++k) any_dl |= (nets[k]->kind == HORA_Q_DEADLOCK && !h_done[k]);
-    if (any_dl && nsurv > 0) {
-      kt.begin(s);
-      Level<D>::deadlock(dn.views, is, succ(), dctl, nsurv, blocks, s);
+      Level<D>::stop(dn.views, store(1), n2, stop.template as<int>(), dctl(), blocks, s);
       kt.end(s, KT_DEADLOCK);
       ++launches;
       HGB_CUDA(cudaGetLastError());
-      HGB_CUDA(read_ctl());
-      if (hctl.err) { status = (int)hctl.err; err = "deadlock test exceeded its escape table"; break; }
+      if ((rc = read_ctl())) return rc;
+      if (hctl.err) { err = "stop-set test exceeded its escape table"; return (int)hctl.err; }
     }
-    if (hctl.found) {
-      HGB_CUDA(cudaMemcpyAsync(h_found.data(), is.found, ni4, cudaMemcpyDeviceToHost, s));
-      HGB_CUDA(cudaStreamSynchronize(s));
-    }
-    // ---- room for the new nodes and the next frontier
-    if ((long long)hctl.nnodes + nsurv > B.ncap) {
-      long long nc = B.ncap;
-      while ((long long)hctl.nnodes + nsurv > nc) nc *= 2;
-      const size_t used = hctl.nnodes;
-      HGB_CUDA(B.nzone.grow(nc * Z2 * 4, used * Z2 * 4, s));
-      HGB_CUDA(B.nnext.grow(nc * 4, used * 4, s));
-      HGB_CUDA(B.nlevel.grow(nc * 4, used * 4, s));
-      HGB_CUDA(B.ndead.grow(nc * 4, used * 4, s));
-      HGB_CUDA(B.ninst.grow(nc * 4, used * 4, s));
-      B.ncap = nc;
-    }
-    if (nsurv > B.fcapb[cur ^ 1]) {   // the next frontier holds at most one entry per survivor
-      const int nxt = cur ^ 1;
-      long long fc = B.fcapb[nxt];
-      while (nsurv > fc) fc *= 2;
-      HGB_CUDA(B.fkey[nxt].alloc(fc * 8)); HGB_CUDA(B.fnode[nxt].alloc(fc * 4));
-      HGB_CUDA(B.frank[nxt].alloc(fc * 4)); HGB_CUDA(B.finst[nxt].alloc(fc * 4));
-      B.fcapb[nxt] = fc;
-    }
-    // ---- group + merge
-    if (ntouched > 0) {
+    unsigned long long iters = 0;
+    for (long long guard = 0; guard <= n2 + 1; ++guard) {
+      HGB_CUDA(cudaMemsetAsync(&dctl()->flag, 0, 4, s));
       kt.begin(s);
-      Level<D>::group(succ(), store(), dctl, nsucc, ntouched, s);
-      kt.end(s, KT_GROUP, 2);
-      kt.begin(s);
-      Level<D>::merge(dn.views, is, front(cur), succ(), store(), front(cur ^ 1), dctl, ntouched, level, blocks, s);
-      kt.end(s, KT_MERGE);
-      launches += 3;
+      Level<D>::gfp_pass(edges(), ne, n2, stop.template as<int>(), W.template as<int>(), F.template as<int>(), dctl(), s);
+      kt.end(s, KT_MERGE, 2);
+      launches += 2;
+      ++iters;
       HGB_CUDA(cudaGetLastError());
+      if ((rc = read_ctl())) return rc;
+      if (!hctl.flag) break;
     }
-    HGB_CUDA(read_ctl());
-    if (hctl.err) { status = (int)hctl.err; err = "device error in merge"; break; }
-    // ---- end of level: goals, adaptive extrapolation, next frontier
+    HGB_CUDA(cudaMemsetAsync(is.found, 0, (size_t)ninst * 4, s));
+    kt.begin(s);
+    Level<D>::gfp_verdict(dn.views, store(1), n2, W.template as<int>(), is, dctl(), s);
+    kt.end(s, KT_OTHER);
+    ++launches;
+    HGB_CUDA(cudaGetLastError());
+    if ((rc = read_ctl())) return rc;
+    gfp_iters = iters;
+    pre_calls = (unsigned long long)ne;
+    return HORA_OK;
+  }
+  unsigned long long gfp_iters = 0, pre_calls = 0;
+
+  int finish(std::vector<InstResult>& res, int status, bool leadsto) {
+    const size_t ni4 = (size_t)ninst * 4, ni8 = (size_t)ninst * 8;
+    InstState is = istate();
+    HGB_CUDA(cudaEventRecord(ev1, s));
+    HGB_CUDA(cudaEventSynchronize(ev1));
+    float dev_ms = 0;
+    HGB_CUDA(cudaEventElapsedTime(&dev_ms, ev0, ev1));
+    HGB_CUDA(cudaMemcpyAsync(h_gen.data(), is.generated, ni8, cudaMemcpyDeviceToHost, s));
     HGB_CUDA(cudaMemcpyAsync(h_found.data(), is.found, ni4, cudaMemcpyDeviceToHost, s));
     HGB_CUDA(cudaMemcpyAsync(h_nlive.data(), is.nlive, ni8, cudaMemcpyDeviceToHost, s));
     HGB_CUDA(cudaMemcpyAsync(h_nkeys.data(), is.nkeys, ni8, cudaMemcpyDeviceToHost, s));
     HGB_CUDA(cudaStreamSynchronize(s));
-    bool changed = false;
+    d2h += 2 * ni8 + ni4 + ni8;
+    const double wall = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+    res.assign(ninst, InstResult{});
     for (int k = 0; k < ninst; ++k) {
-      if (h_done[k]) continue;
-      if (h_found[k]) { h_done[k] = 1; changed = true; continue; }
-      // adaptive switch to Extra_LU+ (src/reachability/engine.cpp:2178-2184)
-      if (h_emode[k] == 0 && h_nkeys[k] && (double)h_nlive[k] >= 4.0 * (double)h_nkeys[k]) { h_emode[k] = 1; changed = true; }
+      InstResult& r = res[k];
+      r.status = status;
+      r.verdict = leadsto ? (h_found[k] ? 0 : 1) : (h_found[k] ? 1 : 0);
+      r.st.explored = explored[k];
+      r.st.expanded = explored[k];
+      r.st.generated = h_gen[k];
+      r.st.stored = (uint64_t)std::max<long long>(0, h_nlive[k]);
+      r.st.keys = h_nkeys[k];
+      r.st.levels = levels[k];
+      r.st.probes = ninst == 1 ? hctl.probes : 0;
+      r.st.pre_calls = pre_calls;
+      r.st.gfp_iters = gfp_iters;
+      r.st.kernel_launches = launches;
+      r.st.seconds = wall;
+      r.st.device_seconds = dev_ms * 1e-3;
+      r.st.extrapolating = h_emode[k];
+      r.st.status = status;
+      for (int q = 0; q < 6; ++q) { r.st.kernel_seconds[q] = kt.sec[q]; r.st.kernel_calls[q] = kt.calls[q]; }
+      r.st.h2d_bytes = h2d;
+      r.st.d2h_bytes = d2h;
     }
-    if (changed) {
-      HGB_CUDA(cudaMemcpyAsync(is.done, h_done.data(), ni4, cudaMemcpyHostToDevice, s));
-      HGB_CUDA(cudaMemcpyAsync(is.emode, h_emode.data(), ni4, cudaMemcpyHostToDevice, s));
-    }
-    nfront = (long long)hctl.nfront;
-    cur ^= 1;
+    return status;
   }
-  HGB_CUDA(cudaEventRecord(ev1, s));
-  HGB_CUDA(cudaEventSynchronize(ev1));
-  float dev_ms = 0;
-  HGB_CUDA(cudaEventElapsedTime(&dev_ms, ev0, ev1));
-  HGB_CUDA(cudaMemcpyAsync(h_gen.data(), is.generated, ni8, cudaMemcpyDeviceToHost, s));
-  HGB_CUDA(cudaMemcpyAsync(h_found.data(), is.found, ni4, cudaMemcpyDeviceToHost, s));
-  HGB_CUDA(cudaMemcpyAsync(h_nlive.data(), is.nlive, ni8, cudaMemcpyDeviceToHost, s));
-  HGB_CUDA(cudaMemcpyAsync(h_nkeys.data(), is.nkeys, ni8, cudaMemcpyDeviceToHost, s));
-  HGB_CUDA(cudaStreamSynchronize(s));
-  const double wall = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
-  for (int k = 0; k < ninst; ++k) {
-    InstResult& r = res[k];
-    r.status = status;
-    r.verdict = h_found[k] ? 1 : 0;
-    r.st.explored = explored[k];
-    r.st.expanded = explored[k];
-    r.st.generated = h_gen[k];
-    r.st.stored = (uint64_t)std::max<long long>(0, h_nlive[k]);
-    r.st.keys = h_nkeys[k];
-    r.st.levels = levels[k];
-    r.st.probes = ninst == 1 ? hctl.probes : 0;
-    r.st.kernel_launches = launches;
-    r.st.seconds = wall;
-    r.st.device_seconds = dev_ms * 1e-3;
-    r.st.extrapolating = h_emode[k];
-    r.st.status = status;
-    for (int q = 0; q < 6; ++q) { r.st.kernel_seconds[q] = kt.sec[q]; r.st.kernel_calls[q] = kt.calls[q]; }
-    r.st.h2d_bytes = h2d;
-    r.st.d2h_bytes = d2h;
+};
+
+template <int D>
+int run_group(const std::vector<const HostNet*>& nets, std::vector<InstResult>& res, const RunOptions& o,
+              std::string& err) {
+  Engine<D> E(nets, o, err);
+  int rc = E.setup();
+  if (rc) return rc;
+  long long nf = 0;
+  if ((rc = E.init(&nf))) return rc;
+  int cur = 0, level = 0;
+  const bool leadsto = !nets.empty() && nets[0]->kind == HORA_Q_LEADSTO;
+  int status = E.run_levels(0, 0, cur, nf, level, nullptr);
+  if (status == HORA_OK && leadsto) status = E.leadsto_phase2(cur);
+  if (status != HORA_OK && status != HORA_E_CANCELLED) {
+    E.finish(res, status, leadsto);
+    return status;
   }
-  return status == HORA_E_CANCELLED ? HORA_E_CANCELLED : (status ? status : HORA_OK);
+  const int frc = E.finish(res, status, leadsto);
+  return frc;
 }
+
 
 template <int D>
 int run_expand(const HostNet& net, int n, const int* locs, const int* ints, const int* zones, int emode, int64_t cap,

@@ -23,7 +23,27 @@ static int ceil_log2(long long n) { int b = 0; while ((1LL << b) < n) ++b; retur
 // src/model/network.cpp (compute_bounds :59-85, compute_loc_bounds :105-182, compute_active
 // :184-232), plus the query constants of reach_engine (src/reachability/engine.cpp:1417-1455).
 // ---------------------------------------------------------------------------------------------
-int compile_net(const hora_net_desc* n, int kind, const hora_pred_desc* target, HostNet& H, std::string& err) {
+static int check_pred(const hora_net_desc* n, const hora_pred_desc* t, std::string& err) {
+  if (!t) return HORA_OK;
+  if (t->nloc < 0 || t->nint < 0 || t->nclk < 0) { err = "negative predicate sizes"; return HORA_E_INVALID; }
+  for (int k = 0; k < t->nloc; ++k) {
+    const int p = t->loc_req[2 * k], l = t->loc_req[2 * k + 1];
+    if (p < 0 || p >= n->nprocs || l < 0 || l >= n->proc_nlocs[p]) { err = "predicate location out of range"; return HORA_E_INVALID; }
+  }
+  for (int k = 0; k < t->nint; ++k)
+    if (t->int_cond[3 * k] < 0 || t->int_cond[3 * k] >= n->nints || t->int_cond[3 * k + 1] < 0 || t->int_cond[3 * k + 1] > 5) {
+      err = "bad predicate integer atom"; return HORA_E_INVALID;
+    }
+  for (int k = 0; k < t->nclk; ++k) {
+    const int i = t->clk_cond[3 * k], j = t->clk_cond[3 * k + 1];
+    if (i < 0 || j < 0 || i > n->nclocks || j > n->nclocks) { err = "predicate clock out of range"; return HORA_E_INVALID; }
+    if (i > 0 && j > 0) { err = "diagonal predicate constraint"; return HORA_E_NOT_SUPPORTED; }
+  }
+  return HORA_OK;
+}
+
+int compile_net(const hora_net_desc* n, int kind, const hora_pred_desc* target, const hora_pred_desc* q, HostNet& H,
+                std::string& err) {
   if (!n) { err = "null network"; return HORA_E_INVALID; }
   if (n->nprocs <= 0 || n->nclocks < 0 || n->nints < 0 || n->nchans < 0 || n->nedges < 0) {
     err = "negative or empty sizes in the network descriptor";
@@ -218,12 +238,47 @@ int compile_net(const hora_net_desc* n, int kind, const hora_pred_desc* target, 
     for (int c = 0; c < dim; ++c) H.L[c] = H.U[c] = std::max(H.L[c], H.U[c]);
     for (size_t k = 0; k < H.Lloc.size(); ++k) H.Lloc[k] = H.Uloc[k] = std::max(H.Lloc[k], H.Uloc[k]);
   }
+  {
+    int rc = check_pred(n, target, err);
+    if (!rc) rc = check_pred(n, q, err);
+    if (rc) return rc;
+  }
+  if (kind == HORA_Q_LEADSTO) {
+    // leads-to: the constants of p and q join the bounds of their clock, which are then collapsed
+    // to the deadlock-sound a_M form L = U = max(L, U) (the route's two searches need a
+    // bisimulation: deadlocks and time divergence must be preserved)
+    if (!target || !q) { err = "leads-to needs p and q"; return HORA_E_INVALID; }
+    if (q->nclk > 1) { err = "the complement of q's clock part must be convex: at most one clock atom"; return HORA_E_NOT_SUPPORTED; }
+    const hora_pred_desc* preds[2] = {target, q};
+    for (const hora_pred_desc* t : preds)
+      for (int k = 0; k < t->nclk; ++k) {
+        const int i = t->clk_cond[3 * k], j = t->clk_cond[3 * k + 1], v = raw_bound(t->clk_cond[3 * k + 2]);
+        const int x = i > 0 ? i : j;
+        if (x <= 0) continue;
+        H.qmask |= 1ull << x;
+        const int a = v < 0 ? -v : v;
+        H.L[x] = std::max(H.L[x], a); H.U[x] = std::max(H.U[x], a);
+        H.Lq[x] = std::max(H.Lq[x], a); H.Uq[x] = std::max(H.Uq[x], a);
+      }
+    for (int c = 0; c < dim; ++c) { H.L[c] = H.U[c] = std::max(H.L[c], H.U[c]); H.Lq[c] = H.Uq[c] = std::max(H.Lq[c], H.Uq[c]); }
+    for (size_t k = 0; k < H.Lloc.size(); ++k) H.Lloc[k] = H.Uloc[k] = std::max(H.Lloc[k], H.Uloc[k]);
+    H.L[0] = H.U[0] = 0;
+    H.p_loc.assign(target->loc_req, target->loc_req + 2 * target->nloc);
+    H.p_int.assign(target->int_cond, target->int_cond + 3 * target->nint);
+    H.p_clk.assign(target->clk_cond, target->clk_cond + 3 * target->nclk);
+    H.av_on = 1;
+    H.av_loc.assign(q->loc_req, q->loc_req + 2 * q->nloc);
+    H.av_int.assign(q->int_cond, q->int_cond + 3 * q->nint);
+    H.av_nclk = q->nclk;
+    if (q->nclk == 1) {
+      H.av_neg[0] = q->clk_cond[1];
+      H.av_neg[1] = q->clk_cond[0];
+      const int r = q->clk_cond[2], v = raw_bound(r);
+      H.av_neg[2] = (r & 1) ? ((-v) << 1) : (((-v) << 1) | 1);
+    }
+  }
   if (kind == HORA_Q_REACH && target) {
     H.t_never = target->never;
-    for (int k = 0; k < target->nloc; ++k) {
-      const int p = target->loc_req[2 * k], l = target->loc_req[2 * k + 1];
-      if (p < 0 || p >= np || l < 0 || l >= n->proc_nlocs[p]) { err = "target location out of range"; return HORA_E_INVALID; }
-    }
     H.t_loc.assign(target->loc_req, target->loc_req + 2 * target->nloc);
     H.t_int.assign(target->int_cond, target->int_cond + 3 * target->nint);
     H.t_clk.assign(target->clk_cond, target->clk_cond + 3 * target->nclk);
@@ -244,6 +299,7 @@ int compile_net(const hora_net_desc* n, int kind, const hora_pred_desc* target, 
 DeviceNets::~DeviceNets() {
   for (void* b : blobs) cudaFree(b);
   if (views) cudaFree(views);
+  if (views_plain) cudaFree(views_plain);
   if (ok) cudaFree(ok);
 }
 
@@ -268,7 +324,8 @@ int upload_nets(const std::vector<const HostNet*>& nets, int inst_shift, DeviceN
                                           &H.edge_chan, &H.edge_dir, &H.edge_guard_off, &H.edge_iguard_off,
                                           &H.edge_reset_off, &H.edge_iupd_off, &H.cons, &H.iatoms, &H.resets,
                                           &H.iupds, &H.Lloc, &H.Uloc, &act32, &H.kshift, &H.kwidth, &H.L, &H.U,
-                                          &H.Lq, &H.Uq, &H.t_loc, &H.t_int, &H.t_clk};
+                                          &H.Lq, &H.Uq, &H.t_loc, &H.t_int, &H.t_clk, &H.av_loc, &H.av_int,
+                                          &H.p_loc, &H.p_int, &H.p_clk};
     for (auto* a : arrs) add(*a);
     void* d = nullptr;
     cudaError_t e = cudaMalloc(&d, blob.size() * 4);
@@ -297,9 +354,19 @@ int upload_nets(const std::vector<const HostNet*>& nets, int inst_shift, DeviceN
     V.t_never = H.t_never;
     V.t_nloc = (int)H.t_loc.size() / 2; V.t_nint = (int)H.t_int.size() / 3; V.t_nclk = (int)H.t_clk.size() / 3;
     V.t_loc = b + offs[q++]; V.t_int = b + offs[q++]; V.t_clk = b + offs[q++];
+    V.av_on = H.av_on; V.av_nclk = H.av_nclk;
+    V.av_nloc = (int)H.av_loc.size() / 2; V.av_nint = (int)H.av_int.size() / 3;
+    V.av_neg[0] = H.av_neg[0]; V.av_neg[1] = H.av_neg[1]; V.av_neg[2] = H.av_neg[2];
+    V.av_loc = b + offs[q++]; V.av_int = b + offs[q++];
+    V.p_nloc = (int)H.p_loc.size() / 2; V.p_nint = (int)H.p_int.size() / 3; V.p_nclk = (int)H.p_clk.size() / 3;
+    V.p_loc = b + offs[q++]; V.p_int = b + offs[q++]; V.p_clk = b + offs[q++];
   }
   cudaError_t e = cudaMalloc(&out.views, sizeof(NetView) * std::max(ninst, 1));
   if (e == cudaSuccess) e = cudaMemcpy(out.views, out.host_views.data(), sizeof(NetView) * ninst, cudaMemcpyHostToDevice);
+  std::vector<NetView> plain = out.host_views;
+  for (NetView& V : plain) V.av_on = 0;
+  if (e == cudaSuccess) e = cudaMalloc(&out.views_plain, sizeof(NetView) * std::max(ninst, 1));
+  if (e == cudaSuccess) e = cudaMemcpy(out.views_plain, plain.data(), sizeof(NetView) * ninst, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMalloc(&out.ok, sizeof(int) * std::max(ninst, 1));
   if (e == cudaSuccess) e = cudaMemcpy(out.ok, okv.data(), sizeof(int) * ninst, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) { err = std::string("CUDA: ") + cudaGetErrorString(e); return HORA_E_CUDA; }
@@ -364,14 +431,15 @@ int32_t hora_gb_device_count(int32_t* count) {
   return HORA_OK;
 }
 
-static int32_t run_single(const hora_net_desc* net, int kind, const hora_pred_desc* target, int32_t backend,
-                          hora_stats* stats, const volatile int32_t* cancel, int32_t* result) {
+static int32_t run_single(const hora_net_desc* net, int kind, const hora_pred_desc* target,
+                          const hora_pred_desc* qpred, int32_t backend, hora_stats* stats,
+                          const volatile int32_t* cancel, int32_t* result) {
   g_last_error.clear();
   if (!result) return fail(HORA_E_INVALID, "null result pointer");
   if (backend != HORA_BACKEND_CUDA) return fail(HORA_E_NOT_SUPPORTED, "this library implements the cuda backend only");
   HostNet H;
   std::string err;
-  int rc = compile_net(net, kind, target, H, err);
+  int rc = compile_net(net, kind, target, qpred, H, err);
   if (rc) return fail(rc, err);
   if ((rc = ensure_device())) return rc;
   std::vector<const HostNet*> v{&H};
@@ -388,18 +456,18 @@ static int32_t run_single(const hora_net_desc* net, int kind, const hora_pred_de
 int32_t hora_gb_reachable_net(const hora_net_desc* net, const hora_pred_desc* target, int32_t backend,
                               hora_stats* stats, int32_t* result) {
   if (!target) return fail(HORA_E_INVALID, "null target");
-  return run_single(net, HORA_Q_REACH, target, backend, stats, nullptr, result);
+  return run_single(net, HORA_Q_REACH, target, nullptr, backend, stats, nullptr, result);
 }
 
 int32_t hora_gb_deadlock_reachable(const hora_net_desc* net, int32_t backend, hora_stats* stats,
                                    const volatile int32_t* cancel, int32_t* result) {
-  return run_single(net, HORA_Q_DEADLOCK, nullptr, backend, stats, cancel, result);
+  return run_single(net, HORA_Q_DEADLOCK, nullptr, nullptr, backend, stats, cancel, result);
 }
 
 int32_t hora_gb_leads_to(const hora_net_desc* net, const hora_pred_desc* p, const hora_pred_desc* q,
                          int32_t backend, hora_stats* stats, int32_t* result) {
-  (void)net; (void)p; (void)q; (void)backend; (void)stats; (void)result;
-  return fail(HORA_E_NOT_SUPPORTED, "leads-to is not available in this build");
+  if (!p || !q) return fail(HORA_E_INVALID, "null predicate");
+  return run_single(net, HORA_Q_LEADSTO, p, q, backend, stats, nullptr, result);
 }
 
 int32_t hora_gb_expand(const hora_net_desc* net, int32_t n, const int32_t* locs, const int32_t* ints,
@@ -410,7 +478,7 @@ int32_t hora_gb_expand(const hora_net_desc* net, int32_t n, const int32_t* locs,
   if (n < 0 || !out_n) return fail(HORA_E_INVALID, "bad arguments");
   HostNet H;
   std::string err;
-  int rc = compile_net(net, HORA_Q_REACH, nullptr, H, err);
+  int rc = compile_net(net, HORA_Q_REACH, nullptr, nullptr, H, err);
   if (rc) return fail(rc, err);
   if ((rc = ensure_device())) return rc;
   if (L && U) {
@@ -437,7 +505,7 @@ int32_t hora_gb_has_deadlock(const hora_net_desc* net, int32_t n, const int32_t*
   if (n < 0 || !out) return fail(HORA_E_INVALID, "bad arguments");
   HostNet H;
   std::string err;
-  int rc = compile_net(net, HORA_Q_DEADLOCK, nullptr, H, err);
+  int rc = compile_net(net, HORA_Q_DEADLOCK, nullptr, nullptr, H, err);
   if (rc) return fail(rc, err);
   if ((rc = ensure_device())) return rc;
   if (n == 0) return HORA_OK;
@@ -458,16 +526,16 @@ int32_t hora_gb_batch_run(int32_t n, const hora_net_desc* nets, const hora_query
   int rc = ensure_device();
   if (rc) return rc;
   std::vector<HostNet> H(n);
+  // one device group per (dimension, leads-to or not): a group runs one level loop
   std::map<int, std::vector<int>> by_dim;
   for (int k = 0; k < n; ++k) {
     verdicts[k] = -1;
     std::string err;
     const hora_query_desc& q = queries[k];
-    int r = HORA_OK;
-    if (q.kind == HORA_Q_LEADSTO) r = HORA_E_NOT_SUPPORTED;
-    else r = compile_net(&nets[k], q.kind, q.kind == HORA_Q_REACH ? &q.p : nullptr, H[k], err);
+    const int r = compile_net(&nets[k], q.kind, q.kind == HORA_Q_DEADLOCK ? nullptr : &q.p,
+                              q.kind == HORA_Q_LEADSTO ? &q.q : nullptr, H[k], err);
     if (stats) { std::memset(&stats[k], 0, sizeof(hora_stats)); stats[k].status = r; }
-    if (r == HORA_OK) by_dim[H[k].dim].push_back(k);
+    if (r == HORA_OK) by_dim[H[k].dim * 2 + (q.kind == HORA_Q_LEADSTO ? 1 : 0)].push_back(k);
   }
   std::string err;
   int first_err = HORA_OK;
@@ -476,7 +544,7 @@ int32_t hora_gb_batch_run(int32_t n, const hora_net_desc* nets, const hora_query
     for (int k : kv.second) v.push_back(&H[k]);
     std::vector<InstResult> res;
     RunOptions o;
-    const int r = dispatch_group(kv.first, v, res, o, err);
+    const int r = dispatch_group(kv.first / 2, v, res, o, err);
     for (size_t q = 0; q < kv.second.size(); ++q) {
       const int k = kv.second[q];
       if (q < res.size()) {

@@ -22,17 +22,24 @@ struct HostNet {
       eloc, edge_tgt, edge_chan, edge_dir, edge_guard_off, edge_iguard_off, edge_reset_off, edge_iupd_off, cons,
       iatoms, resets, iupds, Lloc, Uloc, kshift, kwidth, L, U, Lq, Uq, t_loc, t_int, t_clk;
   std::vector<unsigned long long> act;
+  // leads-to
+  int av_on = 0, av_nclk = 0;
+  int av_neg[3] = {0, 0, 0};
+  std::vector<int32_t> av_loc, av_int, p_loc, p_int, p_clk;
 };
 
-// Compile `net` for query `kind` (HORA_Q_*); `target` is the reach target (may be null).
+// Compile `net` for query `kind` (HORA_Q_*): `p` is the reach target or the left side of a
+// leads-to, `q` its right side (both may be null when unused).
 // Returns HORA_OK, HORA_E_INVALID or HORA_E_NOT_SUPPORTED with a message in `err`.
-int compile_net(const hora_net_desc* net, int kind, const hora_pred_desc* target, HostNet& out, std::string& err);
+int compile_net(const hora_net_desc* net, int kind, const hora_pred_desc* p, const hora_pred_desc* q, HostNet& out,
+                std::string& err);
 
 // Device copy of one or more compiled instances: a blob per instance and the NetView array.
 struct DeviceNets {
   std::vector<void*> blobs;
   std::vector<size_t> blob_bytes;
   NetView* views = nullptr;   // device array
+  NetView* views_plain = nullptr;  // the same with the leads-to restriction off (reachability phases)
   std::vector<NetView> host_views;
   int* ok = nullptr;          // device array of per-instance "runnable" flags
   ~DeviceNets();

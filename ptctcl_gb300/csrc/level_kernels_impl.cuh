@@ -144,7 +144,7 @@ __global__ void __launch_bounds__(kBlock) k_expand(const NetView* nets, InstStat
     }
     if (t.i == 0) {
       if (!ok) atomicMax(&ctl->err, 4u);
-      if (ord) atomicAdd(&is.generated[inst], (unsigned long long)ord);
+      if (ord && !roots) atomicAdd(&is.generated[inst], (unsigned long long)ord);
       if (hit) { is.found[inst] = 1; atomicOr(&ctl->found, 1u); }
     }
   }

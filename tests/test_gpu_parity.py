@@ -131,3 +131,50 @@ def test_batch_matches_single():
         assert v == int(want)
         for k in COUNT_KEYS:
             assert s[k] == wst[k], (k, s[k], wst[k])
+
+
+LT_ROWS = verdict_rows(kinds=(2,))
+LT_COUNTS = ("explored", "generated", "stored", "keys", "levels")
+SLOW_ORACLE = {("grc4", "x0 >= 0 --> T0.far"), ("grc4", "T0.in && x0 >= 0 --> T0.far"),
+               ("grc4", "T0.in --> T0.far && x0 >= 0"), ("grc4", "T0.in --> T0.far")}
+
+
+@pytest.mark.parametrize("model,formula,kind,p,q,result", LT_ROWS, ids=[f"{r[0]}:{r[1]}" for r in LT_ROWS])
+def test_reference_leadsto_verdicts_gpu(model, formula, kind, p, q, result):
+    net = load_model(model)
+    st = ReachStats()
+    got = engine.leads_to_clocks(net, p, q, Backend.Cuda, st)
+    assert got == result
+    if (model, formula) not in SLOW_ORACLE:
+        want, wst = pyoracle.leads_to(net, p, q)
+        for k in LT_COUNTS:
+            assert getattr(st, k) == wst[k], (k, getattr(st, k), wst[k])
+
+
+def small_config3(seed):
+    """The config-3 generator and query shape at a size the single-threaded oracle finishes in
+    seconds (4 automata x 5 locations, 3 clocks); full-size config-3 instances run GPU-only."""
+    import dataclasses
+    from ptctcl_gb300 import generator as G
+    rng = np.random.default_rng([33, seed])
+    g = dataclasses.replace(G.CONFIG_PARAMS[3], nprocs=4, nlocs=5, nclocks=3)
+    net = G.random_network(rng, g)
+    p = Pred(G.two_locations(rng, net), [], [G.clock_term(rng, net, 30)])
+    q = Pred(G.two_locations(rng, net), [], [G.clock_term(rng, net, 30)])
+    return net, 2, p, q
+
+
+# seeds whose oracle run ends within seconds; all non-trivial ones are violated (random networks
+# nearly always admit a run that never reaches q), the others hold because p is unreachable
+SMALL_C3 = [0, 1, 3, 12, 13, 14, 17, 20, 23, 25, 33, 35, 37, 39]
+
+
+@pytest.mark.parametrize("seed", SMALL_C3)
+def test_leadsto_config3(seed):
+    net, kind, p, q = small_config3(seed)
+    want, wst = pyoracle.leads_to(net, p, q)
+    st = ReachStats()
+    got = engine.leads_to_clocks(net, p, q, Backend.Cuda, st)
+    assert got == want
+    for k in LT_COUNTS:
+        assert getattr(st, k) == wst[k], (k, getattr(st, k), wst[k])
