@@ -124,6 +124,117 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def percentile(xs, q):
+    if not xs:
+        return None
+    xs = sorted(xs)
+    k = min(len(xs) - 1, max(0, int(round(q / 100.0 * (len(xs) - 1)))))
+    return xs[k]
+
+
+def run_batched(args):
+    """Config 4: N seeded networks in one batched run vs the same instances one at a time, each form
+    given the same wall-time budget (some generated instances have millions of zones)."""
+    import ctypes
+    from ptctcl_gb300 import engine
+    from ptctcl_gb300.generator import config_instance
+    items = [config_instance(4, s) for s in range(args.instances)]
+    budget = args.budget
+
+    def timed(fn):
+        cancel = ctypes.c_int32(0)
+        tm = threading.Timer(budget, lambda: setattr(cancel, "value", 1))
+        tm.start()
+        t = time.perf_counter()
+        out = fn(cancel)
+        dt = time.perf_counter() - t
+        tm.cancel()
+        return out, dt
+
+    (bv, bst), bdt = timed(lambda c: engine.batch_run(items, cancel=c))
+    b_done = [s for v, s in zip(bv, bst) if v >= 0]
+    b_gen = sum(s["generated"] for s in bst)
+    plain_gen, plain_done, plain_lat, t0 = 0, 0, [], time.perf_counter()
+    for it in items:
+        left = budget - (time.perf_counter() - t0)
+        if left <= 0:
+            break
+        cancel = ctypes.c_int32(0)
+        tm = threading.Timer(left, lambda c=cancel: setattr(c, "value", 1))
+        tm.start()
+        v, st = engine.batch_run([it], cancel=cancel)
+        tm.cancel()
+        plain_gen += st[0]["generated"]
+        if v[0] >= 0:
+            plain_done += 1
+            plain_lat.append(time.perf_counter() - t0)
+    pdt = time.perf_counter() - t0
+    lat = [s["seconds"] for s in b_done]
+    line = {"metric": METRIC, "workload": f"config4: {args.instances} seeded networks (clocks U[2,16], automata "
+            f"U[2,10], locations U[4,12], c in [0,40], query mix 60/30/10), {budget:.0f} s budget per form",
+            "batched": {"value": b_gen / bdt, "unit": UNIT, "seconds": bdt, "verdicts": len(b_done),
+                        "p50_time_to_verdict_s": percentile(lat, 50), "p99_time_to_verdict_s": percentile(lat, 99)},
+            "plain_one_at_a_time": {"value": plain_gen / pdt, "unit": UNIT, "seconds": pdt, "verdicts": plain_done,
+                                    "p50_time_to_verdict_s": percentile(plain_lat, 50),
+                                    "p99_time_to_verdict_s": percentile(plain_lat, 99)},
+            "speedup_successors_per_s": (b_gen / bdt) / max(1e-9, plain_gen / pdt)}
+    print(json.dumps(line), flush=True)
+
+
+def run_serving(args):
+    """Config 5: Poisson arrivals of config-3-distribution requests, continuous admission by a
+    device-memory budget; p50/p99 time-to-verdict and sustained successors/s."""
+    import ctypes
+    import random
+    from ptctcl_gb300 import capi
+    from ptctcl_gb300.model import NetArrays, QueryArrays, Stats
+    from ptctcl_gb300.generator import config_instance
+    lib = capi.load()
+    srv = ctypes.c_void_p()
+    capi.check(lib.hora_gb_server_create(int(args.budget_gb * (1 << 30)), args.inflight, ctypes.byref(srv)), "server")
+    rng = random.Random(5)
+    t0 = time.perf_counter()
+    tickets, keep, k = [], [], 0
+    next_t = 0.0
+    while True:
+        now = time.perf_counter() - t0
+        if now >= args.duration:
+            break
+        if now >= next_t:
+            net, kind, p, q = config_instance(args.serve_config, 100000 + k)
+            na, qa = NetArrays(net), QueryArrays(kind, p, q)
+            keep.append((na, qa))
+            tk = ctypes.c_int64(0)
+            rc = lib.hora_gb_server_submit(srv, ctypes.addressof(na.desc), ctypes.addressof(qa.desc), ctypes.byref(tk))
+            if rc == capi.OK:
+                tickets.append(tk.value)
+            k += 1
+            next_t += rng.expovariate(args.rate)
+        else:
+            time.sleep(min(0.002, next_t - now))
+    submitted = time.perf_counter() - t0
+    # drain
+    lat, gen, done = [], 0, 0
+    active = ctypes.c_int32(1)
+    while active.value > 0 and time.perf_counter() - t0 < args.duration + args.drain:
+        lib.hora_gb_server_step(srv, ctypes.byref(active))
+    total = time.perf_counter() - t0
+    for tk in tickets:
+        d, v, st = ctypes.c_int32(0), ctypes.c_int32(0), Stats()
+        lib.hora_gb_server_poll(srv, tk, ctypes.byref(d), ctypes.byref(v), ctypes.byref(st))
+        if d.value:
+            done += 1
+            lat.append(st.seconds)
+            gen += st.generated
+    lib.hora_gb_server_destroy(srv)
+    line = {"metric": METRIC, "workload": f"config{args.serve_config} requests, Poisson {args.rate}/s for "
+            f"{args.duration:.0f} s, budget {args.budget_gb} GB, {args.inflight} in flight",
+            "offered": len(tickets), "finished": done, "value": gen / total, "unit": UNIT,
+            "p50_time_to_verdict_s": percentile(lat, 50), "p99_time_to_verdict_s": percentile(lat, 99),
+            "seconds": total, "submit_seconds": submitted}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -132,7 +243,22 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--seed", type=int, default=WORKLOAD_SEED)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="deadlock", choices=["deadlock", "batched", "serving"])
+    ap.add_argument("--instances", type=int, default=4096)
+    ap.add_argument("--budget", type=float, default=60.0)
+    ap.add_argument("--rate", type=float, default=100.0)
+    ap.add_argument("--duration", type=float, default=60.0)
+    ap.add_argument("--drain", type=float, default=120.0)
+    ap.add_argument("--budget-gb", type=float, default=64.0)
+    ap.add_argument("--inflight", type=int, default=64)
+    ap.add_argument("--serve-config", type=int, default=3)
     args = ap.parse_args()
+    if args.workload == "batched":
+        run_batched(args)
+        return
+    if args.workload == "serving":
+        run_serving(args)
+        return
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

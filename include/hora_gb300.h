@@ -208,10 +208,14 @@ HORA_GB_API int32_t hora_gb_has_deadlock(const hora_net_desc* net, int32_t n, co
 
 /* Run n independent (network, query) instances together on the device. verdicts[k] receives the
  * result in the single-query convention of the query's kind (reach: reachable; deadlock: deadlock
- * reachable; leads-to: holds); stats (may be null) one record per instance. Returns HORA_OK when
- * every instance ran; per-instance failures are reported in stats[k].status and verdicts[k] = -1. */
+ * reachable; leads-to: holds); stats (may be null) one record per instance, whose seconds field is
+ * the time from the start of the call to that instance's verdict. Returns HORA_OK when every
+ * instance ran; per-instance failures are reported in stats[k].status and verdicts[k] = -1.
+ * cancel (may be null) is polled between BFS levels: once it reads non-zero the call returns
+ * HORA_E_CANCELLED, instances that already had their verdict keep it (status HORA_OK) and the
+ * others report HORA_E_CANCELLED. */
 HORA_GB_API int32_t hora_gb_batch_run(int32_t n, const hora_net_desc* nets, const hora_query_desc* queries,
-                          int32_t* verdicts, hora_stats* stats);
+                          int32_t* verdicts, hora_stats* stats, const volatile int32_t* cancel);
 
 /* ---- serving form ------------------------------------------------------------------------------ */
 

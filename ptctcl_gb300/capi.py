@@ -58,7 +58,7 @@ def load(build_if_missing: bool = True):
     L.hora_gb_expand.restype = I32
     L.hora_gb_has_deadlock.argtypes = [VP, I32, P32, P32, P32, P32]
     L.hora_gb_has_deadlock.restype = I32
-    L.hora_gb_batch_run.argtypes = [I32, VP, VP, P32, VP]
+    L.hora_gb_batch_run.argtypes = [I32, VP, VP, P32, VP, VP]
     L.hora_gb_batch_run.restype = I32
     L.hora_gb_server_create.argtypes = [U64, I32, ctypes.POINTER(VP)]
     L.hora_gb_server_create.restype = I32

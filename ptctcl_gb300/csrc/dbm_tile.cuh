@@ -250,6 +250,44 @@ __device__ __forceinline__ bool alu_le(const Tile<D>& t, const int (&z)[D], cons
   return !t.any(witness);
 }
 
+// Z ≼_aLU Zp decided by ONE lane from whole matrices in global memory (row-major D*D, read through
+// L2 so zones another lane of the tile just wrote are seen), with the per-clock bounds L[] and U[]
+// in registers: the same test as alu_le, used where a tile spreads several stored zones over its
+// lanes instead of one zone over its rows.
+template <int D>
+__device__ __forceinline__ bool alu_le_lane(const int* Z, const int* Zp, const int (&L)[D], const int (&U)[D]) {
+#pragma unroll
+  for (int x = 0; x < D; ++x) {
+    if (U[x] == kAluNegInf) continue;
+    const int z0x = __ldcg(Z + x);
+    if (z0x < r_le(-U[x])) continue;
+#pragma unroll
+    for (int y = 0; y < D; ++y) {
+      if (y == x || L[y] == kAluNegInf) continue;
+      const int zp = __ldcg(Zp + y * D + x);
+      if (zp < __ldcg(Z + y * D + x) && r_add(zp, r_lt(-L[y])) < z0x) return false;
+    }
+  }
+  return true;
+}
+
+// Necessary condition for a convex union, from the clock bounds alone (netengine_metal.mm:455-465):
+// if the projections of a and b on some clock are separated by a gap, a ∪ b is not convex.
+template <int D>
+__device__ __forceinline__ bool union_axis_gap(const Tile<D>& t, const int (&a)[D], const int (&b)[D]) {
+  const int i = t.i;
+  int a0[D], b0[D];
+#pragma unroll
+  for (int j = 0; j < D; ++j) { a0[j] = t.shfl(a[j], 0); b0[j] = t.shfl(b[j], 0); }
+  const int a0i = sel(a0, i), b0i = sel(b0, i);   // row 0 entry i: minus the lower bound of clock i
+  bool gap = false;
+  if (i > 0) {
+    if (b[0] < kInf && a0i < kInf && -r_bound(a0i) > r_bound(b[0])) gap = true;
+    if (a[0] < kInf && b0i < kInf && -r_bound(b0i) > r_bound(a[0])) gap = true;
+  }
+  return t.any(gap);
+}
+
 // One half of the exact convex-union test: does every region the hull h gains past one of z's
 // constraints lie inside `other`?
 template <int D>
@@ -284,6 +322,7 @@ __device__ __forceinline__ bool facets_inside(const Tile<D>& t, const int (&z)[D
 // On success `a` becomes the hull (the entrywise max of two canonical DBMs is canonical).
 template <int D>
 __device__ __forceinline__ bool try_union(const Tile<D>& t, int (&a)[D], const int (&b)[D]) {
+  if (union_axis_gap(t, a, b)) return false;
   int h[D];
 #pragma unroll
   for (int j = 0; j < D; ++j) h[j] = a[j] > b[j] ? a[j] : b[j];

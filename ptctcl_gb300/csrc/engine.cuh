@@ -72,6 +72,7 @@ struct Ctl {
   unsigned long long ntouched;   // hash slots with pending successors
   unsigned long long seg_alloc;  // grouping segment allocator
   unsigned long long nfront;     // next-frontier entries
+  unsigned long long chain_alloc;  // merge's chain-list allocator
   unsigned int found;            // some instance hit its goal this level
   unsigned int overflow;         // expand output overflowed
   // cumulative
@@ -84,6 +85,6 @@ struct Ctl {
   unsigned int err;              // HORA_E_* raised on the device (table full, escape overflow)
   unsigned int flag;             // set by a fixpoint pass that changed something
 };
-constexpr unsigned long long kCtlLevelBytes = 5 * 8 + 2 * 4;
+constexpr unsigned long long kCtlLevelBytes = 6 * 8 + 2 * 4;
 
 }  // namespace hgb

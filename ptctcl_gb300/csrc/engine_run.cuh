@@ -119,8 +119,10 @@ struct Engine {
   int blocks = 0;
   DeviceNets dn;
   StoreBufs<D> S[2];
-  DBuf skey, sparent, sord, sslot, srank, szone, ssurv, sseg, ssorted, stouched;
+  DBuf skey, sparent, sord, sslot, srank, szone, ssurv, sseg, ssorted, stouched, sokh, sokl, sskh, sskl;
   long long scap = 0;
+  DBuf clist;
+  long long ccap = 0;
   DBuf fkey[2], fnode[2], frank[2], finst[2];
   long long fcapb[2] = {0, 0};
   DBuf esrc, edst;
@@ -133,6 +135,7 @@ struct Engine {
   std::vector<unsigned> h_found;
   std::vector<unsigned long long> h_nfront, h_nkeys, h_gen, explored, levels;
   std::vector<long long> h_nlive;
+  std::vector<double> t_fin;   // per instance: seconds from the start to its verdict (-1: not yet)
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   std::chrono::steady_clock::time_point t_start;
 
@@ -160,6 +163,9 @@ struct Engine {
     sc.ord = sord.template as<int>(); sc.slot = sslot.template as<int>(); sc.rank = srank.template as<int>();
     sc.zone = szone.template as<int>(); sc.surv = ssurv.template as<int>(); sc.seg = sseg.template as<int>();
     sc.sorted = ssorted.template as<int>(); sc.touched = stouched.template as<int>(); sc.cap = scap;
+    sc.okh = sokh.template as<unsigned long long>(); sc.okl = sokl.template as<unsigned long long>();
+    sc.skh = sskh.template as<unsigned long long>(); sc.skl = sskl.template as<unsigned long long>();
+    sc.clist = clist.template as<int>(); sc.ccap = ccap;
     return sc;
   }
   Front front(int b) {
@@ -205,6 +211,8 @@ struct Engine {
     HGB_CUDA(sslot.alloc(cap * 4)); HGB_CUDA(srank.alloc(cap * 4)); HGB_CUDA(szone.alloc(cap * Z2 * 4));
     HGB_CUDA(ssurv.alloc(cap * 4)); HGB_CUDA(sseg.alloc(cap * 4)); HGB_CUDA(ssorted.alloc(cap * 4));
     HGB_CUDA(stouched.alloc(cap * 4));
+    HGB_CUDA(sokh.alloc(cap * 8)); HGB_CUDA(sokl.alloc(cap * 8));
+    HGB_CUDA(sskh.alloc(cap * 8)); HGB_CUDA(sskl.alloc(cap * 8));
     return HORA_OK;
   }
   int alloc_front(int b, long long cap) {
@@ -299,6 +307,7 @@ struct Engine {
     h_done.assign(ninst, 0); h_emode.assign(ninst, 0); h_found.assign(ninst, 0);
     h_nfront.assign(ninst, 0); h_nkeys.assign(ninst, 0); h_gen.assign(ninst, 0);
     h_nlive.assign(ninst, 0); explored.assign(ninst, 0); levels.assign(ninst, 0);
+    t_fin.assign(ninst, -1.0);
     HGB_CUDA(cudaEventCreate(&ev0));
     HGB_CUDA(cudaEventCreate(&ev1));
     HGB_CUDA(cudaEventRecord(ev0, s));
@@ -342,6 +351,12 @@ struct Engine {
       if (!roots)
         for (int q = 0; q < ninst; ++q)
           if (!h_done[q] && h_nfront[q]) { explored[q] += h_nfront[q]; levels[q] = level; }
+      if (mode == 0) {
+        // a forward search whose frontier ran dry has its verdict: record when
+        const double now = elapsed();
+        for (int q = 0; q < ninst; ++q)
+          if (!h_done[q] && !h_nfront[q] && t_fin[q] < 0 && nets[q]->kind != HORA_Q_LEADSTO) t_fin[q] = now;
+      }
       // ---- expand; re-run with a larger buffer on overflow (it writes nothing persistent)
       const int* src = roots ? roots_src : S[k].nzone.template as<int>();
       for (;;) {
@@ -392,6 +407,12 @@ struct Engine {
         while (nsurv > fc) fc *= 2;
         if ((rc = alloc_front(cur ^ 1, fc))) return rc;
       }
+      if ((long long)hctl.nnodes + nsurv > ccap) {   // the merge gathers every touched key's chain
+        long long c = std::max<long long>(ccap, 1 << 16);
+        while ((long long)hctl.nnodes + nsurv > c) c *= 2;
+        HGB_CUDA(clist.alloc(c * 4));
+        ccap = c;
+      }
       const int record = (mode == 1 && !roots) ? 1 : 0;
       if (record && (rc = ensure_edges((long long)hctl.nedges + nsucc))) return rc;
       // ---- group + merge
@@ -415,9 +436,15 @@ struct Engine {
         HGB_CUDA(cudaMemcpyAsync(h_nkeys.data(), is.nkeys, ni8, cudaMemcpyDeviceToHost, s));
         HGB_CUDA(cudaStreamSynchronize(s));
         bool changed = false;
+        const double now = elapsed();
         for (int q = 0; q < ninst; ++q) {
           if (h_done[q]) continue;
-          if (h_found[q]) { h_done[q] = 1; changed = true; continue; }
+          if (h_found[q]) {
+            h_done[q] = 1;
+            changed = true;
+            if (t_fin[q] < 0 && nets[q]->kind != HORA_Q_LEADSTO) t_fin[q] = now;
+            continue;
+          }
           // adaptive switch to Extra_LU+ (src/reachability/engine.cpp:2178-2184)
           if (h_emode[q] == 0 && h_nkeys[q] && (double)h_nlive[q] >= 4.0 * (double)h_nkeys[q]) { h_emode[q] = 1; changed = true; }
         }
@@ -509,6 +536,13 @@ struct Engine {
   }
   unsigned long long gfp_iters = 0, pre_calls = 0;
 
+  double elapsed() const {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+  }
+
+  // Per-instance results. After a cancellation, forward-route instances that already had their
+  // verdict (goal found, or frontier exhausted) report it with HORA_OK; the others report
+  // HORA_E_CANCELLED. st.seconds is the time from the start of the run to the instance's verdict.
   int finish(std::vector<InstResult>& res, int status, bool leadsto) {
     const size_t ni4 = (size_t)ninst * 4, ni8 = (size_t)ninst * 8;
     InstState is = istate();
@@ -522,11 +556,12 @@ struct Engine {
     HGB_CUDA(cudaMemcpyAsync(h_nkeys.data(), is.nkeys, ni8, cudaMemcpyDeviceToHost, s));
     HGB_CUDA(cudaStreamSynchronize(s));
     d2h += 2 * ni8 + ni4 + ni8;
-    const double wall = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+    const double wall = elapsed();
     res.assign(ninst, InstResult{});
     for (int k = 0; k < ninst; ++k) {
       InstResult& r = res[k];
-      r.status = status;
+      const int ist = (status == HORA_E_CANCELLED && !leadsto && t_fin[k] >= 0) ? HORA_OK : status;
+      r.status = ist;
       r.verdict = leadsto ? (h_found[k] ? 0 : 1) : (h_found[k] ? 1 : 0);
       r.st.explored = explored[k];
       r.st.expanded = explored[k];
@@ -538,10 +573,10 @@ struct Engine {
       r.st.pre_calls = pre_calls;
       r.st.gfp_iters = gfp_iters;
       r.st.kernel_launches = launches;
-      r.st.seconds = wall;
+      r.st.seconds = (ist == HORA_OK && t_fin[k] >= 0) ? t_fin[k] : wall;
       r.st.device_seconds = dev_ms * 1e-3;
       r.st.extrapolating = h_emode[k];
-      r.st.status = status;
+      r.st.status = ist;
       for (int q = 0; q < 6; ++q) { r.st.kernel_seconds[q] = kt.sec[q]; r.st.kernel_calls[q] = kt.calls[q]; }
       r.st.h2d_bytes = h2d;
       r.st.d2h_bytes = d2h;

@@ -303,30 +303,68 @@ DeviceNets::~DeviceNets() {
   if (ok) cudaFree(ok);
 }
 
+// The instance's device tables as one int32 blob (every array 16-byte aligned) and their offsets.
+void build_blob(const HostNet& H, std::vector<int32_t>& blob, std::vector<size_t>& offs) {
+  blob.clear();
+  offs.clear();
+  auto add = [&](const std::vector<int32_t>& v) {
+    while (blob.size() % 4) blob.push_back(0);
+    offs.push_back(blob.size());
+    blob.insert(blob.end(), v.begin(), v.end());
+    if (v.empty()) blob.push_back(0);
+  };
+  std::vector<int32_t> act32(H.act.size() * 2);
+  std::memcpy(act32.data(), H.act.data(), H.act.size() * 8);
+  const std::vector<int32_t>* arrs[] = {&H.chan_flags, &H.int_lo, &H.int_init, &H.proc_init, &H.loc_base,
+                                        &H.loc_flags, &H.loc_inv_off, &H.eloc_off, &H.eloc, &H.edge_tgt,
+                                        &H.edge_chan, &H.edge_dir, &H.edge_guard_off, &H.edge_iguard_off,
+                                        &H.edge_reset_off, &H.edge_iupd_off, &H.cons, &H.iatoms, &H.resets,
+                                        &H.iupds, &H.Lloc, &H.Uloc, &act32, &H.kshift, &H.kwidth, &H.L, &H.U,
+                                        &H.Lq, &H.Uq, &H.t_loc, &H.t_int, &H.t_clk, &H.av_loc, &H.av_int,
+                                        &H.p_loc, &H.p_int, &H.p_clk};
+  for (auto* a : arrs) add(*a);
+  while (blob.size() % 4) blob.push_back(0);
+}
+
+// The NetView of an instance whose blob lives at device address `b`.
+NetView make_view(const HostNet& H, const int32_t* b, const std::vector<size_t>& offs, int inst_shift) {
+  NetView V{};
+  size_t q = 0;
+  V.nclocks = H.nclocks; V.dim = H.dim; V.nprocs = H.nprocs; V.nints = H.nints; V.nchans = H.nchans;
+  V.nedges = H.nedges; V.nlocs = H.nlocs; V.has_urgent_chan = H.has_urgent_chan; V.kind = H.kind;
+  V.inst_shift = inst_shift;
+  V.chan_flags = b + offs[q++]; V.int_lo = b + offs[q++]; V.int_init = b + offs[q++]; V.proc_init = b + offs[q++];
+  V.loc_base = b + offs[q++]; V.loc_flags = b + offs[q++]; V.loc_inv_off = b + offs[q++];
+  V.eloc_off = b + offs[q++]; V.eloc = b + offs[q++]; V.edge_tgt = b + offs[q++]; V.edge_chan = b + offs[q++];
+  V.edge_dir = b + offs[q++]; V.edge_guard_off = b + offs[q++]; V.edge_iguard_off = b + offs[q++];
+  V.edge_reset_off = b + offs[q++]; V.edge_iupd_off = b + offs[q++]; V.cons = b + offs[q++];
+  V.iatoms = b + offs[q++]; V.resets = b + offs[q++]; V.iupds = b + offs[q++]; V.Lloc = b + offs[q++];
+  V.Uloc = b + offs[q++];
+  V.act = reinterpret_cast<const unsigned long long*>(b + offs[q++]);
+  V.kshift = b + offs[q++]; V.kwidth = b + offs[q++]; V.L = b + offs[q++]; V.U = b + offs[q++];
+  V.Lq = b + offs[q++]; V.Uq = b + offs[q++];
+  V.qmask = H.qmask;
+  V.t_never = H.t_never;
+  V.t_nloc = (int)H.t_loc.size() / 2; V.t_nint = (int)H.t_int.size() / 3; V.t_nclk = (int)H.t_clk.size() / 3;
+  V.t_loc = b + offs[q++]; V.t_int = b + offs[q++]; V.t_clk = b + offs[q++];
+  V.av_on = H.av_on; V.av_nclk = H.av_nclk;
+  V.av_nloc = (int)H.av_loc.size() / 2; V.av_nint = (int)H.av_int.size() / 3;
+  V.av_neg[0] = H.av_neg[0]; V.av_neg[1] = H.av_neg[1]; V.av_neg[2] = H.av_neg[2];
+  V.av_loc = b + offs[q++]; V.av_int = b + offs[q++];
+  V.p_nloc = (int)H.p_loc.size() / 2; V.p_nint = (int)H.p_int.size() / 3; V.p_nclk = (int)H.p_clk.size() / 3;
+  V.p_loc = b + offs[q++]; V.p_int = b + offs[q++]; V.p_clk = b + offs[q++];
+  return V;
+}
+
 int upload_nets(const std::vector<const HostNet*>& nets, int inst_shift, DeviceNets& out, std::string& err) {
   const int ninst = (int)nets.size();
   out.host_views.resize(ninst);
   std::vector<int> okv(ninst, 1);
+  std::vector<int32_t> blob;
+  std::vector<size_t> offs;
   for (int k = 0; k < ninst; ++k) {
     const HostNet& H = *nets[k];
-    std::vector<int32_t> blob;
-    std::vector<size_t> offs;
-    auto add = [&](const std::vector<int32_t>& v) {
-      while (blob.size() % 4) blob.push_back(0);   // 16-byte alignment for every array
-      offs.push_back(blob.size());
-      blob.insert(blob.end(), v.begin(), v.end());
-      if (v.empty()) blob.push_back(0);
-    };
-    std::vector<int32_t> act32(H.act.size() * 2);
-    std::memcpy(act32.data(), H.act.data(), H.act.size() * 8);
-    const std::vector<int32_t>* arrs[] = {&H.chan_flags, &H.int_lo, &H.int_init, &H.proc_init, &H.loc_base,
-                                          &H.loc_flags, &H.loc_inv_off, &H.eloc_off, &H.eloc, &H.edge_tgt,
-                                          &H.edge_chan, &H.edge_dir, &H.edge_guard_off, &H.edge_iguard_off,
-                                          &H.edge_reset_off, &H.edge_iupd_off, &H.cons, &H.iatoms, &H.resets,
-                                          &H.iupds, &H.Lloc, &H.Uloc, &act32, &H.kshift, &H.kwidth, &H.L, &H.U,
-                                          &H.Lq, &H.Uq, &H.t_loc, &H.t_int, &H.t_clk, &H.av_loc, &H.av_int,
-                                          &H.p_loc, &H.p_int, &H.p_clk};
-    for (auto* a : arrs) add(*a);
+    build_blob(H, blob, offs);
     void* d = nullptr;
     cudaError_t e = cudaMalloc(&d, blob.size() * 4);
     if (e != cudaSuccess) { err = std::string("CUDA: cudaMalloc: ") + cudaGetErrorString(e); return HORA_E_NOMEM; }
@@ -334,32 +372,7 @@ int upload_nets(const std::vector<const HostNet*>& nets, int inst_shift, DeviceN
     out.blob_bytes.push_back(blob.size() * 4);
     e = cudaMemcpy(d, blob.data(), blob.size() * 4, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) { err = std::string("CUDA: cudaMemcpy: ") + cudaGetErrorString(e); return HORA_E_CUDA; }
-    const int32_t* b = static_cast<const int32_t*>(d);
-    size_t q = 0;
-    NetView& V = out.host_views[k];
-    V.nclocks = H.nclocks; V.dim = H.dim; V.nprocs = H.nprocs; V.nints = H.nints; V.nchans = H.nchans;
-    V.nedges = H.nedges; V.nlocs = H.nlocs; V.has_urgent_chan = H.has_urgent_chan; V.kind = H.kind;
-    V.inst_shift = inst_shift;
-    V.chan_flags = b + offs[q++]; V.int_lo = b + offs[q++]; V.int_init = b + offs[q++]; V.proc_init = b + offs[q++];
-    V.loc_base = b + offs[q++]; V.loc_flags = b + offs[q++]; V.loc_inv_off = b + offs[q++];
-    V.eloc_off = b + offs[q++]; V.eloc = b + offs[q++]; V.edge_tgt = b + offs[q++]; V.edge_chan = b + offs[q++];
-    V.edge_dir = b + offs[q++]; V.edge_guard_off = b + offs[q++]; V.edge_iguard_off = b + offs[q++];
-    V.edge_reset_off = b + offs[q++]; V.edge_iupd_off = b + offs[q++]; V.cons = b + offs[q++];
-    V.iatoms = b + offs[q++]; V.resets = b + offs[q++]; V.iupds = b + offs[q++]; V.Lloc = b + offs[q++];
-    V.Uloc = b + offs[q++];
-    V.act = reinterpret_cast<const unsigned long long*>(b + offs[q++]);
-    V.kshift = b + offs[q++]; V.kwidth = b + offs[q++]; V.L = b + offs[q++]; V.U = b + offs[q++];
-    V.Lq = b + offs[q++]; V.Uq = b + offs[q++];
-    V.qmask = H.qmask;
-    V.t_never = H.t_never;
-    V.t_nloc = (int)H.t_loc.size() / 2; V.t_nint = (int)H.t_int.size() / 3; V.t_nclk = (int)H.t_clk.size() / 3;
-    V.t_loc = b + offs[q++]; V.t_int = b + offs[q++]; V.t_clk = b + offs[q++];
-    V.av_on = H.av_on; V.av_nclk = H.av_nclk;
-    V.av_nloc = (int)H.av_loc.size() / 2; V.av_nint = (int)H.av_int.size() / 3;
-    V.av_neg[0] = H.av_neg[0]; V.av_neg[1] = H.av_neg[1]; V.av_neg[2] = H.av_neg[2];
-    V.av_loc = b + offs[q++]; V.av_int = b + offs[q++];
-    V.p_nloc = (int)H.p_loc.size() / 2; V.p_nint = (int)H.p_int.size() / 3; V.p_nclk = (int)H.p_clk.size() / 3;
-    V.p_loc = b + offs[q++]; V.p_int = b + offs[q++]; V.p_clk = b + offs[q++];
+    out.host_views[k] = make_view(H, static_cast<const int32_t*>(d), offs, inst_shift);
   }
   cudaError_t e = cudaMalloc(&out.views, sizeof(NetView) * std::max(ninst, 1));
   if (e == cudaSuccess) e = cudaMemcpy(out.views, out.host_views.data(), sizeof(NetView) * ninst, cudaMemcpyHostToDevice);
@@ -405,6 +418,9 @@ static int dispatch_group(int dim, const std::vector<const HostNet*>& nets, std:
 using namespace hgb;
 
 static thread_local std::string g_last_error;
+namespace hgb {
+void set_last_error(const std::string& m) { g_last_error = m; }
+}  // namespace hgb
 
 static int32_t fail(int32_t rc, const std::string& msg) {
   g_last_error = msg;
@@ -520,7 +536,7 @@ int32_t hora_gb_has_deadlock(const hora_net_desc* net, int32_t n, const int32_t*
 }
 
 int32_t hora_gb_batch_run(int32_t n, const hora_net_desc* nets, const hora_query_desc* queries, int32_t* verdicts,
-                          hora_stats* stats) {
+                          hora_stats* stats, const volatile int32_t* cancel) {
   g_last_error.clear();
   if (n < 0 || (n > 0 && (!nets || !queries || !verdicts))) return fail(HORA_E_INVALID, "bad arguments");
   int rc = ensure_device();
@@ -539,23 +555,33 @@ int32_t hora_gb_batch_run(int32_t n, const hora_net_desc* nets, const hora_query
   }
   std::string err;
   int first_err = HORA_OK;
+  bool cancelled = false;
   for (auto& kv : by_dim) {
+    if (cancel && *cancel) {   // groups not yet started are not started
+      for (int k : kv.second)
+        if (stats) stats[k].status = HORA_E_CANCELLED;
+      cancelled = true;
+      continue;
+    }
     std::vector<const HostNet*> v;
     for (int k : kv.second) v.push_back(&H[k]);
     std::vector<InstResult> res;
     RunOptions o;
+    o.cancel = cancel;
     const int r = dispatch_group(kv.first / 2, v, res, o, err);
     for (size_t q = 0; q < kv.second.size(); ++q) {
       const int k = kv.second[q];
-      if (q < res.size()) {
-        if (stats) stats[k] = res[q].st;
-        verdicts[k] = r == HORA_OK ? res[q].verdict : -1;
-      }
-      if (stats && r) stats[k].status = r;
+      const int ist = q < res.size() ? res[q].status : (r ? r : HORA_E_CUDA);
+      if (q < res.size() && stats) stats[k] = res[q].st;
+      if (stats) stats[k].status = ist;
+      verdicts[k] = ist == HORA_OK ? res[q].verdict : -1;
+      cancelled |= ist == HORA_E_CANCELLED;
     }
+    if (r == HORA_E_CANCELLED) continue;
     if (r && !first_err) { first_err = r; g_last_error = err; }
   }
-  return first_err == HORA_E_CUDA ? HORA_E_CUDA : HORA_OK;
+  if (first_err == HORA_E_CUDA) return HORA_E_CUDA;
+  return cancelled ? HORA_E_CANCELLED : HORA_OK;
 }
 
 // ---- serving form: implemented in server.cu ----

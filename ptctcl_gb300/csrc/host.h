@@ -45,6 +45,8 @@ struct DeviceNets {
   ~DeviceNets();
 };
 int upload_nets(const std::vector<const HostNet*>& nets, int inst_shift, DeviceNets& out, std::string& err);
+void build_blob(const HostNet& H, std::vector<int32_t>& blob, std::vector<size_t>& offs);
+NetView make_view(const HostNet& H, const int32_t* device_blob, const std::vector<size_t>& offs, int inst_shift);
 
 // Result of one instance.
 struct InstResult {

@@ -38,7 +38,13 @@ struct Succ {                 // successors of the current level
   int* seg;                   // grouped survivors, one segment per touched slot
   int* sorted;                // the same segments in canonical order
   int* touched;               // touched slots
+  unsigned long long* okh;    // canonical order key of each successor: parent's hash key ...
+  unsigned long long* okl;    // ... then (parent's rank << 32) | emission ordinal
+  unsigned long long* skh;    // the same keys gathered at the successor's segment position
+  unsigned long long* skl;
   long long cap;
+  int* clist;                 // per touched key, its live zones gathered for the merge
+  long long ccap;
 };
 struct Front {                // one frontier
   unsigned long long* key;    // hash key

@@ -127,6 +127,8 @@ __global__ void __launch_bounds__(kBlock) k_expand(const NetView* nets, InstStat
           sc.key[idx] = key_encode(N, tl, ti) | ((unsigned long long)inst << N.inst_shift);
           sc.parent[idx] = (int)f;
           sc.ord[idx] = ord;
+          sc.okh[idx] = hk;
+          sc.okl[idx] = ((unsigned long long)(unsigned)fr.rank[f] << 32) | (unsigned)ord;
         }
       } else if (t.i == 0) {
         ctl->overflow = 1;
@@ -186,16 +188,25 @@ __global__ void __launch_bounds__(kBlock) k_probe(const NetView* nets, InstState
     bool killed = false;
     unsigned long long nprobe = 0;
     if (!inserted && mode == 0) {
-      for (int n = __ldg(st.head + slot); n >= 0; n = __ldg(st.nnext + n)) {
-        if (__ldg(st.ndead + n)) continue;
-        int zp[D];
-        load_rows(t, zp, st.nzone + (long long)n * D * D);
-        ++nprobe;
-        if (alu_le(t, z, zp, z0, Ly, U)) { killed = true; break; }
+      // the lanes take the stored zones of the chain in turn, each deciding a whole a_LU test
+      int Lall[D];
+#pragma unroll
+      for (int x = 0; x < D; ++x) Lall[x] = t.shfl(Ly, x);
+      const int* zs = sc.zone + s * D * D;
+      bool mine = false;
+      int pos = 0;
+      for (int n = __ldg(st.head + slot); n >= 0; n = __ldg(st.nnext + n), ++pos) {
+        const int lane_for = pos % D;
+        if (lane_for == t.i && !mine && !__ldg(st.ndead + n)) {
+          ++nprobe;
+          mine = alu_le_lane<D>(zs, st.nzone + (long long)n * D * D, Lall, U);
+        }
+        if (lane_for == D - 1 && t.any(mine)) break;
       }
+      killed = t.any(mine);
     }
+    if (nprobe) atomicAdd(&ctl->probes, nprobe);
     if (t.i == 0) {
-      if (nprobe) atomicAdd(&ctl->probes, nprobe);
       if (killed) {
         sc.slot[s] = -1;
       } else {
@@ -250,21 +261,16 @@ static __global__ void k_seg_scatter(Succ sc, Store st, long long nsucc) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nsucc; i += (long long)gridDim.x * blockDim.x) {
     const int s = sc.slot[i];
     if (s < 0) continue;
-    sc.seg[st.pend_base[s] + sc.rank[i]] = (int)i;
+    const unsigned pos = st.pend_base[s] + sc.rank[i];
+    sc.seg[pos] = (int)i;
+    sc.skh[pos] = sc.okh[i];
+    sc.skl[pos] = sc.okl[i];
   }
 }
 
 // ---------------------------------------------------------------------------------------------
 // merge: NetPassedT::add folds (passed_set.hpp:287-444) per key, in canonical order
 // ---------------------------------------------------------------------------------------------
-__device__ __forceinline__ bool order_less(const Front& fr, const Succ& sc, int a, int b) {
-  const int pa = sc.parent[a], pb = sc.parent[b];
-  const unsigned long long ka = fr.key[pa], kb = fr.key[pb];
-  if (ka != kb) return ka < kb;
-  const int ra = fr.rank[pa], rb = fr.rank[pb];
-  if (ra != rb) return ra < rb;
-  return sc.ord[a] < sc.ord[b];
-}
 
 template <int D>
 __global__ void __launch_bounds__(kBlock) k_merge(const NetView* nets, InstState is, Front fr, Succ sc, Store st,
@@ -273,6 +279,10 @@ __global__ void __launch_bounds__(kBlock) k_merge(const NetView* nets, InstState
   Tile<D> t;
   if (!make_tile(t, threadIdx.x & 31)) return;
   const int ishift = nets[0].inst_shift;
+  volatile int* vhead = st.head;
+  volatile int* vnext = st.nnext;
+  volatile int* vdead = st.ndead;
+  volatile int* vlevel = st.nlevel;
   for (long long j = tile_id<D>(); j < ntouched; j += tile_count<D>()) {
     const int s = sc.touched[j];
     const unsigned n = st.pend[s];
@@ -283,56 +293,88 @@ __global__ void __launch_bounds__(kBlock) k_merge(const NetView* nets, InstState
     const NetView& N = nets[inst];
     // canonical order: rank every pending survivor by (parent key, parent rank, ordinal)
     for (unsigned e = t.i; e < n; e += D) {
-      const int a = sc.seg[base + e];
+      const unsigned long long kh = sc.skh[base + e], kl = sc.skl[base + e];
       unsigned r = 0;
-      for (unsigned q = 0; q < n; ++q) r += order_less(fr, sc, sc.seg[base + q], a) ? 1u : 0u;
-      sc.sorted[base + r] = a;
+      for (unsigned q = 0; q < n; ++q) {
+        const unsigned long long qh = sc.skh[base + q], ql = sc.skl[base + q];
+        r += (qh < kh || (qh == kh && (ql < kl || (ql == kl && q < e)))) ? 1u : 0u;
+      }
+      sc.sorted[base + r] = sc.seg[base + e];
     }
+    // the key's live zones, gathered once into a contiguous list: oldest first, so that the zones
+    // this merge stores are appended and a backwards scan is the chain's newest-first order
+    long long cb = 0;
+    int clen = 0;
+    if (t.i == 0) {
+      int c = 0;
+      for (int m = vhead[s]; m >= 0; m = vnext[m]) c += vdead[m] ? 0 : 1;
+      cb = (long long)atomicAdd(&ctl->chain_alloc, (unsigned long long)(c + n));
+      if (cb + c + n > sc.ccap) { atomicMax(&ctl->err, 4u); cb = -1; }
+      else {
+        int k = c;
+        for (int m = vhead[s]; m >= 0; m = vnext[m])
+          if (!vdead[m]) sc.clist[cb + (--k)] = m;
+      }
+      clen = c;
+    }
+    cb = (long long)t.shfl64((unsigned long long)cb, 0);
+    clen = t.shfl(clen, 0);
     t.sync();
+    if (cb < 0) continue;
+    volatile int* cl = sc.clist + cb;
     int locs[kMaxProcs], ints[kMaxInts];
     key_decode(N, key_part(hk, ishift), locs, ints);
-    int Ly, U[D];
+    int Ly, U[D], Lall[D];
     key_bounds(N, t, locs, Ly, U);
+#pragma unroll
+    for (int x = 0; x < D; ++x) Lall[x] = t.shfl(Ly, x);
     long long dlive = 0;
     unsigned long long nprobe = 0;
+    // store z as a new node of this key and append it to the list
+    auto store_new = [&](const int (&z)[D]) -> int {
+      long long node = 0;
+      if (t.i == 0) node = (long long)atomicAdd(&ctl->nnodes, 1ull);
+      node = (long long)t.shfl64((unsigned long long)node, 0);
+      store_rows(t, z, st.nzone + node * D * D);
+      t.sync();
+      if (t.i == 0) {
+        const int old_head = vhead[s];
+        if (old_head < 0) { atomicAdd(&ctl->nkeys, 1ull); atomicAdd(&is.nkeys[inst], 1ull); }
+        st.nnext[node] = old_head;
+        st.nlevel[node] = level;
+        st.ndead[node] = 0;
+        st.ninst[node] = inst;
+        st.nkey[node] = hk;
+        cl[clen] = (int)node;
+        __threadfence_block();
+        vhead[s] = (int)node;
+      }
+      ++clen;
+      ++dlive;
+      t.sync();
+      return (int)node;
+    };
     for (unsigned q = 0; q < n; ++q) {
       const int a = ((volatile int*)sc.sorted)[base + q];
+      const int* zs = sc.zone + (long long)a * D * D;
       int z[D], z0[D];
-      load_rows(t, z, sc.zone + (long long)a * D * D);
+      load_rows(t, z, zs);
 #pragma unroll
       for (int x = 0; x < D; ++x) z0[x] = t.shfl(z[x], 0);
       if (mode == 1) {
-        // exact-zone graph: find the identical zone or store a new node, then record the edge
-        int hit = -1;
-        for (int m = ((volatile int*)st.head)[s]; m >= 0; m = ((volatile int*)st.nnext)[m]) {
-          int zp[D];
-          load_rows_rw(t, zp, st.nzone + (long long)m * D * D);
+        // exact-zone graph: the lanes compare the list's zones in turn; at most one can be equal
+        int mine = -1;
+        for (int k = t.i; k < clen; k += D) {
+          const int m = cl[k];
+          const int* zp = st.nzone + (long long)m * D * D;
           bool eq = true;
+          for (int e = 0; e < D * D && eq; ++e) eq = __ldcg(zp + e) == __ldg(zs + e);
+          if (eq) { mine = m; break; }
+        }
+        int hit = -1;
 #pragma unroll
-          for (int j = 0; j < D; ++j) eq &= zp[j] == z[j];
-          if (t.all(eq)) { hit = m; break; }
-        }
-        if (hit < 0) {
-          long long node = 0;
-          if (t.i == 0) node = (long long)atomicAdd(&ctl->nnodes, 1ull);
-          node = (long long)t.shfl64((unsigned long long)node, 0);
-          store_rows(t, z, st.nzone + node * D * D);
-          t.sync();
-          if (t.i == 0) {
-            const int old_head = ((volatile int*)st.head)[s];
-            if (old_head < 0) { atomicAdd(&ctl->nkeys, 1ull); atomicAdd(&is.nkeys[inst], 1ull); }
-            st.nnext[node] = old_head;
-            st.nlevel[node] = level;
-            st.ndead[node] = 0;
-            st.ninst[node] = inst;
-            st.nkey[node] = hk;
-            __threadfence_block();
-            ((volatile int*)st.head)[s] = (int)node;
-          }
-          ++dlive;
-          hit = (int)node;
-          t.sync();
-        }
+        for (int l = 0; l < D; ++l) { const int v = t.shfl(mine, l); hit = v >= 0 ? v : hit; }
+        if (hit < 0) hit = store_new(z);
         if (record && t.i == 0) {
           const unsigned long long e = atomicAdd(&ctl->nedges, 1ull);
           if ((long long)e < ed.cap) { ed.src[e] = fr.node[sc.parent[a]]; ed.dst[e] = hit; }
@@ -340,42 +382,49 @@ __global__ void __launch_bounds__(kBlock) k_merge(const NetView* nets, InstState
         }
         continue;
       }
-      // (1)+(2): dropped if a stored zone simulates it
+      // (1)+(2): dropped if a stored zone simulates it. Every zone stored before this level was
+      // already tested by the probe, and a stored zone is only ever retired by one that simulates
+      // it, so only the zones stored at this level -- the list's tail -- can still drop it.
       bool drop = false;
-      for (int m = ((volatile int*)st.head)[s]; m >= 0; m = ((volatile int*)st.nnext)[m]) {
-        if (((volatile int*)st.ndead)[m]) continue;
+      for (int k = clen - 1; k >= 0; --k) {
+        const int m = cl[k];
+        if (m < 0) continue;
+        if (vlevel[m] != level) break;
         int zp[D];
         load_rows_rw(t, zp, st.nzone + (long long)m * D * D);
         ++nprobe;
         if (alu_le(t, z, zp, z0, Ly, U)) { drop = true; break; }
       }
       if (drop) continue;
-      // (3): retire stored zones the new one simulates
-      for (int m = ((volatile int*)st.head)[s]; m >= 0; m = ((volatile int*)st.nnext)[m]) {
-        if (((volatile int*)st.ndead)[m]) continue;
-        int zp[D], zp0[D];
-        load_rows_rw(t, zp, st.nzone + (long long)m * D * D);
-#pragma unroll
-        for (int x = 0; x < D; ++x) zp0[x] = t.shfl(zp[x], 0);
-        if (alu_le(t, zp, z, zp0, Ly, U)) {
-          t.sync();
-          if (t.i == 0) ((volatile int*)st.ndead)[m] = 1;
-          --dlive;
-          t.sync();
+      // (3): retire the stored zones the new one simulates; the lanes take the list in turn
+      {
+        int retired = 0;
+        for (int k = t.i; k < clen; k += D) {
+          const int m = cl[k];
+          if (m < 0) continue;
+          if (alu_le_lane<D>(st.nzone + (long long)m * D * D, zs, Lall, U)) {
+            vdead[m] = 1;
+            cl[k] = -1;
+            ++retired;
+          }
         }
+        t.sync();
+#pragma unroll
+        for (int l = 0; l < D; ++l) dlive -= t.shfl(retired, l);
       }
       // (4): convex-union absorb within the newest kMergeScan live zones, restarting after each
       for (bool merged = true; merged;) {
         merged = false;
         int seen = 0;
-        for (int m = ((volatile int*)st.head)[s]; m >= 0 && seen < kMergeScan; m = ((volatile int*)st.nnext)[m]) {
-          if (((volatile int*)st.ndead)[m]) continue;
+        for (int k = clen - 1; k >= 0 && seen < kMergeScan; --k) {
+          const int m = cl[k];
+          if (m < 0) continue;
           ++seen;
           int zp[D];
           load_rows_rw(t, zp, st.nzone + (long long)m * D * D);
           if (try_union(t, z, zp)) {
             t.sync();
-            if (t.i == 0) ((volatile int*)st.ndead)[m] = 1;
+            if (t.i == 0) { vdead[m] = 1; cl[k] = -1; }
             --dlive;
             t.sync();
             merged = true;
@@ -384,30 +433,14 @@ __global__ void __launch_bounds__(kBlock) k_merge(const NetView* nets, InstState
         }
       }
       // (5): prepend
-      long long node = 0;
-      if (t.i == 0) node = (long long)atomicAdd(&ctl->nnodes, 1ull);
-      node = (long long)t.shfl64((unsigned long long)node, 0);
-      store_rows(t, z, st.nzone + node * D * D);
-      t.sync();
-      if (t.i == 0) {
-        const int old_head = ((volatile int*)st.head)[s];
-        if (old_head < 0) { atomicAdd(&ctl->nkeys, 1ull); atomicAdd(&is.nkeys[inst], 1ull); }
-        st.nnext[node] = old_head;
-        st.nlevel[node] = level;
-        st.ndead[node] = 0;
-        st.ninst[node] = inst;
-        st.nkey[node] = hk;
-        __threadfence_block();
-        ((volatile int*)st.head)[s] = (int)node;
-      }
-      ++dlive;
-      t.sync();
+      store_new(z);
     }
     // this key's zones stored at this level enter the next frontier, in chain order
     if (t.i == 0) {
       int r = 0;
-      for (int m = ((volatile int*)st.head)[s]; m >= 0; m = ((volatile int*)st.nnext)[m]) {
-        if (((volatile int*)st.ndead)[m] || ((volatile int*)st.nlevel)[m] != level) continue;
+      for (int k = clen - 1; k >= 0; --k) {
+        const int m = cl[k];
+        if (m < 0 || vlevel[m] != level) continue;
         const unsigned long long f = atomicAdd(&ctl->nfront, 1ull);
         out.key[f] = hk; out.node[f] = m; out.rank[f] = r++; out.inst[f] = inst;
       }
@@ -416,9 +449,9 @@ __global__ void __launch_bounds__(kBlock) k_merge(const NetView* nets, InstState
         atomicAdd((unsigned long long*)&ctl->nlive, (unsigned long long)dlive);
         atomicAdd((unsigned long long*)&is.nlive[inst], (unsigned long long)dlive);
       }
-      if (nprobe) atomicAdd(&ctl->probes, nprobe);
       st.pend[s] = 0;
     }
+    if (nprobe) atomicAdd(&ctl->probes, nprobe);
     t.sync();
   }
 }
@@ -439,7 +472,8 @@ static __global__ void k_collect_p(const NetView* nets, Store st, long long nnod
     key_decode(N, key_part(hk, ishift), locs, ints);
     if (!pred_disc(N.p_loc, N.p_nloc, N.p_int, N.p_nint, locs, ints)) continue;
     const unsigned long long f = atomicAdd(&ctl->nfront, 1ull);
-    out.key[f] = hk; out.node[f] = (int)n; out.rank[f] = 0; out.inst[f] = inst;
+    // the node id as rank keeps the order keys of one key's roots distinct
+    out.key[f] = hk; out.node[f] = (int)n; out.rank[f] = (int)n; out.inst[f] = inst;
   }
 }
 

@@ -1,13 +1,17 @@
-// server.cu -- the serving form of the C ABI: a request queue drained into device batches.
+// server.cu -- the serving form of the C ABI: continuous admission of verification requests.
 //
-// Requests are copied at submit time (the caller's descriptor arrays may be freed afterwards).
-// Each hora_gb_server_step() admits queued requests in arrival order while their estimated
-// passed/waiting-store footprint fits the budget and the in-flight limit allows, runs the admitted
-// set as one batched level-synchronous search per DBM dimension, and publishes the results.
+// Requests are copied at submit time (the caller's descriptor arrays may be freed afterwards) and
+// admitted in arrival order while their estimated passed/waiting-store footprint fits the
+// device-memory budget and the in-flight limit allows. Admitted requests run as batched
+// level-synchronous searches on worker threads, each on its own CUDA stream, so requests admitted
+// while others are running overlap with them on the device.
 #include <cuda_runtime.h>
 
+#include <chrono>
+#include <condition_variable>
 #include <cstring>
 #include <deque>
+#include <thread>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -69,17 +73,29 @@ struct Request {
   int done = 0;
   int verdict = -1;
   hora_stats st{};
+  std::chrono::steady_clock::time_point t_submit;
 };
 
 }  // namespace hgb
 
+// The serving loop: worker threads, each of which repeatedly takes every queued request that still
+// fits the device-memory budget (up to its share of the in-flight limit), runs them together as one
+// batch on its own CUDA stream, and publishes the results. Several workers keep several batches on
+// the device at once, so a request that arrives while others are running starts as soon as a worker
+// and budget are free instead of waiting for the running batches to end.
 struct hora_server {
   uint64_t budget = 0;
+  uint64_t in_use = 0;                 // estimated bytes of the requests on the device
   int max_inflight = 0;
+  int inflight = 0;
   int64_t next_ticket = 1;
   std::deque<std::unique_ptr<hgb::Request>> queue;
   std::map<int64_t, std::unique_ptr<hgb::Request>> finished;
   std::mutex mu;
+  std::condition_variable cv;
+  bool stop = false;
+  std::vector<std::thread> workers;
+  int device = 0;
 };
 
 using namespace hgb;
@@ -90,13 +106,66 @@ static uint64_t estimate_bytes(const hora_net_desc* n) {
   return (1ull << 16) * (d * d * 4 + 32);
 }
 
+static void worker_main(hora_server* s, int per_batch) {
+  cudaSetDevice(s->device);
+  for (;;) {
+    std::vector<std::unique_ptr<Request>> batch;
+    {
+      std::unique_lock<std::mutex> g(s->mu);
+      s->cv.wait(g, [&] {
+        return s->stop || (!s->queue.empty() && s->inflight < s->max_inflight &&
+                           s->in_use + s->queue.front()->est_bytes <= s->budget);
+      });
+      if (s->stop) return;
+      while (!s->queue.empty() && (int)batch.size() < per_batch && s->inflight < s->max_inflight &&
+             s->in_use + s->queue.front()->est_bytes <= s->budget) {
+        s->in_use += s->queue.front()->est_bytes;
+        ++s->inflight;
+        batch.push_back(std::move(s->queue.front()));
+        s->queue.pop_front();
+      }
+    }
+    std::vector<hora_net_desc> nets;
+    std::vector<hora_query_desc> qs;
+    for (auto& r : batch) { nets.push_back(r->net.d); qs.push_back(r->net.q); }
+    std::vector<int32_t> verdicts(batch.size());
+    std::vector<hora_stats> st(batch.size());
+    const int rc = hora_gb_batch_run((int32_t)batch.size(), nets.data(), qs.data(), verdicts.data(), st.data(),
+                                     nullptr);
+    const auto now = std::chrono::steady_clock::now();
+    {
+      std::lock_guard<std::mutex> g(s->mu);
+      for (size_t k = 0; k < batch.size(); ++k) {
+        Request& r = *batch[k];
+        r.done = 1;
+        r.verdict = rc == HORA_OK ? verdicts[k] : -1;
+        r.st = st[k];
+        if (rc) r.st.status = rc;
+        // time to verdict: submission to publication
+        r.st.seconds = std::chrono::duration<double>(now - r.t_submit).count();
+        s->in_use -= r.est_bytes;
+        --s->inflight;
+        const int64_t t = r.ticket;
+        s->finished[t] = std::move(batch[k]);
+      }
+    }
+    s->cv.notify_all();
+  }
+}
+
 extern "C" {
 
 int32_t hora_gb_server_create(uint64_t budget_bytes, int32_t max_inflight, hora_server** out) {
   if (!out || max_inflight <= 0) return HORA_E_INVALID;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) return HORA_E_NO_DEVICE;
   hora_server* s = new hora_server;
   s->budget = budget_bytes;
   s->max_inflight = max_inflight;
+  cudaGetDevice(&s->device);
+  const int nworkers = std::min(8, max_inflight);
+  const int per_batch = (max_inflight + nworkers - 1) / nworkers;
+  for (int w = 0; w < nworkers; ++w) s->workers.emplace_back(worker_main, s, per_batch);
   *out = s;
   return HORA_OK;
 }
@@ -108,47 +177,23 @@ int32_t hora_gb_server_submit(hora_server* s, const hora_net_desc* net, const ho
   auto r = std::make_unique<Request>();
   r->net.copy(net, q);
   r->est_bytes = est;
-  std::lock_guard<std::mutex> g(s->mu);
-  r->ticket = s->next_ticket++;
-  *ticket = r->ticket;
-  s->queue.push_back(std::move(r));
+  r->t_submit = std::chrono::steady_clock::now();
+  {
+    std::lock_guard<std::mutex> g(s->mu);
+    r->ticket = s->next_ticket++;
+    *ticket = r->ticket;
+    s->queue.push_back(std::move(r));
+  }
+  s->cv.notify_all();
   return HORA_OK;
 }
 
 int32_t hora_gb_server_step(hora_server* s, int32_t* active) {
   if (!s) return HORA_E_INVALID;
-  std::vector<std::unique_ptr<Request>> batch;
-  {
-    std::lock_guard<std::mutex> g(s->mu);
-    uint64_t used = 0;
-    while (!s->queue.empty() && (int)batch.size() < s->max_inflight &&
-           used + s->queue.front()->est_bytes <= s->budget) {
-      used += s->queue.front()->est_bytes;
-      batch.push_back(std::move(s->queue.front()));
-      s->queue.pop_front();
-    }
-  }
-  if (!batch.empty()) {
-    std::vector<hora_net_desc> nets;
-    std::vector<hora_query_desc> qs;
-    for (auto& r : batch) { nets.push_back(r->net.d); qs.push_back(r->net.q); }
-    std::vector<int32_t> verdicts(batch.size());
-    std::vector<hora_stats> st(batch.size());
-    const int rc = hora_gb_batch_run((int32_t)batch.size(), nets.data(), qs.data(), verdicts.data(), st.data());
-    std::lock_guard<std::mutex> g(s->mu);
-    for (size_t k = 0; k < batch.size(); ++k) {
-      batch[k]->done = 1;
-      batch[k]->verdict = rc == HORA_OK ? verdicts[k] : -1;
-      batch[k]->st = st[k];
-      if (rc) batch[k]->st.status = rc;
-      const int64_t t = batch[k]->ticket;
-      s->finished[t] = std::move(batch[k]);
-    }
-  }
-  if (active) {
-    std::lock_guard<std::mutex> g(s->mu);
-    *active = (int32_t)s->queue.size();
-  }
+  std::unique_lock<std::mutex> g(s->mu);
+  // wait briefly for progress so that a polling caller does not spin
+  s->cv.wait_for(g, std::chrono::milliseconds(1));
+  if (active) *active = (int32_t)s->queue.size() + s->inflight;
   return HORA_OK;
 }
 
@@ -164,6 +209,13 @@ int32_t hora_gb_server_poll(hora_server* s, int64_t ticket, int32_t* done, int32
 }
 
 int32_t hora_gb_server_destroy(hora_server* s) {
+  if (!s) return HORA_E_INVALID;
+  {
+    std::lock_guard<std::mutex> g(s->mu);
+    s->stop = true;
+  }
+  s->cv.notify_all();
+  for (auto& t : s->workers) t.join();
   delete s;
   return HORA_OK;
 }

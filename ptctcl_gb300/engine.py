@@ -164,8 +164,11 @@ def has_deadlock(net: Network, locs, ints, zones) -> np.ndarray:
     return out.astype(bool)
 
 
-def batch_run(items: Sequence[Tuple[Network, int, Pred, Pred]]):
-    """Run (network, kind, p, q) instances together; returns (verdicts, [stats dict])."""
+def batch_run(items: Sequence[Tuple[Network, int, Pred, Pred]], cancel: Optional[ctypes.c_int32] = None):
+    """Run (network, kind, p, q) instances together; returns (verdicts, [stats dict]).
+
+    cancel: a ctypes.c_int32 another thread may set to 1; instances without a verdict by then come
+    back with verdict -1 and stats status E_CANCELLED (no exception is raised for that)."""
     lib = capi.load()
     n = len(items)
     nas = [NetArrays(it[0]) for it in items]
@@ -175,6 +178,56 @@ def batch_run(items: Sequence[Tuple[Network, int, Pred, Pred]]):
     verdicts = np.zeros(max(n, 1), np.int32)
     stats = (Stats * max(n, 1))()
     rc = lib.hora_gb_batch_run(n, ctypes.addressof(nets), ctypes.addressof(qs), capi.p32(verdicts),
-                               ctypes.addressof(stats))
-    capi.check(rc, "batch_run")
+                               ctypes.addressof(stats), ctypes.addressof(cancel) if cancel is not None else None)
+    if rc != capi.E_CANCELLED:
+        capi.check(rc, "batch_run")
     return verdicts[:n].tolist(), [stats[k].as_dict() for k in range(n)]
+
+
+class Server:
+    """The serving form (hora_gb_server_*): requests are queued, admitted while their estimated
+    store footprint fits `budget_bytes` and at most `max_inflight` run at once, and run on the
+    device in batches by background workers; `poll` returns (verdict, stats dict) once a ticket is
+    done, else None."""
+
+    def __init__(self, budget_bytes: int, max_inflight: int):
+        self._lib = capi.load()
+        self._h = ctypes.c_void_p()
+        capi.check(self._lib.hora_gb_server_create(int(budget_bytes), int(max_inflight), ctypes.byref(self._h)),
+                   "server_create")
+
+    def submit(self, net: Network, kind: int, p: Pred, q: Optional[Pred] = None) -> int:
+        na, qa = NetArrays(net), QueryArrays(kind, p, q)
+        t = ctypes.c_int64(0)
+        capi.check(self._lib.hora_gb_server_submit(self._h, ctypes.addressof(na.desc), ctypes.addressof(qa.desc),
+                                                   ctypes.byref(t)), "server_submit")
+        return t.value   # the descriptors were copied: na/qa may go
+
+    def active(self) -> int:
+        a = ctypes.c_int32(0)
+        capi.check(self._lib.hora_gb_server_step(self._h, ctypes.byref(a)), "server_step")
+        return a.value
+
+    def poll(self, ticket: int):
+        d, v, st = ctypes.c_int32(0), ctypes.c_int32(0), Stats()
+        capi.check(self._lib.hora_gb_server_poll(self._h, ticket, ctypes.byref(d), ctypes.byref(v),
+                                                 ctypes.byref(st)), "server_poll")
+        return (v.value, st.as_dict()) if d.value else None
+
+    def drain(self, timeout: float = 600.0):
+        import time
+        t0 = time.perf_counter()
+        while self.active() > 0:
+            if time.perf_counter() - t0 > timeout:
+                raise TimeoutError("server did not drain")
+
+    def close(self):
+        if self._h:
+            capi.check(self._lib.hora_gb_server_destroy(self._h), "server_destroy")
+            self._h = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

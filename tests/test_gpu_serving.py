@@ -1,0 +1,63 @@
+"""The batched and serving forms on the GPU: every request's verdict and counts are the same
+whether it runs alone, in a batch, or through the request queue mixed with other requests; a
+cancelled batch reports its unfinished instances as cancelled; the queue rejects a request whose
+store estimate exceeds the whole memory budget."""
+import ctypes
+
+import pytest
+
+from ptctcl_gb300 import capi, engine
+from ptctcl_gb300.generator import config_instance
+from test_gpu_parity import C4_SMALL, small_config3
+
+pytestmark = pytest.mark.gpu
+
+COUNTS = ("explored", "generated", "stored", "keys", "levels")
+
+
+def _mix():
+    items = [config_instance(4, s) for s in C4_SMALL]
+    for seed in (0, 1, 3):
+        items.append(small_config3(seed))
+    return items
+
+
+def test_server_matches_alone_and_batch():
+    items = _mix()
+    alone = [engine.batch_run([it]) for it in items]
+    bv, bst = engine.batch_run(items)
+    with engine.Server(budget_bytes=8 << 30, max_inflight=8) as srv:
+        tickets = [srv.submit(*it) for it in items]
+        srv.drain(timeout=600)
+        got = [srv.poll(t) for t in tickets]
+    for k, (it, (av, ast), g) in enumerate(zip(items, alone, got)):
+        assert g is not None, k
+        v, st = g
+        assert st["status"] == capi.OK, (k, st["status"])
+        assert v == av[0] == bv[k], (k, v, av[0], bv[k])
+        for c in COUNTS:
+            assert st[c] == ast[0][c] == bst[k][c], (k, c, st[c], ast[0][c], bst[k][c])
+
+
+def test_batch_cancelled_before_start():
+    items = [config_instance(4, s) for s in C4_SMALL[:4]]
+    cancel = ctypes.c_int32(1)
+    verdicts, stats = engine.batch_run(items, cancel=cancel)
+    assert verdicts == [-1] * len(items)
+    assert all(s["status"] == capi.E_CANCELLED for s in stats)
+
+
+def test_batch_time_to_verdict_within_run():
+    items = [config_instance(4, s) for s in C4_SMALL]
+    _, stats = engine.batch_run(items)
+    for s in stats:
+        assert s["status"] == capi.OK
+        assert 0.0 <= s["seconds"] <= stats[0]["device_seconds"] + 60.0
+
+
+def test_server_rejects_over_budget():
+    net, kind, p, q = config_instance(4, C4_SMALL[0])
+    with engine.Server(budget_bytes=1024, max_inflight=2) as srv:
+        with pytest.raises(capi.HoraError) as ei:
+            srv.submit(net, kind, p, q)
+        assert ei.value.code == capi.E_BUDGET
