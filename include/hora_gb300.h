@@ -204,6 +204,20 @@ HORA_GB_API int32_t hora_gb_expand(const hora_net_desc* net, int32_t n, const in
 HORA_GB_API int32_t hora_gb_has_deadlock(const hora_net_desc* net, int32_t n, const int32_t* locs,
                              const int32_t* ints, const int32_t* zones, int32_t* out);
 
+/* Deadlock predicate for callers that cannot allocate device memory. No counterpart in the
+ * reference: it exists for callers whose device memory is owned by another allocator (a framework
+ * pool that reserved the device) or who cannot take cudaMalloc/cudaFree's implicit synchronisation.
+ * The caller passes DEVICE buffers: d_locs[n*nprocs], d_ints[n*nints] (may be null when nints is
+ * 0), d_zones[n*dim*dim] and d_out[n]; the call allocates nothing. The compiled network lives in
+ * one static device array of 1 MiB (held by every GPU that loads the library until exit); a
+ * network whose tables do not fit is rejected with HORA_E_INVALID. The array's device address is
+ * fetched on the first call on each device, which should therefore come before any stream capture.
+ * The array is shared by all calls and keeps the last call's contents (its counters are cleared on
+ * every call): calls that overlap on the GPU race. Runs on the legacy default stream and returns
+ * after the kernel has finished. */
+HORA_GB_API int32_t hora_gb_has_deadlock_noalloc(const hora_net_desc* net, int32_t n, const int32_t* d_locs,
+                                                 const int32_t* d_ints, const int32_t* d_zones, int32_t* d_out);
+
 /* ---- batched form ----------------------------------------------------------------------------- */
 
 /* Run n independent (network, query) instances together on the device. verdicts[k] receives the

@@ -18,7 +18,7 @@ EXPORTS = (
     "hora_gb_last_error", "hora_gb_abi_version", "hora_gb_device_count", "hora_gb_reachable_net",
     "hora_gb_deadlock_reachable", "hora_gb_leads_to", "hora_gb_expand", "hora_gb_has_deadlock",
     "hora_gb_batch_run", "hora_gb_server_create", "hora_gb_server_submit", "hora_gb_server_step",
-    "hora_gb_server_poll", "hora_gb_server_destroy",
+    "hora_gb_server_poll", "hora_gb_server_destroy", "hora_gb_has_deadlock_noalloc",
 )
 
 _lib = None
@@ -58,6 +58,8 @@ def load(build_if_missing: bool = True):
     L.hora_gb_expand.restype = I32
     L.hora_gb_has_deadlock.argtypes = [VP, I32, P32, P32, P32, P32]
     L.hora_gb_has_deadlock.restype = I32
+    L.hora_gb_has_deadlock_noalloc.argtypes = [VP, I32, VP, VP, VP, VP]
+    L.hora_gb_has_deadlock_noalloc.restype = I32
     L.hora_gb_batch_run.argtypes = [I32, VP, VP, P32, VP, VP]
     L.hora_gb_batch_run.restype = I32
     L.hora_gb_server_create.argtypes = [U64, I32, ctypes.POINTER(VP)]

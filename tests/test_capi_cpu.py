@@ -24,7 +24,7 @@ def declared_symbols():
 def test_library_exports_every_declared_symbol():
     lib = capi.load()
     syms = declared_symbols()
-    assert syms >= set(capi.EXPORTS) - {"hora_gb_run_no_alloc"}
+    assert syms >= set(capi.EXPORTS)
     for s in syms:
         assert hasattr(lib, s), s
     assert lib.hora_gb_abi_version() == 1
