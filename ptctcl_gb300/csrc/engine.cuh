@@ -73,6 +73,10 @@ struct Ctl {
   unsigned long long seg_alloc;  // grouping segment allocator
   unsigned long long nfront;     // next-frontier entries
   unsigned long long chain_alloc;  // merge's chain-list allocator
+  unsigned long long nheavy;     // touched keys merged block-wide ...
+  unsigned long long nlight;     // ... and by one tile
+  unsigned long long heavy_next; // merge work counters
+  unsigned long long light_next;
   unsigned int found;            // some instance hit its goal this level
   unsigned int overflow;         // expand output overflowed
   // cumulative
@@ -85,6 +89,6 @@ struct Ctl {
   unsigned int err;              // HORA_E_* raised on the device (table full, escape overflow)
   unsigned int flag;             // set by a fixpoint pass that changed something
 };
-constexpr unsigned long long kCtlLevelBytes = 6 * 8 + 2 * 4;
+constexpr unsigned long long kCtlLevelBytes = 10 * 8 + 2 * 4;
 
 }  // namespace hgb

@@ -52,8 +52,9 @@ struct DBuf {
   template <class T> T* as() const { return static_cast<T*>(p); }
 };
 
-static __global__ void k_rehash(const unsigned long long* okey, const int* ohead, unsigned long long ocap,
-                                unsigned long long* nkey, int* nhead, unsigned long long nmask, unsigned* err) {
+static __global__ void k_rehash(const unsigned long long* okey, const int* ohead, const int* olive,
+                                unsigned long long ocap, unsigned long long* nkey, int* nhead, int* nlive,
+                                unsigned long long nmask, unsigned* err) {
   for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < ocap;
        i += (unsigned long long)gridDim.x * blockDim.x) {
     const unsigned long long k = okey[i];
@@ -61,7 +62,7 @@ static __global__ void k_rehash(const unsigned long long* okey, const int* ohead
     unsigned long long h = hash_mix(k) & nmask;
     unsigned long long probe = 0;
     for (; probe <= nmask; ++probe) {
-      if (atomicCAS(&nkey[h], kEmptyKey, k) == kEmptyKey) { nhead[h] = ohead[i]; break; }
+      if (atomicCAS(&nkey[h], kEmptyKey, k) == kEmptyKey) { nhead[h] = ohead[i]; nlive[h] = olive[i]; break; }
       h = (h + 1) & nmask;
     }
     if (probe > nmask) atomicMax(err, 4u);
@@ -99,7 +100,7 @@ enum { KT_EXPAND = 0, KT_PROBE = 1, KT_DEADLOCK = 2, KT_GROUP = 3, KT_MERGE = 4,
 
 template <int D>
 struct StoreBufs {
-  DBuf hkey, head, pend, pend_base;           // hash table
+  DBuf hkey, head, pend, pend_base, klive;    // hash table
   DBuf nzone, nnext, nlevel, ndead, ninst, nkey;  // nodes
   unsigned long long hcap = 0;
   long long ncap = 0;
@@ -119,7 +120,8 @@ struct Engine {
   int blocks = 0;
   DeviceNets dn;
   StoreBufs<D> S[2];
-  DBuf skey, sparent, sord, sslot, srank, szone, ssurv, sseg, ssorted, stouched, sokh, sokl, sskh, sskl;
+  DBuf skey, sparent, sord, sslot, srank, szone, ssurv, sseg, ssorted, stouched, sokh, sokl, sskh, sskl, sheavy,
+      slight;
   long long scap = 0;
   DBuf clist;
   long long ccap = 0;
@@ -127,6 +129,9 @@ struct Engine {
   long long fcapb[2] = {0, 0};
   DBuf esrc, edst;
   long long ecap = 0;
+  int merge_blocks = 0;         // resident blocks of the merge kernel (it schedules keys itself)
+  DBuf zw;                      // exact-zone table of the graph store
+  unsigned long long zcap = 0;
   DBuf ctl, emode, done, found, generated, gen_backup, nlive, nkeys, nfront, probes;
   Ctl hctl{};
   KTimer kt;
@@ -151,6 +156,7 @@ struct Engine {
     Store st;
     st.hkey = B.hkey.template as<unsigned long long>(); st.head = B.head.template as<int>();
     st.pend = B.pend.template as<unsigned>(); st.pend_base = B.pend_base.template as<unsigned>();
+    st.klive = B.klive.template as<int>();
     st.hmask = B.hcap - 1;
     st.nzone = B.nzone.template as<int>(); st.nnext = B.nnext.template as<int>();
     st.nlevel = B.nlevel.template as<int>(); st.ndead = B.ndead.template as<int>(); st.ninst = B.ninst.template as<int>();
@@ -164,6 +170,7 @@ struct Engine {
     sc.zone = szone.template as<int>(); sc.surv = ssurv.template as<int>(); sc.seg = sseg.template as<int>();
     sc.sorted = ssorted.template as<int>(); sc.touched = stouched.template as<int>(); sc.cap = scap;
     sc.okh = sokh.template as<unsigned long long>(); sc.okl = sokl.template as<unsigned long long>();
+    sc.heavy = sheavy.template as<int>(); sc.light = slight.template as<int>();
     sc.skh = sskh.template as<unsigned long long>(); sc.skl = sskl.template as<unsigned long long>();
     sc.clist = clist.template as<int>(); sc.ccap = ccap;
     return sc;
@@ -175,6 +182,7 @@ struct Engine {
     return f;
   }
   Edges edges() { return Edges{esrc.template as<int>(), edst.template as<int>(), ecap}; }
+  ZTab ztab() { return ZTab{zw.template as<unsigned long long>(), zcap - 1}; }
   InstState istate() {
     InstState is;
     is.emode = emode.template as<int>(); is.done = done.template as<int>(); is.found = found.template as<unsigned>();
@@ -197,7 +205,8 @@ struct Engine {
     B.hcap = hcap;
     B.ncap = ncap;
     HGB_CUDA(B.hkey.alloc(hcap * 8)); HGB_CUDA(B.head.alloc(hcap * 4)); HGB_CUDA(B.pend.alloc(hcap * 4));
-    HGB_CUDA(B.pend_base.alloc(hcap * 4));
+    HGB_CUDA(B.pend_base.alloc(hcap * 4)); HGB_CUDA(B.klive.alloc(hcap * 4));
+    HGB_CUDA(cudaMemsetAsync(B.klive.p, 0, hcap * 4, s));
     HGB_CUDA(cudaMemsetAsync(B.hkey.p, 0xff, hcap * 8, s));
     HGB_CUDA(cudaMemsetAsync(B.head.p, 0xff, hcap * 4, s));
     HGB_CUDA(cudaMemsetAsync(B.pend.p, 0, hcap * 4, s));
@@ -212,6 +221,7 @@ struct Engine {
     HGB_CUDA(ssurv.alloc(cap * 4)); HGB_CUDA(sseg.alloc(cap * 4)); HGB_CUDA(ssorted.alloc(cap * 4));
     HGB_CUDA(stouched.alloc(cap * 4));
     HGB_CUDA(sokh.alloc(cap * 8)); HGB_CUDA(sokl.alloc(cap * 8));
+    HGB_CUDA(sheavy.alloc(cap * 4)); HGB_CUDA(slight.alloc(cap * 4));
     HGB_CUDA(sskh.alloc(cap * 8)); HGB_CUDA(sskl.alloc(cap * 8));
     return HORA_OK;
   }
@@ -227,14 +237,17 @@ struct Engine {
     if ((hctl.nslots + extra) * 2 <= B.hcap) return HORA_OK;
     unsigned long long ncap = B.hcap;
     while ((hctl.nslots + extra) * 2 > ncap) ncap <<= 1;
-    DBuf k2, h2, p2, pb2;
+    DBuf k2, h2, p2, pb2, l2;
     HGB_CUDA(k2.alloc(ncap * 8)); HGB_CUDA(h2.alloc(ncap * 4)); HGB_CUDA(p2.alloc(ncap * 4)); HGB_CUDA(pb2.alloc(ncap * 4));
+    HGB_CUDA(l2.alloc(ncap * 4));
+    HGB_CUDA(cudaMemsetAsync(l2.p, 0, ncap * 4, s));
     HGB_CUDA(cudaMemsetAsync(k2.p, 0xff, ncap * 8, s));
     HGB_CUDA(cudaMemsetAsync(h2.p, 0xff, ncap * 4, s));
     HGB_CUDA(cudaMemsetAsync(p2.p, 0, ncap * 4, s));
     kt.begin(s);
-    k_rehash<<<1024, 256, 0, s>>>(B.hkey.template as<unsigned long long>(), B.head.template as<int>(), B.hcap,
-                                 k2.template as<unsigned long long>(), h2.template as<int>(), ncap - 1, &dctl()->err);
+    k_rehash<<<1024, 256, 0, s>>>(B.hkey.template as<unsigned long long>(), B.head.template as<int>(),
+                                 B.klive.template as<int>(), B.hcap, k2.template as<unsigned long long>(),
+                                 h2.template as<int>(), l2.template as<int>(), ncap - 1, &dctl()->err);
     kt.end(s, KT_OTHER);
     ++launches;
     HGB_CUDA(cudaGetLastError());
@@ -244,7 +257,64 @@ struct Engine {
     std::swap(B.head.p, h2.p); std::swap(B.head.bytes, h2.bytes);
     std::swap(B.pend.p, p2.p); std::swap(B.pend.bytes, p2.bytes);
     std::swap(B.pend_base.p, pb2.p); std::swap(B.pend_base.bytes, pb2.bytes);
+    std::swap(B.klive.p, l2.p); std::swap(B.klive.bytes, l2.bytes);
     B.hcap = ncap;
+    return HORA_OK;
+  }
+  // Room in the exact-zone table of store k for `extra` more zones (load factor at most 1/2);
+  // a larger table is refilled from the stored nodes.
+  int ensure_ztab(int k, long long extra) {
+    const unsigned long long need = 2ull * ((unsigned long long)hctl.nnodes + (unsigned long long)extra);
+    if (need <= zcap) return HORA_OK;
+    unsigned long long c = std::max<unsigned long long>(zcap, 1ull << 16);
+    while (c < need) c <<= 1;
+    if (c > (1ull << 31)) { err = "exact-zone table beyond 2^31 slots"; return HORA_E_NOMEM; }
+    HGB_CUDA(zw.alloc(c * 8));
+    HGB_CUDA(cudaMemsetAsync(zw.p, 0, c * 8, s));
+    zcap = c;
+    kt.begin(s);
+    Level<D>::graph_rehash(store(k), (long long)hctl.nnodes, ztab(), dctl(), blocks, s);
+    kt.end(s, KT_OTHER);
+    ++launches;
+    HGB_CUDA(cudaGetLastError());
+    return HORA_OK;
+  }
+  // One level of the exact-zone graph: dedup by zone hash, store the new zones, record the edges.
+  int graph_level(const NetView* V, int k, int cur, long long nsucc, int level, bool roots) {
+    int rc;
+    InstState is = istate();
+    if ((rc = ensure_ztab(k, nsucc))) return rc;
+    if (nsucc > 0) {
+      kt.begin(s);
+      Level<D>::graph_probe(V, is, succ(), store(k), ztab(), dctl(), nsucc, blocks, s);
+      kt.end(s, KT_PROBE);
+      ++launches;
+      HGB_CUDA(cudaGetLastError());
+    }
+    if ((rc = read_ctl())) return rc;
+    if (hctl.err) { err = "device error in the graph probe"; return (int)hctl.err; }
+    const long long nnew = (long long)hctl.nsurv;
+    if ((rc = ensure_nodes(k, nnew))) return rc;
+    if (nnew > fcapb[cur ^ 1]) {
+      long long fc = fcapb[cur ^ 1];
+      while (nnew > fc) fc *= 2;
+      if ((rc = alloc_front(cur ^ 1, fc))) return rc;
+    }
+    const bool record = !roots;
+    if (record && (rc = ensure_edges((long long)hctl.nedges + nsucc))) return rc;
+    kt.begin(s);
+    if (nnew > 0) {
+      Level<D>::graph_store(V, is, succ(), store(k), ztab(), front(cur ^ 1), dctl(), nnew, level, blocks, s);
+      ++launches;
+    }
+    if (record && nsucc > 0) {
+      Level<D>::graph_edges(succ(), front(cur), edges(), dctl(), nsucc, s);
+      ++launches;
+    }
+    kt.end(s, KT_MERGE, (nnew > 0 ? 1 : 0) + (record && nsucc > 0 ? 1 : 0));
+    HGB_CUDA(cudaGetLastError());
+    if ((rc = read_ctl())) return rc;
+    if (hctl.err) { err = "device error in the graph store"; return (int)hctl.err; }
     return HORA_OK;
   }
   int ensure_nodes(int k, long long extra) {
@@ -286,6 +356,7 @@ struct Engine {
     HGB_CUDA(cudaGetDevice(&dev));
     HGB_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     blocks = o.blocks > 0 ? o.blocks : nsm * 16;
+    merge_blocks = nsm * std::max(1, Level<D>::merge_blocks_per_sm());
     int rc = upload_nets(nets, inst_shift, dn, err);
     if (rc) return rc;
     for (size_t k = 0; k < dn.blob_bytes.size(); ++k) h2d += dn.blob_bytes[k];
@@ -375,6 +446,13 @@ struct Engine {
       if (hctl.err) { err = "device error in expand"; return (int)hctl.err; }
       const long long nsucc = (long long)hctl.nsucc;
       if ((rc = ensure_hash(k, (unsigned long long)nsucc))) return rc;
+      if (mode == 1) {   // exact-zone graph
+        if ((rc = graph_level(V, k, cur, nsucc, level, roots))) return rc;
+        nf = (long long)hctl.nfront;
+        cur ^= 1;
+        roots = false;
+        continue;
+      }
       // ---- probe
       if (nsucc > 0) {
         kt.begin(s);
@@ -413,16 +491,13 @@ struct Engine {
         HGB_CUDA(clist.alloc(c * 4));
         ccap = c;
       }
-      const int record = (mode == 1 && !roots) ? 1 : 0;
-      if (record && (rc = ensure_edges((long long)hctl.nedges + nsucc))) return rc;
       // ---- group + merge
       if (ntouched > 0) {
         kt.begin(s);
         Level<D>::group(succ(), store(k), dctl(), nsucc, ntouched, s);
         kt.end(s, KT_GROUP, 2);
         kt.begin(s);
-        Level<D>::merge(V, is, front(cur), succ(), store(k), front(cur ^ 1), dctl(), ntouched, level, mode,
-                        edges(), record, blocks, s);
+        Level<D>::merge(V, is, succ(), store(k), front(cur ^ 1), dctl(), ntouched, level, merge_blocks, s);
         kt.end(s, KT_MERGE);
         launches += 3;
         HGB_CUDA(cudaGetLastError());
@@ -490,8 +565,9 @@ struct Engine {
     if ((rc = read_ctl())) return rc;
     long long nf = (long long)hctl.nfront;
     int level = 0;
+    // the reported level count is the graph's: per instance, its last level with a frontier
+    for (int q = 0; q < ninst; ++q) levels[q] = 0;
     if ((rc = run_levels(1, 1, cur, nf, level, S[0].nzone.template as<int>()))) return rc;
-    for (int q = 0; q < ninst; ++q) levels[q] = (unsigned long long)level;
     // stop flags and the sweep
     const long long n2 = (long long)hctl.nnodes, ne = (long long)hctl.nedges;
     DBuf stop, W, F;

@@ -13,6 +13,7 @@ struct Store {
   int* head;                  // [cap] newest node of the key's antichain, -1 when none
   unsigned* pend;             // [cap] survivors pending for this key in the current level
   unsigned* pend_base;        // [cap] their segment offset
+  int* klive;                 // [cap] live zones of the key (its chain links only live zones)
   unsigned long long hmask;   // cap - 1
   // passed-store nodes
   int* nzone;                 // [ncap * D*D]
@@ -38,6 +39,8 @@ struct Succ {                 // successors of the current level
   int* seg;                   // grouped survivors, one segment per touched slot
   int* sorted;                // the same segments in canonical order
   int* touched;               // touched slots
+  int* heavy;                 // touched slots merged block-wide
+  int* light;                 // touched slots merged by one tile
   unsigned long long* okh;    // canonical order key of each successor: parent's hash key ...
   unsigned long long* okl;    // ... then (parent's rank << 32) | emission ordinal
   unsigned long long* skh;    // the same keys gathered at the successor's segment position
@@ -46,6 +49,11 @@ struct Succ {                 // successors of the current level
   int* clist;                 // per touched key, its live zones gathered for the merge
   long long ccap;
 };
+struct ZTab {                 // exact-zone table of the graph store: one word per slot,
+  unsigned long long* w;      // (32-bit zone hash << 32) | ref, 0 when free; ref = node id, or
+  unsigned long long mask;    // kZRefSucc | successor index while a level is being inserted
+};
+constexpr unsigned kZRefSucc = 0x80000000u;
 struct Front {                // one frontier
   unsigned long long* key;    // hash key
   int* node;                  // passed-store node
@@ -76,8 +84,17 @@ struct Level {
   static void deadlock(const NetView* nets, InstState is, Succ sc, Ctl* ctl, long long nsurv, int blocks,
                        cudaStream_t s);
   static void group(Succ sc, Store st, Ctl* ctl, long long nsucc, long long ntouched, cudaStream_t s);
-  static void merge(const NetView* nets, InstState is, Front fr, Succ sc, Store st, Front out, Ctl* ctl,
-                    long long ntouched, int level, int mode, Edges ed, int record, int blocks, cudaStream_t s);
+  static void merge(const NetView* nets, InstState is, Succ sc, Store st, Front out, Ctl* ctl, long long ntouched,
+                    int level, int blocks, cudaStream_t s);
+  static int merge_blocks_per_sm();
+  // exact-zone graph store (leads-to graph mode): deduplicate the successors against the store and
+  // each other by zone hash, store the new zones, record one edge per successor
+  static void graph_probe(const NetView* nets, InstState is, Succ sc, Store st, ZTab zt, Ctl* ctl, long long nsucc,
+                          int blocks, cudaStream_t s);
+  static void graph_store(const NetView* nets, InstState is, Succ sc, Store st, ZTab zt, Front out, Ctl* ctl,
+                          long long nnew, int level, int blocks, cudaStream_t s);
+  static void graph_edges(Succ sc, Front fr, Edges ed, Ctl* ctl, long long nsucc, cudaStream_t s);
+  static void graph_rehash(Store st, long long nnodes, ZTab zt, Ctl* ctl, int blocks, cudaStream_t s);
   // leads-to: phase-1 nodes whose discrete state satisfies p, as a frontier
   static void collect_p(const NetView* nets, Store st, long long nnodes, Front out, Ctl* ctl, cudaStream_t s);
   // leads-to: end-of-run flags and the greatest-fixpoint sweep over the recorded graph

@@ -87,6 +87,7 @@ __global__ void __launch_bounds__(kBlock) k_init(const NetView* nets, int ninst,
     if (t.i == 0) {
       st.nnext[node] = -1; st.nlevel[node] = 0; st.ndead[node] = 0; st.ninst[node] = inst; st.nkey[node] = hk;
       st.head[slot] = (int)node;
+      st.klive[slot] = 1;
       const unsigned long long f = atomicAdd(&ctl->nfront, 1ull);
       out.key[f] = hk; out.node[f] = (int)node; out.rank[f] = 0; out.inst[f] = inst;
       is.nkeys[inst] = 1; is.nlive[inst] = 1; is.nfront[inst] = 1;
@@ -249,12 +250,18 @@ __global__ void __launch_bounds__(kBlock) k_deadlock(const NetView* nets, InstSt
 }
 
 // ---------------------------------------------------------------------------------------------
-// group: one contiguous segment of survivors per touched slot
+// group: one contiguous segment of survivors per touched slot; keys whose merge is long (many
+// survivors against a long antichain) go to the block-wide merge, the rest to the tile merge
 // ---------------------------------------------------------------------------------------------
+constexpr long long kHeavyMerge = 2048;   // survivors x (live zones + survivors) of a block-wide key
+
 static __global__ void k_seg_alloc(Succ sc, Store st, Ctl* ctl, long long ntouched) {
   for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < ntouched; j += (long long)gridDim.x * blockDim.x) {
     const int s = sc.touched[j];
-    st.pend_base[s] = (unsigned)atomicAdd(&ctl->seg_alloc, (unsigned long long)st.pend[s]);
+    const unsigned n = st.pend[s];
+    st.pend_base[s] = (unsigned)atomicAdd(&ctl->seg_alloc, (unsigned long long)n);
+    if ((long long)n * ((long long)st.klive[s] + n) >= kHeavyMerge) sc.heavy[atomicAdd(&ctl->nheavy, 1ull)] = s;
+    else sc.light[atomicAdd(&ctl->nlight, 1ull)] = s;
   }
 }
 static __global__ void k_seg_scatter(Succ sc, Store st, long long nsucc) {
@@ -270,189 +277,512 @@ static __global__ void k_seg_scatter(Succ sc, Store st, long long nsucc) {
 
 // ---------------------------------------------------------------------------------------------
 // merge: NetPassedT::add folds (passed_set.hpp:287-444) per key, in canonical order
+//
+// Per touched key: rank its survivors by the order key (parent key, parent rank, ordinal), gather
+// its live zones into a list (oldest first; the zones this merge stores are appended, so a
+// backwards scan is newest-first chain order), then for each survivor in order:
+//   (1)+(2) drop it if a zone stored at this level simulates it -- every older zone was already
+//           tried by the probe, and a stored zone is only retired by one that simulates it;
+//   (3)     retire the stored zones it simulates;
+//   (4)     absorb the newest convex-union partner among the newest kMergeScan live zones, and
+//           repeat with the hull until none is left;
+//   (5)     store it.
+// Finally the key's zones stored at this level go to the next frontier in chain order and the
+// key's chain is relinked through its live zones only.
 // ---------------------------------------------------------------------------------------------
+constexpr int kMergeBlock = 256;
+
+// Z ≼_aLU Zp decided by one thread from whole matrices behind plain pointers (global or shared).
+template <int D>
+__device__ __forceinline__ bool alu_le_ptr(const int* Z, const int* Zp, const int (&L)[D], const int (&U)[D]) {
+#pragma unroll
+  for (int x = 0; x < D; ++x) {
+    if (U[x] == kAluNegInf) continue;
+    const int z0x = Z[x];
+    if (z0x < r_le(-U[x])) continue;
+#pragma unroll
+    for (int y = 0; y < D; ++y) {
+      if (y == x || L[y] == kAluNegInf) continue;
+      const int zp = Zp[y * D + x];
+      if (zp < Z[y * D + x] && r_add(zp, r_lt(-L[y])) < z0x) return false;
+    }
+  }
+  return true;
+}
+
+// Canonical rank of every survivor of a segment; threads [tid, n) step `stride`.
+__device__ __forceinline__ void rank_segment(const Succ& sc, unsigned base, unsigned n, unsigned tid, unsigned stride) {
+  for (unsigned e = tid; e < n; e += stride) {
+    const unsigned long long kh = sc.skh[base + e], kl = sc.skl[base + e];
+    unsigned r = 0;
+    for (unsigned q = 0; q < n; ++q) {
+      const unsigned long long qh = sc.skh[base + q], ql = sc.skl[base + q];
+      r += (qh < kh || (qh == kh && (ql < kl || (ql == kl && q < e)))) ? 1u : 0u;
+    }
+    sc.sorted[base + r] = sc.seg[base + e];
+  }
+}
+
+// The key's live zones into clist, oldest first. Returns the list offset, or -1 on overflow.
+__device__ __forceinline__ long long gather_chain(const Succ& sc, const Store& st, int s, unsigned n, Ctl* ctl) {
+  const int c = st.klive[s];
+  const long long cb = (long long)atomicAdd(&ctl->chain_alloc, (unsigned long long)(c + n));
+  if (cb + c + n > sc.ccap) { atomicMax(&ctl->err, 4u); return -1; }
+  int k = c;
+  for (int m = st.head[s]; m >= 0 && k > 0; m = st.nnext[m])
+    if (!st.ndead[m]) sc.clist[cb + (--k)] = m;
+  if (k != 0) { atomicMax(&ctl->err, 4u); return -1; }
+  return cb;
+}
+
+// End of a key's merge (one thread): frontier entries, live-only chain, counters.
+__device__ __forceinline__ void finish_key(const Succ& sc, const Store& st, const Front& out, const InstState& is,
+                                           Ctl* ctl, int s, unsigned long long hk, int inst, const int* cl,
+                                           int clen0, int clen, long long dlive) {
+  int r = 0;
+  for (int k = clen - 1; k >= clen0; --k) {
+    const int m = cl[k];
+    if (m < 0) continue;
+    const unsigned long long f = atomicAdd(&ctl->nfront, 1ull);
+    out.key[f] = hk; out.node[f] = m; out.rank[f] = r++; out.inst[f] = inst;
+  }
+  if (r) atomicAdd(&is.nfront[inst], (unsigned long long)r);
+  const bool was_empty = st.head[s] < 0;
+  int prev = -1, live = 0;
+  for (int k = 0; k < clen; ++k) {
+    const int m = cl[k];
+    if (m < 0) continue;
+    st.nnext[m] = prev;
+    prev = m;
+    ++live;
+  }
+  st.head[s] = prev;
+  st.klive[s] = live;
+  if (was_empty && prev >= 0) { atomicAdd(&ctl->nkeys, 1ull); atomicAdd(&is.nkeys[inst], 1ull); }
+  if (dlive) {
+    atomicAdd((unsigned long long*)&ctl->nlive, (unsigned long long)dlive);
+    atomicAdd((unsigned long long*)&is.nlive[inst], (unsigned long long)dlive);
+  }
+  st.pend[s] = 0;
+}
+
+// New node for zone rows `z` of key hk (metadata only; the caller writes the zone).
+__device__ __forceinline__ void node_meta(const Store& st, long long node, int level, int inst, unsigned long long hk) {
+  st.nnext[node] = -1;
+  st.nlevel[node] = level;
+  st.ndead[node] = 0;
+  st.ninst[node] = inst;
+  st.nkey[node] = hk;
+}
 
 template <int D>
-__global__ void __launch_bounds__(kBlock) k_merge(const NetView* nets, InstState is, Front fr, Succ sc, Store st,
-                                                  Front out, Ctl* ctl, long long ntouched, int level, int mode,
-                                                  Edges ed, int record) {
-  Tile<D> t;
-  if (!make_tile(t, threadIdx.x & 31)) return;
+struct MergeShared {
+  int z[D * D];         // the survivor being added (becomes the hull on a union)
+  int L[D], U[D];       // the key's per-clock bounds
+  int win[kMergeScan];  // list positions of the newest live zones, newest first
+  long long cb;
+  int nw, best, node, retired, clen, job;
+};
+
+// One key merged by a whole block.
+template <int D>
+__device__ void merge_key_block(const NetView* nets, const InstState& is, const Succ& sc, const Store& st,
+                                const Front& out, Ctl* ctl, int s, int level, bool in_tile, const Tile<D>& t,
+                                MergeShared<D>& sh) {
+  constexpr int TPW = 32 / D;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int ishift = nets[0].inst_shift;
-  volatile int* vhead = st.head;
-  volatile int* vnext = st.nnext;
-  volatile int* vdead = st.ndead;
-  volatile int* vlevel = st.nlevel;
-  for (long long j = tile_id<D>(); j < ntouched; j += tile_count<D>()) {
-    const int s = sc.touched[j];
-    const unsigned n = st.pend[s];
-    const unsigned base = st.pend_base[s];
-    const unsigned long long hk = st.hkey[s];
-    const int inst = (int)(hk >> ishift);
-    if (is.found[inst] || is.done[inst]) { t.sync(); if (t.i == 0) st.pend[s] = 0; continue; }
-    const NetView& N = nets[inst];
-    // canonical order: rank every pending survivor by (parent key, parent rank, ordinal)
-    for (unsigned e = t.i; e < n; e += D) {
-      const unsigned long long kh = sc.skh[base + e], kl = sc.skl[base + e];
-      unsigned r = 0;
-      for (unsigned q = 0; q < n; ++q) {
-        const unsigned long long qh = sc.skh[base + q], ql = sc.skl[base + q];
-        r += (qh < kh || (qh == kh && (ql < kl || (ql == kl && q < e)))) ? 1u : 0u;
-      }
-      sc.sorted[base + r] = sc.seg[base + e];
-    }
-    // the key's live zones, gathered once into a contiguous list: oldest first, so that the zones
-    // this merge stores are appended and a backwards scan is the chain's newest-first order
-    long long cb = 0;
-    int clen = 0;
-    if (t.i == 0) {
-      int c = 0;
-      for (int m = vhead[s]; m >= 0; m = vnext[m]) c += vdead[m] ? 0 : 1;
-      cb = (long long)atomicAdd(&ctl->chain_alloc, (unsigned long long)(c + n));
-      if (cb + c + n > sc.ccap) { atomicMax(&ctl->err, 4u); cb = -1; }
-      else {
-        int k = c;
-        for (int m = vhead[s]; m >= 0; m = vnext[m])
-          if (!vdead[m]) sc.clist[cb + (--k)] = m;
-      }
-      clen = c;
-    }
-    cb = (long long)t.shfl64((unsigned long long)cb, 0);
-    clen = t.shfl(clen, 0);
-    t.sync();
-    if (cb < 0) continue;
-    volatile int* cl = sc.clist + cb;
+  const unsigned n = st.pend[s];
+  const unsigned base = st.pend_base[s];
+  const unsigned long long hk = st.hkey[s];
+  const int inst = (int)(hk >> ishift);
+  if (is.found[inst] || is.done[inst]) {
+    __syncthreads();
+    if (tid == 0) st.pend[s] = 0;
+    return;
+  }
+  const NetView& N = nets[inst];
+  rank_segment(sc, base, n, tid, blockDim.x);
+  if (tid == 0) {
+    sh.cb = gather_chain(sc, st, s, n, ctl);
+    sh.clen = st.klive[s];
+    sh.retired = 0;
+  }
+  if (warp == 0 && in_tile && t.base == 0) {
     int locs[kMaxProcs], ints[kMaxInts];
     key_decode(N, key_part(hk, ishift), locs, ints);
-    int Ly, U[D], Lall[D];
+    int Ly, U[D];
     key_bounds(N, t, locs, Ly, U);
+    sh.L[t.i] = Ly;
+    sh.U[t.i] = U[t.i];
+  }
+  __syncthreads();
+  if (sh.cb < 0) { __syncthreads(); return; }
+  int Lr[D], Ur[D];
 #pragma unroll
-    for (int x = 0; x < D; ++x) Lall[x] = t.shfl(Ly, x);
-    long long dlive = 0;
-    unsigned long long nprobe = 0;
-    // store z as a new node of this key and append it to the list
-    auto store_new = [&](const int (&z)[D]) -> int {
-      long long node = 0;
-      if (t.i == 0) node = (long long)atomicAdd(&ctl->nnodes, 1ull);
-      node = (long long)t.shfl64((unsigned long long)node, 0);
-      store_rows(t, z, st.nzone + node * D * D);
-      t.sync();
-      if (t.i == 0) {
-        const int old_head = vhead[s];
-        if (old_head < 0) { atomicAdd(&ctl->nkeys, 1ull); atomicAdd(&is.nkeys[inst], 1ull); }
-        st.nnext[node] = old_head;
-        st.nlevel[node] = level;
-        st.ndead[node] = 0;
-        st.ninst[node] = inst;
-        st.nkey[node] = hk;
-        cl[clen] = (int)node;
-        __threadfence_block();
-        vhead[s] = (int)node;
+  for (int x = 0; x < D; ++x) { Lr[x] = sh.L[x]; Ur[x] = sh.U[x]; }
+  int* cl = sc.clist + sh.cb;
+  const int clen0 = sh.clen;
+  long long dlive = 0;   // meaningful on thread 0
+  const int tile_idx = warp * TPW + lane / D, ntiles = (blockDim.x >> 5) * TPW;
+  for (unsigned q = 0; q < n; ++q) {
+    const int a = sc.sorted[base + q];
+    for (int e = tid; e < D * D; e += blockDim.x) sh.z[e] = sc.zone[(long long)a * D * D + e];
+    __syncthreads();
+    const int clen = sh.clen;
+    // (1)+(2)
+    bool drop = false;
+    for (int k = clen0 + tid; k < clen && !drop; k += blockDim.x) {
+      const int m = cl[k];
+      if (m >= 0) drop = alu_le_ptr<D>(sh.z, st.nzone + (long long)m * D * D, Lr, Ur);
+    }
+    if (__syncthreads_or(drop)) continue;
+    // (3)
+    int ret = 0;
+    for (int k = tid; k < clen; k += blockDim.x) {
+      const int m = cl[k];
+      if (m >= 0 && alu_le_ptr<D>(st.nzone + (long long)m * D * D, sh.z, Lr, Ur)) {
+        st.ndead[m] = 1;
+        cl[k] = -1;
+        ++ret;
       }
-      ++clen;
-      ++dlive;
-      t.sync();
-      return (int)node;
-    };
-    for (unsigned q = 0; q < n; ++q) {
-      const int a = ((volatile int*)sc.sorted)[base + q];
-      const int* zs = sc.zone + (long long)a * D * D;
-      int z[D], z0[D];
-      load_rows(t, z, zs);
-#pragma unroll
-      for (int x = 0; x < D; ++x) z0[x] = t.shfl(z[x], 0);
-      if (mode == 1) {
-        // exact-zone graph: the lanes compare the list's zones in turn; at most one can be equal
-        int mine = -1;
-        for (int k = t.i; k < clen; k += D) {
-          const int m = cl[k];
-          const int* zp = st.nzone + (long long)m * D * D;
-          bool eq = true;
-          for (int e = 0; e < D * D && eq; ++e) eq = __ldcg(zp + e) == __ldg(zs + e);
-          if (eq) { mine = m; break; }
+    }
+    if (ret) atomicAdd(&sh.retired, ret);
+    // (4)
+    for (;;) {
+      __syncthreads();
+      if (warp == 0) {
+        int nw = 0;
+        for (int top = clen - 1; top >= 0 && nw < kMergeScan; top -= 32) {
+          const int k = top - lane;
+          const bool live = k >= 0 && cl[k] >= 0;
+          const unsigned b = __ballot_sync(0xffffffffu, live);
+          const int before = __popc(b & ((1u << lane) - 1u));
+          if (live && nw + before < kMergeScan) sh.win[nw + before] = k;
+          nw += __popc(b);
         }
-        int hit = -1;
-#pragma unroll
-        for (int l = 0; l < D; ++l) { const int v = t.shfl(mine, l); hit = v >= 0 ? v : hit; }
-        if (hit < 0) hit = store_new(z);
-        if (record && t.i == 0) {
-          const unsigned long long e = atomicAdd(&ctl->nedges, 1ull);
-          if ((long long)e < ed.cap) { ed.src[e] = fr.node[sc.parent[a]]; ed.dst[e] = hit; }
-          else atomicMax(&ctl->err, 4u);
+        if (lane == 0) {
+          sh.nw = nw < kMergeScan ? nw : kMergeScan;
+          sh.best = 0x7fffffff;
+          dlive -= sh.retired;
+          sh.retired = 0;
         }
-        continue;
       }
-      // (1)+(2): dropped if a stored zone simulates it. Every zone stored before this level was
-      // already tested by the probe, and a stored zone is only ever retired by one that simulates
-      // it, so only the zones stored at this level -- the list's tail -- can still drop it.
-      bool drop = false;
-      for (int k = clen - 1; k >= 0; --k) {
-        const int m = cl[k];
-        if (m < 0) continue;
-        if (vlevel[m] != level) break;
-        int zp[D];
-        load_rows_rw(t, zp, st.nzone + (long long)m * D * D);
-        ++nprobe;
-        if (alu_le(t, z, zp, z0, Ly, U)) { drop = true; break; }
-      }
-      if (drop) continue;
-      // (3): retire the stored zones the new one simulates; the lanes take the list in turn
-      {
-        int retired = 0;
-        for (int k = t.i; k < clen; k += D) {
-          const int m = cl[k];
-          if (m < 0) continue;
-          if (alu_le_lane<D>(st.nzone + (long long)m * D * D, zs, Lall, U)) {
-            vdead[m] = 1;
-            cl[k] = -1;
-            ++retired;
-          }
-        }
-        t.sync();
+      __syncthreads();
+      const int nw = sh.nw;
+      if (nw == 0) break;
+      int mybest = 0x7fffffff;
+      int hull[D];
+      if (in_tile) {
+        for (int c = tile_idx; c < nw; c += ntiles) {
+          int za[D], zb[D];
 #pragma unroll
-        for (int l = 0; l < D; ++l) dlive -= t.shfl(retired, l);
-      }
-      // (4): convex-union absorb within the newest kMergeScan live zones, restarting after each
-      for (bool merged = true; merged;) {
-        merged = false;
-        int seen = 0;
-        for (int k = clen - 1; k >= 0 && seen < kMergeScan; --k) {
-          const int m = cl[k];
-          if (m < 0) continue;
-          ++seen;
-          int zp[D];
-          load_rows_rw(t, zp, st.nzone + (long long)m * D * D);
-          if (try_union(t, z, zp)) {
-            t.sync();
-            if (t.i == 0) { vdead[m] = 1; cl[k] = -1; }
-            --dlive;
-            t.sync();
-            merged = true;
+          for (int j = 0; j < D; ++j) za[j] = sh.z[t.i * D + j];
+          load_rows_rw(t, zb, st.nzone + (long long)cl[sh.win[c]] * D * D);
+          if (try_union(t, za, zb)) {
+            mybest = c;
+#pragma unroll
+            for (int j = 0; j < D; ++j) hull[j] = za[j];
             break;
           }
         }
+        if (t.i == 0 && mybest != 0x7fffffff) atomicMin(&sh.best, mybest);
       }
-      // (5): prepend
-      store_new(z);
+      __syncthreads();
+      const int best = sh.best;
+      if (best == 0x7fffffff) break;
+      if (in_tile && mybest == best) {
+#pragma unroll
+        for (int j = 0; j < D; ++j) sh.z[t.i * D + j] = hull[j];
+      }
+      if (tid == 0) {
+        const int k = sh.win[best];
+        st.ndead[cl[k]] = 1;
+        cl[k] = -1;
+        --dlive;
+      }
     }
-    // this key's zones stored at this level enter the next frontier, in chain order
-    if (t.i == 0) {
-      int r = 0;
-      for (int k = clen - 1; k >= 0; --k) {
-        const int m = cl[k];
-        if (m < 0 || vlevel[m] != level) continue;
-        const unsigned long long f = atomicAdd(&ctl->nfront, 1ull);
-        out.key[f] = hk; out.node[f] = m; out.rank[f] = r++; out.inst[f] = inst;
-      }
-      if (r) atomicAdd(&is.nfront[inst], (unsigned long long)r);
-      if (dlive) {
-        atomicAdd((unsigned long long*)&ctl->nlive, (unsigned long long)dlive);
-        atomicAdd((unsigned long long*)&is.nlive[inst], (unsigned long long)dlive);
-      }
-      st.pend[s] = 0;
+    // (5)
+    if (tid == 0) {
+      const long long node = (long long)atomicAdd(&ctl->nnodes, 1ull);
+      sh.node = (int)node;
+      node_meta(st, node, level, inst, hk);
+      cl[clen] = (int)node;
+      sh.clen = clen + 1;
+      ++dlive;
     }
-    if (nprobe) atomicAdd(&ctl->probes, nprobe);
+    __syncthreads();
+    const long long node = sh.node;
+    for (int e = tid; e < D * D; e += blockDim.x) st.nzone[node * D * D + e] = sh.z[e];
+    __syncthreads();   // the zone is written before the next survivor replaces sh.z
+  }
+  __syncthreads();
+  if (tid == 0) finish_key(sc, st, out, is, ctl, s, hk, inst, cl, clen0, sh.clen, dlive);
+  __syncthreads();
+}
+
+// One key merged by one tile (keys with little work).
+template <int D>
+__device__ void merge_key_tile(const NetView* nets, const InstState& is, const Succ& sc, const Store& st,
+                               const Front& out, Ctl* ctl, int s, int level, const Tile<D>& t) {
+  const int ishift = nets[0].inst_shift;
+  const unsigned n = st.pend[s];
+  const unsigned base = st.pend_base[s];
+  const unsigned long long hk = st.hkey[s];
+  const int inst = (int)(hk >> ishift);
+  if (is.found[inst] || is.done[inst]) { t.sync(); if (t.i == 0) st.pend[s] = 0; return; }
+  const NetView& N = nets[inst];
+  rank_segment(sc, base, n, t.i, D);
+  long long cb = 0;
+  if (t.i == 0) cb = gather_chain(sc, st, s, n, ctl);
+  cb = (long long)t.shfl64((unsigned long long)cb, 0);
+  t.sync();
+  if (cb < 0) return;
+  int clen = st.klive[s];
+  const int clen0 = clen;
+  volatile int* cl = sc.clist + cb;
+  volatile int* vdead = st.ndead;
+  int locs[kMaxProcs], ints[kMaxInts];
+  key_decode(N, key_part(hk, ishift), locs, ints);
+  int Ly, U[D], Lall[D];
+  key_bounds(N, t, locs, Ly, U);
+#pragma unroll
+  for (int x = 0; x < D; ++x) Lall[x] = t.shfl(Ly, x);
+  long long dlive = 0;
+  for (unsigned q = 0; q < n; ++q) {
+    const int a = ((volatile int*)sc.sorted)[base + q];
+    const int* zs = sc.zone + (long long)a * D * D;
+    int z[D];
+    load_rows(t, z, zs);
+    // (1)+(2): the lanes take this level's zones in turn
+    bool drop = false;
+    for (int k = clen0 + t.i; k < clen && !drop; k += D) {
+      const int m = cl[k];
+      if (m >= 0) drop = alu_le_lane<D>(zs, st.nzone + (long long)m * D * D, Lall, U);
+    }
+    if (t.any(drop)) continue;
+    // (3)
+    int retired = 0;
+    for (int k = t.i; k < clen; k += D) {
+      const int m = cl[k];
+      if (m >= 0 && alu_le_lane<D>(st.nzone + (long long)m * D * D, zs, Lall, U)) {
+        vdead[m] = 1;
+        cl[k] = -1;
+        ++retired;
+      }
+    }
     t.sync();
+#pragma unroll
+    for (int l = 0; l < D; ++l) dlive -= t.shfl(retired, l);
+    // (4)
+    for (bool merged = true; merged;) {
+      merged = false;
+      int seen = 0;
+      for (int k = clen - 1; k >= 0 && seen < kMergeScan; --k) {
+        const int m = cl[k];
+        if (m < 0) continue;
+        ++seen;
+        int zp[D];
+        load_rows_rw(t, zp, st.nzone + (long long)m * D * D);
+        if (try_union(t, z, zp)) {
+          t.sync();
+          if (t.i == 0) { vdead[m] = 1; cl[k] = -1; }
+          --dlive;
+          t.sync();
+          merged = true;
+          break;
+        }
+      }
+    }
+    // (5)
+    long long node = 0;
+    if (t.i == 0) node = (long long)atomicAdd(&ctl->nnodes, 1ull);
+    node = (long long)t.shfl64((unsigned long long)node, 0);
+    store_rows(t, z, st.nzone + node * D * D);
+    if (t.i == 0) {
+      node_meta(st, node, level, inst, hk);
+      cl[clen] = (int)node;
+    }
+    ++clen;
+    ++dlive;
+    t.sync();
+  }
+  if (t.i == 0) finish_key(sc, st, out, is, ctl, s, hk, inst, (const int*)cl, clen0, clen, dlive);
+  t.sync();
+}
+
+template <int D>
+__global__ void __launch_bounds__(kMergeBlock) k_merge(const NetView* nets, InstState is, Succ sc, Store st,
+                                                       Front out, Ctl* ctl, int level) {
+  __shared__ MergeShared<D> sh;
+  Tile<D> t;
+  const bool in_tile = make_tile(t, threadIdx.x & 31);
+  // keys with much work: one block each, taken in turn
+  const long long nheavy = (long long)ctl->nheavy, nlight = (long long)ctl->nlight;
+  for (;;) {
+    if (threadIdx.x == 0) sh.job = (int)atomicAdd(&ctl->heavy_next, 1ull);
+    __syncthreads();
+    const long long j = sh.job;
+    __syncthreads();
+    if (j >= nheavy) break;
+    merge_key_block<D>(nets, is, sc, st, out, ctl, sc.heavy[j], level, in_tile, t, sh);
+  }
+  // the rest: one tile each, taken in turn
+  if (!in_tile) return;
+  for (;;) {
+    unsigned long long j = 0;
+    if (t.i == 0) j = atomicAdd(&ctl->light_next, 1ull);
+    j = t.shfl64(j, 0);
+    if ((long long)j >= nlight) break;
+    merge_key_tile<D>(nets, is, sc, st, out, ctl, sc.light[j], level, t);
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// exact-zone graph store (leads-to graph mode): hash dedup instead of a per-key list scan
+// ---------------------------------------------------------------------------------------------
+// 32-bit hash of (hash key, zone), never 0: each lane mixes its row, lane 0 folds the rows in order.
+template <int D>
+__device__ __forceinline__ unsigned zone_hash(const Tile<D>& t, const int (&z)[D], unsigned long long hk) {
+  unsigned long long r = 0x9e3779b97f4a7c15ull * (unsigned long long)(t.i + 1);
+#pragma unroll
+  for (int j = 0; j < D; ++j) r = hash_mix(r ^ (unsigned)z[j]);
+  unsigned long long h = hash_mix(hk);
+#pragma unroll
+  for (int l = 0; l < D; ++l) h = hash_mix(h ^ t.shfl64(r, l));
+  const unsigned v = (unsigned)(h >> 32);
+  return v ? v : 1u;
+}
+
+// Per successor: find an equal stored zone, an equal successor of this level that claimed a slot
+// first, or claim a free slot. Claimers are listed in sc.surv; sc.slot[s] = claimed slot (>= 0),
+// -2 for a duplicate (sc.rank[s] = the slot word's ref), -1 when the instance is finished.
+template <int D>
+__global__ void __launch_bounds__(kBlock) k_graph_probe(const NetView* nets, InstState is, Succ sc, Store st, ZTab zt,
+                                                        Ctl* ctl, long long nsucc) {
+  Tile<D> t;
+  if (!make_tile(t, threadIdx.x & 31)) return;
+  const int ishift = nets[0].inst_shift;
+  volatile unsigned long long* vw = zt.w;
+  for (long long s = tile_id<D>(); s < nsucc; s += tile_count<D>()) {
+    const unsigned long long hk = sc.key[s];
+    const int inst = (int)(hk >> ishift);
+    if (is.found[inst] || is.done[inst]) { if (t.i == 0) sc.slot[s] = -1; continue; }
+    int z[D];
+    load_rows(t, z, sc.zone + s * D * D);
+    const unsigned h = zone_hash(t, z, hk);
+    const unsigned long long mine = ((unsigned long long)h << 32) | (kZRefSucc | (unsigned)s);
+    unsigned long long pos = hash_mix(((unsigned long long)h << 32) ^ hk) & zt.mask;
+    int result = -3;   // -3 searching, >= 0 claimed slot, -2 duplicate
+    unsigned ref = 0;
+    for (unsigned long long it = 0; it <= zt.mask && result == -3; ++it, pos = (pos + 1) & zt.mask) {
+      unsigned long long w = 0;
+      if (t.i == 0) {
+        w = vw[pos];
+        if (w == 0) w = atomicCAS(&zt.w[pos], 0ull, mine);   // 0: claimed
+      }
+      w = t.shfl64(w, 0);
+      if (w == 0) { result = (int)pos; break; }
+      if ((unsigned)(w >> 32) != h) continue;
+      const unsigned r = (unsigned)w;
+      const bool succ_ref = (r & kZRefSucc) != 0;
+      const long long idx = (long long)(r & ~kZRefSucc);
+      const unsigned long long okey = succ_ref ? sc.key[idx] : st.nkey[idx];
+      if (okey != hk) continue;
+      const int* oz = (succ_ref ? sc.zone : st.nzone) + idx * D * D;
+      bool eq = true;
+#pragma unroll
+      for (int j = 0; j < D; ++j) eq &= __ldcg(oz + t.i * D + j) == z[j];
+      if (t.all(eq)) { result = -2; ref = r; }
+    }
+    if (t.i == 0) {
+      if (result == -3) {   // table full: the host sizes it at most half full, so this is an error
+        atomicMax(&ctl->err, 4u);
+        sc.slot[s] = -1;
+      } else {
+        sc.slot[s] = result;
+        if (result == -2) sc.rank[s] = (int)ref;
+        else sc.surv[atomicAdd(&ctl->nsurv, 1ull)] = (int)s;
+        // keys are counted once, by the successor that first inserts the discrete key
+        bool ins = false;
+        const long long ks = slot_find_insert(st, hk, &ins);
+        if (ks < 0) atomicMax(&ctl->err, 4u);
+        else if (ins) { atomicAdd(&ctl->nslots, 1ull); atomicAdd(&ctl->nkeys, 1ull); atomicAdd(&is.nkeys[inst], 1ull); }
+      }
+    }
+  }
+}
+
+// Store every claimer as a node of this level, point its slot at the node and put it in the next
+// frontier; sc.rank[s] = its node id.
+template <int D>
+__global__ void __launch_bounds__(kBlock) k_graph_store(const NetView* nets, InstState is, Succ sc, Store st, ZTab zt,
+                                                        Front out, Ctl* ctl, long long nnew, int level) {
+  Tile<D> t;
+  if (!make_tile(t, threadIdx.x & 31)) return;
+  const int ishift = nets[0].inst_shift;
+  for (long long w = tile_id<D>(); w < nnew; w += tile_count<D>()) {
+    const int s = sc.surv[w];
+    const unsigned long long hk = sc.key[s];
+    const int inst = (int)(hk >> ishift);
+    long long node = 0;
+    if (t.i == 0) node = (long long)atomicAdd(&ctl->nnodes, 1ull);
+    node = (long long)t.shfl64((unsigned long long)node, 0);
+    int z[D];
+    load_rows(t, z, sc.zone + (long long)s * D * D);
+    store_rows(t, z, st.nzone + node * D * D);
+    if (t.i == 0) {
+      st.nnext[node] = -1;
+      st.nlevel[node] = level;
+      st.ndead[node] = 0;
+      st.ninst[node] = inst;
+      st.nkey[node] = hk;
+      const long long pos = sc.slot[s];
+      zt.w[pos] = (zt.w[pos] & 0xffffffff00000000ull) | (unsigned)node;
+      sc.rank[s] = (int)node;
+      const unsigned long long f = atomicAdd(&ctl->nfront, 1ull);
+      out.key[f] = hk; out.node[f] = (int)node; out.rank[f] = 0; out.inst[f] = inst;
+      atomicAdd(&is.nfront[inst], 1ull);
+      atomicAdd((unsigned long long*)&ctl->nlive, 1ull);
+      atomicAdd((unsigned long long*)&is.nlive[inst], 1ull);
+    }
+  }
+}
+
+// One edge per successor, from its parent's node to the node holding its zone.
+static __global__ void k_graph_edges(Succ sc, Front fr, Edges ed, Ctl* ctl, long long nsucc) {
+  for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < nsucc; s += (long long)gridDim.x * blockDim.x) {
+    const int sl = sc.slot[s];
+    if (sl == -1) continue;
+    int node;
+    if (sl >= 0) node = sc.rank[s];
+    else {
+      const unsigned r = (unsigned)sc.rank[s];
+      node = (r & kZRefSucc) ? sc.rank[r & ~kZRefSucc] : (int)r;
+    }
+    const unsigned long long e = atomicAdd(&ctl->nedges, 1ull);
+    if ((long long)e < ed.cap) { ed.src[e] = fr.node[sc.parent[s]]; ed.dst[e] = node; }
+    else atomicMax(&ctl->err, 4u);
+  }
+}
+
+// Re-insert every stored node into a fresh (larger) zone table.
+template <int D>
+__global__ void __launch_bounds__(kBlock) k_graph_rehash(Store st, long long nnodes, ZTab zt, Ctl* ctl) {
+  Tile<D> t;
+  if (!make_tile(t, threadIdx.x & 31)) return;
+  for (long long n = tile_id<D>(); n < nnodes; n += tile_count<D>()) {
+    const unsigned long long hk = st.nkey[n];
+    int z[D];
+    load_rows(t, z, st.nzone + n * D * D);
+    const unsigned h = zone_hash(t, z, hk);
+    if (t.i == 0) {
+      unsigned long long pos = hash_mix(((unsigned long long)h << 32) ^ hk) & zt.mask;
+      unsigned long long it = 0;
+      for (; it <= zt.mask; ++it, pos = (pos + 1) & zt.mask)
+        if (atomicCAS(&zt.w[pos], 0ull, ((unsigned long long)h << 32) | (unsigned)n) == 0ull) break;
+      if (it > zt.mask) atomicMax(&ctl->err, 4u);
+    }
   }
 }
 
@@ -642,11 +972,36 @@ void Level<D>::group(Succ sc, Store st, Ctl* ctl, long long nsucc, long long nto
   k_seg_scatter<<<grid_for(nsucc, 256, 4096), 256, 0, s>>>(sc, st, nsucc);
 }
 template <int D>
-void Level<D>::merge(const NetView* nets, InstState is, Front fr, Succ sc, Store st, Front out, Ctl* ctl,
-                     long long ntouched, int level, int mode, Edges ed, int record, int blocks, cudaStream_t s) {
+int Level<D>::merge_blocks_per_sm() {
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_merge<D>, kMergeBlock, 0) != cudaSuccess) n = 1;
+  return n;
+}
+template <int D>
+void Level<D>::merge(const NetView* nets, InstState is, Succ sc, Store st, Front out, Ctl* ctl, long long ntouched,
+                     int level, int blocks, cudaStream_t s) {
+  const long long g = ntouched < blocks ? ntouched : blocks;
+  k_merge<D><<<(int)(g > 0 ? g : 1), kMergeBlock, 0, s>>>(nets, is, sc, st, out, ctl, level);
+}template <int D>
+void Level<D>::graph_probe(const NetView* nets, InstState is, Succ sc, Store st, ZTab zt, Ctl* ctl, long long nsucc,
+                           int blocks, cudaStream_t s) {
   constexpr int TPB = (kBlock / 32) * (32 / D);
-  k_merge<D><<<grid_for(ntouched, TPB, blocks), kBlock, 0, s>>>(nets, is, fr, sc, st, out, ctl, ntouched, level,
-                                                                mode, ed, record);
+  k_graph_probe<D><<<grid_for(nsucc, TPB, blocks), kBlock, 0, s>>>(nets, is, sc, st, zt, ctl, nsucc);
+}
+template <int D>
+void Level<D>::graph_store(const NetView* nets, InstState is, Succ sc, Store st, ZTab zt, Front out, Ctl* ctl,
+                           long long nnew, int level, int blocks, cudaStream_t s) {
+  constexpr int TPB = (kBlock / 32) * (32 / D);
+  k_graph_store<D><<<grid_for(nnew, TPB, blocks), kBlock, 0, s>>>(nets, is, sc, st, zt, out, ctl, nnew, level);
+}
+template <int D>
+void Level<D>::graph_edges(Succ sc, Front fr, Edges ed, Ctl* ctl, long long nsucc, cudaStream_t s) {
+  k_graph_edges<<<grid_for(nsucc, 256, 8192), 256, 0, s>>>(sc, fr, ed, ctl, nsucc);
+}
+template <int D>
+void Level<D>::graph_rehash(Store st, long long nnodes, ZTab zt, Ctl* ctl, int blocks, cudaStream_t s) {
+  constexpr int TPB = (kBlock / 32) * (32 / D);
+  if (nnodes > 0) k_graph_rehash<D><<<grid_for(nnodes, TPB, blocks), kBlock, 0, s>>>(st, nnodes, zt, ctl);
 }
 template <int D>
 void Level<D>::collect_p(const NetView* nets, Store st, long long nnodes, Front out, Ctl* ctl, cudaStream_t s) {
