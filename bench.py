@@ -32,7 +32,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 WORKLOAD_CONFIG = 2
-WORKLOAD_SEED = int(os.environ.get("HORA_BENCH_SEED", "23"))
+WORKLOAD_SEED = int(os.environ.get("HORA_BENCH_SEED", "2483"))
 CPU_SAMPLE_SECONDS = 20.0
 METRIC = "zone successors/s"
 UNIT = "successors/s"

@@ -65,13 +65,13 @@ struct NetView {
   const int* p_clk;
 };
 
-// Device-side counters, read back with a single copy. The first block is reset at every level.
+// Device-side counters, read back with a single copy. The first block is reset before every
+// expand (a level runs as one or more chunks of instances), nfront at every level.
 struct Ctl {
   unsigned long long nsucc;      // successors produced by expand (may exceed capacity)
   unsigned long long nsurv;      // successors that passed the probe
   unsigned long long ntouched;   // hash slots with pending successors
   unsigned long long seg_alloc;  // grouping segment allocator
-  unsigned long long nfront;     // next-frontier entries
   unsigned long long chain_alloc;  // merge's chain-list allocator
   unsigned long long nheavy;     // touched keys merged block-wide ...
   unsigned long long nlight;     // ... and by one tile
@@ -79,16 +79,19 @@ struct Ctl {
   unsigned long long light_next;
   unsigned int found;            // some instance hit its goal this level
   unsigned int overflow;         // expand output overflowed
+  // per level
+  unsigned long long nfront;     // next-frontier entries
   // cumulative
   unsigned long long nnodes;     // passed-store nodes allocated
   unsigned long long nkeys;      // distinct keys holding at least one stored zone
   unsigned long long nslots;     // occupied hash slots
   unsigned long long nedges;     // graph edges recorded (leads-to graph mode)
   unsigned long long probes;     // stored zones read by the probe and the merge
+  unsigned long long arena_alloc;  // key-list arena in use
   long long nlive;               // live passed-store zones
   unsigned int err;              // HORA_E_* raised on the device (table full, escape overflow)
   unsigned int flag;             // set by a fixpoint pass that changed something
 };
-constexpr unsigned long long kCtlLevelBytes = 10 * 8 + 2 * 4;
+constexpr unsigned long long kCtlChunkBytes = 9 * 8 + 2 * 4;
 
 }  // namespace hgb

@@ -52,8 +52,8 @@ struct DBuf {
   template <class T> T* as() const { return static_cast<T*>(p); }
 };
 
-static __global__ void k_rehash(const unsigned long long* okey, const int* ohead, const int* olive,
-                                unsigned long long ocap, unsigned long long* nkey, int* nhead, int* nlive,
+static __global__ void k_rehash(const unsigned long long* okey, const long long* ooff, const int* olive,
+                                unsigned long long ocap, unsigned long long* nkey, long long* noff, int* nlive,
                                 unsigned long long nmask, unsigned* err) {
   for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < ocap;
        i += (unsigned long long)gridDim.x * blockDim.x) {
@@ -62,7 +62,7 @@ static __global__ void k_rehash(const unsigned long long* okey, const int* ohead
     unsigned long long h = hash_mix(k) & nmask;
     unsigned long long probe = 0;
     for (; probe <= nmask; ++probe) {
-      if (atomicCAS(&nkey[h], kEmptyKey, k) == kEmptyKey) { nhead[h] = ohead[i]; nlive[h] = olive[i]; break; }
+      if (atomicCAS(&nkey[h], kEmptyKey, k) == kEmptyKey) { noff[h] = ooff[i]; nlive[h] = olive[i]; break; }
       h = (h + 1) & nmask;
     }
     if (probe > nmask) atomicMax(err, 4u);
@@ -100,10 +100,11 @@ enum { KT_EXPAND = 0, KT_PROBE = 1, KT_DEADLOCK = 2, KT_GROUP = 3, KT_MERGE = 4,
 
 template <int D>
 struct StoreBufs {
-  DBuf hkey, head, pend, pend_base, klive;    // hash table
-  DBuf nzone, nnext, nlevel, ndead, ninst, nkey;  // nodes
+  DBuf hkey, pend, pend_base, klive, kloff;   // hash table
+  DBuf arena;                                 // key lists
+  DBuf nzone, nlevel, ndead, ninst, nkey;     // nodes
   unsigned long long hcap = 0;
-  long long ncap = 0;
+  long long ncap = 0, acap = 0;
 };
 
 // The level-synchronous engine over a group of instances sharing the DBM dimension D. Store 0 is
@@ -154,11 +155,12 @@ struct Engine {
   Store store(int k) {
     StoreBufs<D>& B = S[k];
     Store st;
-    st.hkey = B.hkey.template as<unsigned long long>(); st.head = B.head.template as<int>();
+    st.hkey = B.hkey.template as<unsigned long long>();
     st.pend = B.pend.template as<unsigned>(); st.pend_base = B.pend_base.template as<unsigned>();
-    st.klive = B.klive.template as<int>();
+    st.klive = B.klive.template as<int>(); st.kloff = B.kloff.template as<long long>();
     st.hmask = B.hcap - 1;
-    st.nzone = B.nzone.template as<int>(); st.nnext = B.nnext.template as<int>();
+    st.arena = B.arena.template as<int>(); st.acap = B.acap;
+    st.nzone = B.nzone.template as<int>();
     st.nlevel = B.nlevel.template as<int>(); st.ndead = B.ndead.template as<int>(); st.ninst = B.ninst.template as<int>();
     st.nkey = B.nkey.template as<unsigned long long>();
     return st;
@@ -204,13 +206,14 @@ struct Engine {
     StoreBufs<D>& B = S[k];
     B.hcap = hcap;
     B.ncap = ncap;
-    HGB_CUDA(B.hkey.alloc(hcap * 8)); HGB_CUDA(B.head.alloc(hcap * 4)); HGB_CUDA(B.pend.alloc(hcap * 4));
-    HGB_CUDA(B.pend_base.alloc(hcap * 4)); HGB_CUDA(B.klive.alloc(hcap * 4));
+    HGB_CUDA(B.hkey.alloc(hcap * 8)); HGB_CUDA(B.pend.alloc(hcap * 4));
+    HGB_CUDA(B.pend_base.alloc(hcap * 4)); HGB_CUDA(B.klive.alloc(hcap * 4)); HGB_CUDA(B.kloff.alloc(hcap * 8));
     HGB_CUDA(cudaMemsetAsync(B.klive.p, 0, hcap * 4, s));
     HGB_CUDA(cudaMemsetAsync(B.hkey.p, 0xff, hcap * 8, s));
-    HGB_CUDA(cudaMemsetAsync(B.head.p, 0xff, hcap * 4, s));
     HGB_CUDA(cudaMemsetAsync(B.pend.p, 0, hcap * 4, s));
-    HGB_CUDA(B.nzone.alloc(ncap * Z2 * 4)); HGB_CUDA(B.nnext.alloc(ncap * 4)); HGB_CUDA(B.nlevel.alloc(ncap * 4));
+    B.acap = std::max<long long>(1 << 16, 2 * ncap);
+    HGB_CUDA(B.arena.alloc((size_t)B.acap * 4));
+    HGB_CUDA(B.nzone.alloc(ncap * Z2 * 4)); HGB_CUDA(B.nlevel.alloc(ncap * 4));
     HGB_CUDA(B.ndead.alloc(ncap * 4)); HGB_CUDA(B.ninst.alloc(ncap * 4)); HGB_CUDA(B.nkey.alloc(ncap * 8));
     return HORA_OK;
   }
@@ -237,28 +240,53 @@ struct Engine {
     if ((hctl.nslots + extra) * 2 <= B.hcap) return HORA_OK;
     unsigned long long ncap = B.hcap;
     while ((hctl.nslots + extra) * 2 > ncap) ncap <<= 1;
-    DBuf k2, h2, p2, pb2, l2;
-    HGB_CUDA(k2.alloc(ncap * 8)); HGB_CUDA(h2.alloc(ncap * 4)); HGB_CUDA(p2.alloc(ncap * 4)); HGB_CUDA(pb2.alloc(ncap * 4));
+    DBuf k2, o2, p2, pb2, l2;
+    HGB_CUDA(k2.alloc(ncap * 8)); HGB_CUDA(o2.alloc(ncap * 8)); HGB_CUDA(p2.alloc(ncap * 4)); HGB_CUDA(pb2.alloc(ncap * 4));
     HGB_CUDA(l2.alloc(ncap * 4));
     HGB_CUDA(cudaMemsetAsync(l2.p, 0, ncap * 4, s));
     HGB_CUDA(cudaMemsetAsync(k2.p, 0xff, ncap * 8, s));
-    HGB_CUDA(cudaMemsetAsync(h2.p, 0xff, ncap * 4, s));
     HGB_CUDA(cudaMemsetAsync(p2.p, 0, ncap * 4, s));
     kt.begin(s);
-    k_rehash<<<1024, 256, 0, s>>>(B.hkey.template as<unsigned long long>(), B.head.template as<int>(),
+    k_rehash<<<1024, 256, 0, s>>>(B.hkey.template as<unsigned long long>(), B.kloff.template as<long long>(),
                                  B.klive.template as<int>(), B.hcap, k2.template as<unsigned long long>(),
-                                 h2.template as<int>(), l2.template as<int>(), ncap - 1, &dctl()->err);
+                                 o2.template as<long long>(), l2.template as<int>(), ncap - 1, &dctl()->err);
     kt.end(s, KT_OTHER);
     ++launches;
     HGB_CUDA(cudaGetLastError());
     HGB_CUDA(cudaStreamSynchronize(s));
     kt.collect();
     std::swap(B.hkey.p, k2.p); std::swap(B.hkey.bytes, k2.bytes);
-    std::swap(B.head.p, h2.p); std::swap(B.head.bytes, h2.bytes);
+    std::swap(B.kloff.p, o2.p); std::swap(B.kloff.bytes, o2.bytes);
     std::swap(B.pend.p, p2.p); std::swap(B.pend.bytes, p2.bytes);
     std::swap(B.pend_base.p, pb2.p); std::swap(B.pend_base.bytes, pb2.bytes);
     std::swap(B.klive.p, l2.p); std::swap(B.klive.bytes, l2.bytes);
     B.hcap = ncap;
+    return HORA_OK;
+  }
+  // Room in store k's key-list arena for `extra` more entries; when full, the live lists are
+  // copied into a fresh arena sized for twice the live zones plus the coming survivors.
+  int ensure_arena(int k, long long extra) {
+    StoreBufs<D>& B = S[k];
+    if ((long long)hctl.arena_alloc + extra <= B.acap) return HORA_OK;
+    const long long live = std::max<long long>(0, hctl.nlive);
+    const long long cap = std::max<long long>(1 << 20, 2 * (live + extra));
+    DBuf a2, n2;
+    HGB_CUDA(a2.alloc((size_t)cap * 4));
+    HGB_CUDA(n2.alloc(8));
+    HGB_CUDA(cudaMemsetAsync(n2.p, 0, 8, s));
+    kt.begin(s);
+    k_arena_compact<<<1024, 256, 0, s>>>(store(k), a2.template as<int>(), cap, n2.template as<unsigned long long>(),
+                                        dctl());
+    kt.end(s, KT_OTHER);
+    ++launches;
+    HGB_CUDA(cudaGetLastError());
+    HGB_CUDA(cudaMemcpyAsync(&dctl()->arena_alloc, n2.p, 8, cudaMemcpyDeviceToDevice, s));
+    HGB_CUDA(cudaStreamSynchronize(s));
+    std::swap(B.arena.p, a2.p); std::swap(B.arena.bytes, a2.bytes);
+    B.acap = cap;
+    const int rc = read_ctl();
+    if (rc) return rc;
+    if (hctl.err) { err = "key-list arena overflow"; return (int)hctl.err; }
     return HORA_OK;
   }
   // Room in the exact-zone table of store k for `extra` more zones (load factor at most 1/2);
@@ -295,11 +323,7 @@ struct Engine {
     if (hctl.err) { err = "device error in the graph probe"; return (int)hctl.err; }
     const long long nnew = (long long)hctl.nsurv;
     if ((rc = ensure_nodes(k, nnew))) return rc;
-    if (nnew > fcapb[cur ^ 1]) {
-      long long fc = fcapb[cur ^ 1];
-      while (nnew > fc) fc *= 2;
-      if ((rc = alloc_front(cur ^ 1, fc))) return rc;
-    }
+    if ((rc = grow_front(cur ^ 1, (long long)hctl.nfront, nnew))) return rc;
     const bool record = !roots;
     if (record && (rc = ensure_edges((long long)hctl.nedges + nsucc))) return rc;
     kt.begin(s);
@@ -324,7 +348,6 @@ struct Engine {
     while ((long long)hctl.nnodes + extra > nc) nc *= 2;
     const size_t used = hctl.nnodes;
     HGB_CUDA(B.nzone.grow(nc * Z2 * 4, used * Z2 * 4, s));
-    HGB_CUDA(B.nnext.grow(nc * 4, used * 4, s));
     HGB_CUDA(B.nlevel.grow(nc * 4, used * 4, s));
     HGB_CUDA(B.ndead.grow(nc * 4, used * 4, s));
     HGB_CUDA(B.ninst.grow(nc * 4, used * 4, s));
@@ -344,7 +367,7 @@ struct Engine {
   }
 
   int setup() {
-    t_start = std::chrono::steady_clock::now();
+    t_start = o.has_t_call ? o.t_call : std::chrono::steady_clock::now();
     ninst = (int)nets.size();
     int instbits = 0;
     while ((1 << instbits) < ninst) ++instbits;
@@ -418,6 +441,7 @@ struct Engine {
       if (!roots) ++level;
       HGB_CUDA(cudaMemcpyAsync(h_nfront.data(), is.nfront, ni8, cudaMemcpyDeviceToHost, s));
       HGB_CUDA(cudaMemsetAsync(is.nfront, 0, ni8, s));
+      HGB_CUDA(cudaMemsetAsync(&dctl()->nfront, 0, 8, s));
       HGB_CUDA(cudaStreamSynchronize(s));
       if (!roots)
         for (int q = 0; q < ninst; ++q)
@@ -428,82 +452,22 @@ struct Engine {
         for (int q = 0; q < ninst; ++q)
           if (!h_done[q] && !h_nfront[q] && t_fin[q] < 0 && nets[q]->kind != HORA_Q_LEADSTO) t_fin[q] = now;
       }
-      // ---- expand; re-run with a larger buffer on overflow (it writes nothing persistent)
-      const int* src = roots ? roots_src : S[k].nzone.template as<int>();
-      for (;;) {
-        HGB_CUDA(cudaMemsetAsync(dctl(), 0, kCtlLevelBytes, s));
-        HGB_CUDA(cudaMemcpyAsync(gen_backup.p, is.generated, ni8, cudaMemcpyDeviceToDevice, s));
-        kt.begin(s);
-        Level<D>::expand(V, is, front(cur), (int)nf, src, succ(), dctl(), roots ? 1 : 0, blocks, s);
-        kt.end(s, KT_EXPAND);
-        ++launches;
-        HGB_CUDA(cudaGetLastError());
-        if ((rc = read_ctl())) return rc;
-        if (!hctl.overflow) break;
-        HGB_CUDA(cudaMemcpyAsync(is.generated, gen_backup.p, ni8, cudaMemcpyDeviceToDevice, s));
-        if ((rc = alloc_succ((long long)(hctl.nsucc + hctl.nsucc / 4 + 1024)))) return rc;
-      }
-      if (hctl.err) { err = "device error in expand"; return (int)hctl.err; }
-      const long long nsucc = (long long)hctl.nsucc;
-      if ((rc = ensure_hash(k, (unsigned long long)nsucc))) return rc;
-      if (mode == 1) {   // exact-zone graph
-        if ((rc = graph_level(V, k, cur, nsucc, level, roots))) return rc;
-        nf = (long long)hctl.nfront;
-        cur ^= 1;
-        roots = false;
-        continue;
-      }
-      // ---- probe
-      if (nsucc > 0) {
-        kt.begin(s);
-        Level<D>::probe(V, is, succ(), store(k), dctl(), nsucc, mode, blocks, s);
-        kt.end(s, KT_PROBE);
-        ++launches;
-        HGB_CUDA(cudaGetLastError());
-      }
-      if ((rc = read_ctl())) return rc;
-      if (hctl.err) { err = "device error in probe"; return (int)hctl.err; }
-      const long long nsurv = (long long)hctl.nsurv, ntouched = (long long)hctl.ntouched;
-      // ---- deadlock goal on the survivors
-      if (mode == 0) {
-        bool any_dl = false;
-        for (int q = 0; q < ninst; ++q) any_dl |= (nets[q]->kind == HORA_Q_DEADLOCK && !h_done[q]);
-        if (any_dl && nsurv > 0) {
-          kt.begin(s);
-          Level<D>::deadlock(V, is, succ(), dctl(), nsurv, blocks, s);
-          kt.end(s, KT_DEADLOCK);
-          ++launches;
-          HGB_CUDA(cudaGetLastError());
-          if ((rc = read_ctl())) return rc;
-          if (hctl.err) { err = "deadlock test exceeded its escape table"; return (int)hctl.err; }
+      // ---- the level in chunks of whole instances, so that one chunk's successors fit the budget;
+      // an instance's level is never split, so its canonical insertion order is kept
+      std::vector<int> cuts{0};
+      {
+        const double fan = std::max(8.0, 2.0 * (double)gen_total / (double)std::max<unsigned long long>(1, exp_total));
+        const double budget = (double)o.succ_budget_bytes / (double)(Z2 * 4 + 96);
+        double acc = 0;
+        for (int q = 0; q < ninst; ++q) {
+          const double e = (double)h_nfront[q] * fan;
+          if (acc > 0 && acc + e > budget) { cuts.push_back(q); acc = 0; }
+          acc += e;
         }
+        cuts.push_back(ninst);
       }
-      // ---- room for the new nodes, the next frontier and the edges
-      if ((rc = ensure_nodes(k, nsurv))) return rc;
-      if (nsurv > fcapb[cur ^ 1]) {
-        long long fc = fcapb[cur ^ 1];
-        while (nsurv > fc) fc *= 2;
-        if ((rc = alloc_front(cur ^ 1, fc))) return rc;
-      }
-      if ((long long)hctl.nnodes + nsurv > ccap) {   // the merge gathers every touched key's chain
-        long long c = std::max<long long>(ccap, 1 << 16);
-        while ((long long)hctl.nnodes + nsurv > c) c *= 2;
-        HGB_CUDA(clist.alloc(c * 4));
-        ccap = c;
-      }
-      // ---- group + merge
-      if (ntouched > 0) {
-        kt.begin(s);
-        Level<D>::group(succ(), store(k), dctl(), nsucc, ntouched, s);
-        kt.end(s, KT_GROUP, 2);
-        kt.begin(s);
-        Level<D>::merge(V, is, succ(), store(k), front(cur ^ 1), dctl(), ntouched, level, merge_blocks, s);
-        kt.end(s, KT_MERGE);
-        launches += 3;
-        HGB_CUDA(cudaGetLastError());
-      }
-      if ((rc = read_ctl())) return rc;
-      if (hctl.err) { err = "device error in merge"; return (int)hctl.err; }
+      for (size_t c = 0; c + 1 < cuts.size(); ++c)
+        if ((rc = run_chunk(k, mode, cur, nf, level, roots, roots_src, V, cuts[c], cuts[c + 1]))) return rc;
       // ---- end of level: goals and the adaptive extrapolation (store 0 only)
       if (mode == 0) {
         HGB_CUDA(cudaMemcpyAsync(h_found.data(), is.found, ni4, cudaMemcpyDeviceToHost, s));
@@ -529,10 +493,102 @@ struct Engine {
           h2d += 2 * ni4;
         }
       }
+      if ((rc = read_ctl())) return rc;
       nf = (long long)hctl.nfront;
       cur ^= 1;
       roots = false;
     }
+    return HORA_OK;
+  }
+  unsigned long long gen_total = 0, exp_total = 0;   // successors / expanded states so far (fan-out)
+
+  // Room for `extra` more entries in frontier buffer b, keeping the `used` ones already there.
+  int grow_front(int b, long long used, long long extra) {
+    if (used + extra <= fcapb[b]) return HORA_OK;
+    long long fc = std::max<long long>(fcapb[b], 1 << 14);
+    while (used + extra > fc) fc *= 2;
+    HGB_CUDA(fkey[b].grow(fc * 8, used * 8, s)); HGB_CUDA(fnode[b].grow(fc * 4, used * 4, s));
+    HGB_CUDA(frank[b].grow(fc * 4, used * 4, s)); HGB_CUDA(finst[b].grow(fc * 4, used * 4, s));
+    fcapb[b] = fc;
+    return HORA_OK;
+  }
+
+  // One chunk of a level: the frontier entries of instances [i0, i1).
+  int run_chunk(int k, int mode, int cur, long long nf, int level, bool roots, const int* roots_src,
+                const NetView* V, int i0, int i1) {
+    const size_t ni8 = (size_t)ninst * 8;
+    InstState is = istate();
+    int rc;
+    // ---- expand; re-run with a larger buffer on overflow (it writes nothing persistent)
+    const int* src = roots ? roots_src : S[k].nzone.template as<int>();
+    for (;;) {
+      HGB_CUDA(cudaMemsetAsync(dctl(), 0, kCtlChunkBytes, s));
+      HGB_CUDA(cudaMemcpyAsync(gen_backup.p, is.generated, ni8, cudaMemcpyDeviceToDevice, s));
+      kt.begin(s);
+      Level<D>::expand(V, is, front(cur), (int)nf, src, succ(), dctl(), roots ? 1 : 0, i0, i1, blocks, s);
+      kt.end(s, KT_EXPAND);
+      ++launches;
+      HGB_CUDA(cudaGetLastError());
+      if ((rc = read_ctl())) return rc;
+      if (!hctl.overflow) break;
+      HGB_CUDA(cudaMemcpyAsync(is.generated, gen_backup.p, ni8, cudaMemcpyDeviceToDevice, s));
+      if ((rc = alloc_succ((long long)(hctl.nsucc + hctl.nsucc / 4 + 1024)))) return rc;
+    }
+    if (hctl.err) { err = "device error in expand"; return (int)hctl.err; }
+    const long long nsucc = (long long)hctl.nsucc;
+    if (!roots) {
+      gen_total += (unsigned long long)nsucc;
+      for (int q = i0; q < i1; ++q) exp_total += h_nfront[q];
+    }
+    if ((rc = ensure_hash(k, (unsigned long long)nsucc))) return rc;
+    if (mode == 1) return graph_level(V, k, cur, nsucc, level, roots);   // exact-zone graph
+    // ---- probe
+    if (nsucc > 0) {
+      kt.begin(s);
+      Level<D>::probe(V, is, succ(), store(k), dctl(), nsucc, mode, blocks, s);
+      kt.end(s, KT_PROBE);
+      ++launches;
+      HGB_CUDA(cudaGetLastError());
+    }
+    if ((rc = read_ctl())) return rc;
+    if (hctl.err) { err = "device error in probe"; return (int)hctl.err; }
+    const long long nsurv = (long long)hctl.nsurv, ntouched = (long long)hctl.ntouched;
+    // ---- deadlock goal on the survivors
+    bool any_dl = false;
+    for (int q = i0; q < i1; ++q) any_dl |= (nets[q]->kind == HORA_Q_DEADLOCK && !h_done[q]);
+    if (any_dl && nsurv > 0) {
+      kt.begin(s);
+      Level<D>::deadlock(V, is, succ(), dctl(), nsurv, blocks, s);
+      kt.end(s, KT_DEADLOCK);
+      ++launches;
+      HGB_CUDA(cudaGetLastError());
+      if ((rc = read_ctl())) return rc;
+      if (hctl.err) { err = "deadlock test exceeded its escape table"; return (int)hctl.err; }
+    }
+    // ---- room for the new nodes, their key lists and the next frontier
+    if ((rc = ensure_nodes(k, nsurv))) return rc;
+    if ((rc = ensure_arena(k, std::max<long long>(0, hctl.nlive) + nsurv))) return rc;
+    if ((rc = grow_front(cur ^ 1, (long long)hctl.nfront, nsurv))) return rc;
+    const long long clneed = std::max<long long>(0, hctl.nlive) + nsurv;   // touched keys' lists + survivors
+    if (clneed > ccap) {
+      long long c = std::max<long long>(ccap, 1 << 16);
+      while (clneed > c) c *= 2;
+      HGB_CUDA(clist.alloc(c * 4));
+      ccap = c;
+    }
+    // ---- group + merge
+    if (ntouched > 0) {
+      kt.begin(s);
+      Level<D>::group(succ(), store(k), dctl(), nsucc, ntouched, s);
+      kt.end(s, KT_GROUP, 2);
+      kt.begin(s);
+      Level<D>::merge(V, is, succ(), store(k), front(cur ^ 1), dctl(), ntouched, level, merge_blocks, s);
+      kt.end(s, KT_MERGE);
+      launches += 3;
+      HGB_CUDA(cudaGetLastError());
+    }
+    if ((rc = read_ctl())) return rc;
+    if (hctl.err) { err = "device error in merge"; return (int)hctl.err; }
     return HORA_OK;
   }
 
@@ -556,7 +612,8 @@ struct Engine {
     if ((rc = alloc_store(1, hcap, std::max<long long>(1 << 14, 2LL * ninst)))) return rc;
     // the p-nodes of phase 1 as a frontier
     if (n1 > fcapb[cur]) { if ((rc = alloc_front(cur, n1))) return rc; }
-    HGB_CUDA(cudaMemsetAsync(dctl(), 0, kCtlLevelBytes, s));
+    HGB_CUDA(cudaMemsetAsync(dctl(), 0, kCtlChunkBytes, s));
+    HGB_CUDA(cudaMemsetAsync(&dctl()->nfront, 0, 8, s));
     kt.begin(s);
     Level<D>::collect_p(dn.views_plain, store(0), n1, front(cur), dctl(), s);
     kt.end(s, KT_OTHER);

@@ -2,12 +2,15 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <memory>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "host.h"
@@ -422,6 +425,19 @@ namespace hgb {
 void set_last_error(const std::string& m) { g_last_error = m; }
 }  // namespace hgb
 
+// Run options common to every search. HORA_GB_SUCC_BUDGET (environment, bytes, read per call) caps
+// the device memory one chunk of a level's successors may take (default 8 GiB); a batch level above
+// it runs in chunks of whole instances.
+static RunOptions run_options(const volatile int32_t* cancel) {
+  RunOptions o;
+  o.cancel = cancel;
+  if (const char* e = std::getenv("HORA_GB_SUCC_BUDGET")) {
+    const long long b = std::atoll(e);
+    if (b > 0) o.succ_budget_bytes = (size_t)b;
+  }
+  return o;
+}
+
 static int32_t fail(int32_t rc, const std::string& msg) {
   g_last_error = msg;
   return rc;
@@ -460,8 +476,7 @@ static int32_t run_single(const hora_net_desc* net, int kind, const hora_pred_de
   if ((rc = ensure_device())) return rc;
   std::vector<const HostNet*> v{&H};
   std::vector<InstResult> res;
-  RunOptions o;
-  o.cancel = cancel;
+  const RunOptions o = run_options(cancel);
   rc = dispatch_group(H.dim, v, res, o, err);
   if (!res.empty()) stats_out(stats, res[0].st);
   if (rc) return fail(rc, err);
@@ -553,32 +568,55 @@ int32_t hora_gb_batch_run(int32_t n, const hora_net_desc* nets, const hora_query
     if (stats) { std::memset(&stats[k], 0, sizeof(hora_stats)); stats[k].status = r; }
     if (r == HORA_OK) by_dim[H[k].dim * 2 + (q.kind == HORA_Q_LEADSTO ? 1 : 0)].push_back(k);
   }
-  std::string err;
+  // the groups run concurrently, each on its own host thread and CUDA stream
+  std::vector<std::pair<int, std::vector<int>>> groups(by_dim.begin(), by_dim.end());
+  const int ng = (int)groups.size();
+  std::vector<int> grc(ng, HORA_OK);
+  std::vector<std::vector<InstResult>> gres(ng);
+  std::vector<std::string> gerr(ng);
+  std::vector<char> gskipped(ng, 0);
+  int dev = 0;
+  cudaGetDevice(&dev);
+  RunOptions o = run_options(cancel);
+  o.t_call = std::chrono::steady_clock::now();
+  o.has_t_call = true;
+  std::atomic<int> next{0};
+  auto worker = [&]() {
+    cudaSetDevice(dev);
+    for (int g; (g = next.fetch_add(1)) < ng;) {
+      if (cancel && *cancel) { gskipped[g] = 1; continue; }   // groups not yet started are not started
+      std::vector<const HostNet*> v;
+      for (int k : groups[g].second) v.push_back(&H[k]);
+      grc[g] = dispatch_group(groups[g].first / 2, v, gres[g], o, gerr[g]);
+    }
+  };
+  const int nthreads = std::max(1, std::min(ng, 16));
+  std::vector<std::thread> pool;
+  for (int i = 1; i < nthreads; ++i) pool.emplace_back(worker);
+  worker();
+  for (auto& t : pool) t.join();
   int first_err = HORA_OK;
   bool cancelled = false;
-  for (auto& kv : by_dim) {
-    if (cancel && *cancel) {   // groups not yet started are not started
-      for (int k : kv.second)
+  for (int g = 0; g < ng; ++g) {
+    const std::vector<int>& ks = groups[g].second;
+    if (gskipped[g]) {
+      for (int k : ks)
         if (stats) stats[k].status = HORA_E_CANCELLED;
       cancelled = true;
       continue;
     }
-    std::vector<const HostNet*> v;
-    for (int k : kv.second) v.push_back(&H[k]);
-    std::vector<InstResult> res;
-    RunOptions o;
-    o.cancel = cancel;
-    const int r = dispatch_group(kv.first / 2, v, res, o, err);
-    for (size_t q = 0; q < kv.second.size(); ++q) {
-      const int k = kv.second[q];
+    const int r = grc[g];
+    const std::vector<InstResult>& res = gres[g];
+    for (size_t q = 0; q < ks.size(); ++q) {
+      const int k = ks[q];
       const int ist = q < res.size() ? res[q].status : (r ? r : HORA_E_CUDA);
       if (q < res.size() && stats) stats[k] = res[q].st;
       if (stats) stats[k].status = ist;
-      verdicts[k] = ist == HORA_OK ? res[q].verdict : -1;
+      verdicts[k] = (ist == HORA_OK && q < res.size()) ? res[q].verdict : -1;
       cancelled |= ist == HORA_E_CANCELLED;
     }
     if (r == HORA_E_CANCELLED) continue;
-    if (r && !first_err) { first_err = r; g_last_error = err; }
+    if (r && !first_err) { first_err = r; g_last_error = gerr[g]; }
   }
   if (first_err == HORA_E_CUDA) return HORA_E_CUDA;
   return cancelled ? HORA_E_CANCELLED : HORA_OK;

@@ -1,6 +1,7 @@
 // host.h -- host-side model compilation and the per-dimension engine entry points.
 #pragma once
 #include <cstdint>
+#include <chrono>
 #include <string>
 #include <vector>
 
@@ -59,6 +60,9 @@ struct RunOptions {
   int blocks = 0;             // grid cap for the level kernels (0: derived from the SM count)
   const volatile int32_t* cancel = nullptr;
   size_t succ_cap0 = 1 << 16; // initial successor-buffer capacity
+  size_t succ_budget_bytes = size_t(8) << 30;  // a level's successors beyond this run in instance chunks
+  bool has_t_call = false;    // per-instance times count from t_call (the batch call) when set
+  std::chrono::steady_clock::time_point t_call{};
 };
 
 // Run a group of instances that share the DBM dimension D (one level-synchronous BFS over all of

@@ -10,14 +10,15 @@ namespace hgb {
 struct Store {
   // hash table of discrete keys
   unsigned long long* hkey;   // [cap] key | instance << inst_shift, kEmptyKey when free
-  int* head;                  // [cap] newest node of the key's antichain, -1 when none
   unsigned* pend;             // [cap] survivors pending for this key in the current level
   unsigned* pend_base;        // [cap] their segment offset
-  int* klive;                 // [cap] live zones of the key (its chain links only live zones)
+  int* klive;                 // [cap] live zones of the key's antichain ...
+  long long* kloff;           // [cap] ... listed oldest first at arena[kloff .. kloff + klive)
   unsigned long long hmask;   // cap - 1
+  int* arena;                 // key lists; a merged key's list is rewritten at a fresh offset
+  long long acap;
   // passed-store nodes
   int* nzone;                 // [ncap * D*D]
-  int* nnext;                 // [ncap]
   int* nlevel;                // [ncap]
   int* ndead;                 // [ncap]
   int* ninst;                 // [ncap]
@@ -77,8 +78,9 @@ struct Level {
   //       1 = exact-zone graph store with edges (leads-to phase 2)
   static void init(const NetView* nets, int ninst, const int* inst_dim_ok, Store st, Front out, InstState is,
                    Ctl* ctl, cudaStream_t s);
+  // expands the frontier entries of instances [i0, i1)
   static void expand(const NetView* nets, InstState is, Front fr, int nfront, const int* src_zone, Succ sc, Ctl* ctl,
-                     int roots, int blocks, cudaStream_t s);
+                     int roots, int i0, int i1, int blocks, cudaStream_t s);
   static void probe(const NetView* nets, InstState is, Succ sc, Store st, Ctl* ctl, long long nsucc, int mode,
                     int blocks, cudaStream_t s);
   static void deadlock(const NetView* nets, InstState is, Succ sc, Ctl* ctl, long long nsurv, int blocks,

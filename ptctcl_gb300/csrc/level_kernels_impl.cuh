@@ -85,9 +85,10 @@ __global__ void __launch_bounds__(kBlock) k_init(const NetView* nets, int ninst,
     if (slot < 0) { if (t.i == 0) atomicMax(&ctl->err, 4u); continue; }
     store_rows(t, z, st.nzone + node * D * D);
     if (t.i == 0) {
-      st.nnext[node] = -1; st.nlevel[node] = 0; st.ndead[node] = 0; st.ninst[node] = inst; st.nkey[node] = hk;
-      st.head[slot] = (int)node;
-      st.klive[slot] = 1;
+      st.nlevel[node] = 0; st.ndead[node] = 0; st.ninst[node] = inst; st.nkey[node] = hk;
+      const long long off = (long long)atomicAdd(&ctl->arena_alloc, 1ull);
+      if (off < st.acap) { st.arena[off] = (int)node; st.kloff[slot] = off; st.klive[slot] = 1; }
+      else atomicMax(&ctl->err, 4u);
       const unsigned long long f = atomicAdd(&ctl->nfront, 1ull);
       out.key[f] = hk; out.node[f] = (int)node; out.rank[f] = 0; out.inst[f] = inst;
       is.nkeys[inst] = 1; is.nlive[inst] = 1; is.nfront[inst] = 1;
@@ -103,12 +104,12 @@ __global__ void __launch_bounds__(kBlock) k_init(const NetView* nets, int ninst,
 // ---------------------------------------------------------------------------------------------
 template <int D>
 __global__ void __launch_bounds__(kBlock) k_expand(const NetView* nets, InstState is, Front fr, int nfront,
-                                                   const int* src_zone, Succ sc, Ctl* ctl, int roots) {
+                                                   const int* src_zone, Succ sc, Ctl* ctl, int roots, int i0, int i1) {
   Tile<D> t;
   if (!make_tile(t, threadIdx.x & 31)) return;
   for (long long f = tile_id<D>(); f < nfront; f += tile_count<D>()) {
     const int inst = fr.inst[f];
-    if (is.done[inst]) continue;
+    if (inst < i0 || inst >= i1 || is.done[inst]) continue;
     const NetView& N = nets[inst];
     const unsigned long long hk = fr.key[f];
     int locs[kMaxProcs], ints[kMaxInts];
@@ -189,22 +190,22 @@ __global__ void __launch_bounds__(kBlock) k_probe(const NetView* nets, InstState
     bool killed = false;
     unsigned long long nprobe = 0;
     if (!inserted && mode == 0) {
-      // the lanes take the stored zones of the chain in turn, each deciding a whole a_LU test
+      // the lanes take the key's live zones in turn, newest first, each deciding a whole a_LU test
       int Lall[D];
 #pragma unroll
       for (int x = 0; x < D; ++x) Lall[x] = t.shfl(Ly, x);
       const int* zs = sc.zone + s * D * D;
+      const int nl = __ldg(st.klive + slot);
+      const int* lst = st.arena + __ldg(st.kloff + slot);
       bool mine = false;
-      int pos = 0;
-      for (int n = __ldg(st.head + slot); n >= 0; n = __ldg(st.nnext + n), ++pos) {
-        const int lane_for = pos % D;
-        if (lane_for == t.i && !mine && !__ldg(st.ndead + n)) {
+      for (int k0 = nl - 1; k0 >= 0 && !killed; k0 -= D) {
+        const int k = k0 - t.i;
+        if (k >= 0) {
           ++nprobe;
-          mine = alu_le_lane<D>(zs, st.nzone + (long long)n * D * D, Lall, U);
+          mine = alu_le_lane<D>(zs, st.nzone + (long long)__ldg(lst + k) * D * D, Lall, U);
         }
-        if (lane_for == D - 1 && t.any(mine)) break;
+        killed = t.any(mine);
       }
-      killed = t.any(mine);
     }
     if (nprobe) atomicAdd(&ctl->probes, nprobe);
     if (t.i == 0) {
@@ -323,15 +324,12 @@ __device__ __forceinline__ void rank_segment(const Succ& sc, unsigned base, unsi
   }
 }
 
-// The key's live zones into clist, oldest first. Returns the list offset, or -1 on overflow.
-__device__ __forceinline__ long long gather_chain(const Succ& sc, const Store& st, int s, unsigned n, Ctl* ctl) {
+// Room in clist for the key's live zones and its survivors (one thread). Returns the offset, or -1
+// on overflow; the caller copies the key's list there.
+__device__ __forceinline__ long long alloc_clist(const Succ& sc, const Store& st, int s, unsigned n, Ctl* ctl) {
   const int c = st.klive[s];
   const long long cb = (long long)atomicAdd(&ctl->chain_alloc, (unsigned long long)(c + n));
   if (cb + c + n > sc.ccap) { atomicMax(&ctl->err, 4u); return -1; }
-  int k = c;
-  for (int m = st.head[s]; m >= 0 && k > 0; m = st.nnext[m])
-    if (!st.ndead[m]) sc.clist[cb + (--k)] = m;
-  if (k != 0) { atomicMax(&ctl->err, 4u); return -1; }
   return cb;
 }
 
@@ -347,18 +345,20 @@ __device__ __forceinline__ void finish_key(const Succ& sc, const Store& st, cons
     out.key[f] = hk; out.node[f] = m; out.rank[f] = r++; out.inst[f] = inst;
   }
   if (r) atomicAdd(&is.nfront[inst], (unsigned long long)r);
-  const bool was_empty = st.head[s] < 0;
-  int prev = -1, live = 0;
-  for (int k = 0; k < clen; ++k) {
-    const int m = cl[k];
-    if (m < 0) continue;
-    st.nnext[m] = prev;
-    prev = m;
-    ++live;
+  const bool was_empty = st.klive[s] == 0;
+  int live = 0;
+  for (int k = 0; k < clen; ++k) live += cl[k] >= 0 ? 1 : 0;
+  const long long off = (long long)atomicAdd(&ctl->arena_alloc, (unsigned long long)live);
+  if (off + live > st.acap) {
+    atomicMax(&ctl->err, 4u);
+  } else {
+    int w = 0;
+    for (int k = 0; k < clen; ++k)
+      if (cl[k] >= 0) st.arena[off + (w++)] = cl[k];
+    st.kloff[s] = off;
+    st.klive[s] = live;
   }
-  st.head[s] = prev;
-  st.klive[s] = live;
-  if (was_empty && prev >= 0) { atomicAdd(&ctl->nkeys, 1ull); atomicAdd(&is.nkeys[inst], 1ull); }
+  if (was_empty && live > 0) { atomicAdd(&ctl->nkeys, 1ull); atomicAdd(&is.nkeys[inst], 1ull); }
   if (dlive) {
     atomicAdd((unsigned long long*)&ctl->nlive, (unsigned long long)dlive);
     atomicAdd((unsigned long long*)&is.nlive[inst], (unsigned long long)dlive);
@@ -368,7 +368,6 @@ __device__ __forceinline__ void finish_key(const Succ& sc, const Store& st, cons
 
 // New node for zone rows `z` of key hk (metadata only; the caller writes the zone).
 __device__ __forceinline__ void node_meta(const Store& st, long long node, int level, int inst, unsigned long long hk) {
-  st.nnext[node] = -1;
   st.nlevel[node] = level;
   st.ndead[node] = 0;
   st.ninst[node] = inst;
@@ -404,9 +403,14 @@ __device__ void merge_key_block(const NetView* nets, const InstState& is, const 
   const NetView& N = nets[inst];
   rank_segment(sc, base, n, tid, blockDim.x);
   if (tid == 0) {
-    sh.cb = gather_chain(sc, st, s, n, ctl);
+    sh.cb = alloc_clist(sc, st, s, n, ctl);
     sh.clen = st.klive[s];
     sh.retired = 0;
+  }
+  __syncthreads();
+  if (sh.cb >= 0) {
+    const int* lst = st.arena + st.kloff[s];
+    for (int k = tid; k < sh.clen; k += blockDim.x) sc.clist[sh.cb + k] = lst[k];
   }
   if (warp == 0 && in_tile && t.base == 0) {
     int locs[kMaxProcs], ints[kMaxInts];
@@ -534,11 +538,15 @@ __device__ void merge_key_tile(const NetView* nets, const InstState& is, const S
   const NetView& N = nets[inst];
   rank_segment(sc, base, n, t.i, D);
   long long cb = 0;
-  if (t.i == 0) cb = gather_chain(sc, st, s, n, ctl);
+  if (t.i == 0) cb = alloc_clist(sc, st, s, n, ctl);
   cb = (long long)t.shfl64((unsigned long long)cb, 0);
-  t.sync();
-  if (cb < 0) return;
+  if (cb < 0) { t.sync(); return; }
   int clen = st.klive[s];
+  {
+    const int* lst = st.arena + st.kloff[s];
+    for (int k = t.i; k < clen; k += D) sc.clist[cb + k] = lst[k];
+  }
+  t.sync();
   const int clen0 = clen;
   volatile int* cl = sc.clist + cb;
   volatile int* vdead = st.ndead;
@@ -638,6 +646,20 @@ __global__ void __launch_bounds__(kMergeBlock) k_merge(const NetView* nets, Inst
   }
 }
 
+// Copy every key's list into a fresh arena (thread per slot), dropping the lists merges replaced.
+static __global__ void k_arena_compact(Store st, int* narena, long long ncap, unsigned long long* nalloc, Ctl* ctl) {
+  for (unsigned long long h = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; h <= st.hmask;
+       h += (unsigned long long)gridDim.x * blockDim.x) {
+    const int c = st.klive[h];
+    if (c <= 0) continue;
+    const long long off = (long long)atomicAdd(nalloc, (unsigned long long)c);
+    if (off + c > ncap) { atomicMax(&ctl->err, 4u); continue; }
+    const int* src = st.arena + st.kloff[h];
+    for (int k = 0; k < c; ++k) narena[off + k] = src[k];
+    st.kloff[h] = off;
+  }
+}
+
 // ---------------------------------------------------------------------------------------------
 // exact-zone graph store (leads-to graph mode): hash dedup instead of a per-key list scan
 // ---------------------------------------------------------------------------------------------
@@ -732,7 +754,6 @@ __global__ void __launch_bounds__(kBlock) k_graph_store(const NetView* nets, Ins
     load_rows(t, z, sc.zone + (long long)s * D * D);
     store_rows(t, z, st.nzone + node * D * D);
     if (t.i == 0) {
-      st.nnext[node] = -1;
       st.nlevel[node] = level;
       st.ndead[node] = 0;
       st.ninst[node] = inst;
@@ -950,9 +971,9 @@ void Level<D>::init(const NetView* nets, int ninst, const int* ok, Store st, Fro
 }
 template <int D>
 void Level<D>::expand(const NetView* nets, InstState is, Front fr, int nfront, const int* src_zone, Succ sc,
-                      Ctl* ctl, int roots, int blocks, cudaStream_t s) {
+                      Ctl* ctl, int roots, int i0, int i1, int blocks, cudaStream_t s) {
   constexpr int TPB = (kBlock / 32) * (32 / D);
-  k_expand<D><<<grid_for(nfront, TPB, blocks), kBlock, 0, s>>>(nets, is, fr, nfront, src_zone, sc, ctl, roots);
+  k_expand<D><<<grid_for(nfront, TPB, blocks), kBlock, 0, s>>>(nets, is, fr, nfront, src_zone, sc, ctl, roots, i0, i1);
 }
 template <int D>
 void Level<D>::probe(const NetView* nets, InstState is, Succ sc, Store st, Ctl* ctl, long long nsucc, int mode,

@@ -61,3 +61,29 @@ def test_server_rejects_over_budget():
         with pytest.raises(capi.HoraError) as ei:
             srv.submit(net, kind, p, q)
         assert ei.value.code == capi.E_BUDGET
+
+
+def test_batch_in_instance_chunks_matches_whole_levels():
+    """A 1-byte successor budget runs every level of the batch one instance at a time; verdicts and
+    counts stay those of the unchunked run."""
+    import json
+    import os
+    import subprocess
+    import sys
+    here = os.path.dirname(os.path.abspath(__file__))
+    code = ("import json, sys; sys.path.insert(0, %r); sys.path.insert(0, %r)\n"
+            "from test_gpu_serving import _mix\n"
+            "from ptctcl_gb300 import engine\n"
+            "v, st = engine.batch_run(_mix())\n"
+            "print(json.dumps([v, [{k: s[k] for k in %r} for s in st]]))\n") % (
+        os.path.dirname(here), here, COUNTS)
+    out = {}
+    for budget in ("", "1"):
+        env = dict(os.environ)
+        env.pop("HORA_GB_SUCC_BUDGET", None)
+        if budget:
+            env["HORA_GB_SUCC_BUDGET"] = budget
+        r = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=600)
+        assert r.returncode == 0, r.stderr[-2000:]
+        out[budget] = json.loads(r.stdout.strip().splitlines()[-1])
+    assert out[""] == out["1"]
