@@ -227,7 +227,8 @@ HORA_GB_API int32_t hora_gb_has_deadlock_noalloc(const hora_net_desc* net, int32
  * instance ran; per-instance failures are reported in stats[k].status and verdicts[k] = -1.
  * cancel (may be null) is polled between BFS levels: once it reads non-zero the call returns
  * HORA_E_CANCELLED, instances that already had their verdict keep it (status HORA_OK) and the
- * others report HORA_E_CANCELLED. */
+ * others report HORA_E_CANCELLED. Instances share three quarters of the free device memory; one
+ * whose passed store outgrows its share stops with status HORA_E_BUDGET and no verdict. */
 HORA_GB_API int32_t hora_gb_batch_run(int32_t n, const hora_net_desc* nets, const hora_query_desc* queries,
                           int32_t* verdicts, hora_stats* stats, const volatile int32_t* cancel);
 

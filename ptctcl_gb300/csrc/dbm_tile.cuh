@@ -271,6 +271,20 @@ __device__ __forceinline__ bool alu_le_lane(const int* Z, const int* Zp, const i
   return true;
 }
 
+// True if column 0 alone shows Z is not simulated by Zp (the x = 0 case of the a_LU test, which
+// decides most failing tests): some clock y has Zp[y][0] < Z[y][0] and Zp[y][0] - L_y < Z[0][0].
+template <int D>
+__device__ __forceinline__ bool alu_col0_witness(const int (&zc0)[D], const int* zpc0, const int (&L)[D]) {
+  bool w = false;
+#pragma unroll
+  for (int y = 1; y < D; ++y) {
+    if (L[y] == kAluNegInf) continue;
+    const int zp = __ldg(zpc0 + y);
+    w |= zp < zc0[y] && r_add(zp, r_lt(-L[y])) < zc0[0];
+  }
+  return w;
+}
+
 // Necessary condition for a convex union, from the clock bounds alone (netengine_metal.mm:455-465):
 // if the projections of a and b on some clock are separated by a gap, a ∪ b is not convex.
 template <int D>

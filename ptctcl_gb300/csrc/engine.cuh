@@ -77,6 +77,7 @@ struct Ctl {
   unsigned long long nlight;     // ... and by one tile
   unsigned long long heavy_next; // merge work counters
   unsigned long long light_next;
+  unsigned long long bm_need;    // words of the heavy keys' relation blocks
   unsigned int found;            // some instance hit its goal this level
   unsigned int overflow;         // expand output overflowed
   // per level
@@ -92,6 +93,6 @@ struct Ctl {
   unsigned int err;              // HORA_E_* raised on the device (table full, escape overflow)
   unsigned int flag;             // set by a fixpoint pass that changed something
 };
-constexpr unsigned long long kCtlChunkBytes = 9 * 8 + 2 * 4;
+constexpr unsigned long long kCtlChunkBytes = 10 * 8 + 2 * 4;
 
 }  // namespace hgb

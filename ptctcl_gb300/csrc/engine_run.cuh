@@ -102,7 +102,7 @@ template <int D>
 struct StoreBufs {
   DBuf hkey, pend, pend_base, klive, kloff;   // hash table
   DBuf arena;                                 // key lists
-  DBuf nzone, nlevel, ndead, ninst, nkey;     // nodes
+  DBuf nzone, ncol0, nlevel, ndead, ninst, nkey;   // nodes
   unsigned long long hcap = 0;
   long long ncap = 0, acap = 0;
 };
@@ -131,6 +131,10 @@ struct Engine {
   DBuf esrc, edst;
   long long ecap = 0;
   int merge_blocks = 0;         // resident blocks of the merge kernel (it schedules keys itself)
+  DBuf hv_n, hv_a, hv_cb, hv_bm, hv_bounds, hv_pool, hv_prefix;   // keys merged block-wide
+  long long hv_cap = 0, pool_cap = 0, prefix_cap = 0;
+  std::vector<int> h_hn, h_ha;
+  std::vector<long long> h_hbm, h_prefix;
   DBuf zw;                      // exact-zone table of the graph store
   unsigned long long zcap = 0;
   DBuf ctl, emode, done, found, generated, gen_backup, nlive, nkeys, nfront, probes;
@@ -142,6 +146,7 @@ struct Engine {
   std::vector<unsigned long long> h_nfront, h_nkeys, h_gen, explored, levels;
   std::vector<long long> h_nlive;
   std::vector<double> t_fin;   // per instance: seconds from the start to its verdict (-1: not yet)
+  std::vector<char> h_budget;  // per instance: stopped because the group's store budget ran out
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   std::chrono::steady_clock::time_point t_start;
 
@@ -160,7 +165,7 @@ struct Engine {
     st.klive = B.klive.template as<int>(); st.kloff = B.kloff.template as<long long>();
     st.hmask = B.hcap - 1;
     st.arena = B.arena.template as<int>(); st.acap = B.acap;
-    st.nzone = B.nzone.template as<int>();
+    st.nzone = B.nzone.template as<int>(); st.ncol0 = B.ncol0.template as<int>();
     st.nlevel = B.nlevel.template as<int>(); st.ndead = B.ndead.template as<int>(); st.ninst = B.ninst.template as<int>();
     st.nkey = B.nkey.template as<unsigned long long>();
     return st;
@@ -175,6 +180,9 @@ struct Engine {
     sc.heavy = sheavy.template as<int>(); sc.light = slight.template as<int>();
     sc.skh = sskh.template as<unsigned long long>(); sc.skl = sskl.template as<unsigned long long>();
     sc.clist = clist.template as<int>(); sc.ccap = ccap;
+    sc.hv.n = hv_n.template as<int>(); sc.hv.a = hv_a.template as<int>();
+    sc.hv.cb = hv_cb.template as<long long>(); sc.hv.bm = hv_bm.template as<long long>();
+    sc.hv.bounds = hv_bounds.template as<int>(); sc.hv.pool = hv_pool.template as<unsigned>();
     return sc;
   }
   Front front(int b) {
@@ -213,7 +221,7 @@ struct Engine {
     HGB_CUDA(cudaMemsetAsync(B.pend.p, 0, hcap * 4, s));
     B.acap = std::max<long long>(1 << 16, 2 * ncap);
     HGB_CUDA(B.arena.alloc((size_t)B.acap * 4));
-    HGB_CUDA(B.nzone.alloc(ncap * Z2 * 4)); HGB_CUDA(B.nlevel.alloc(ncap * 4));
+    HGB_CUDA(B.nzone.alloc(ncap * Z2 * 4)); HGB_CUDA(B.ncol0.alloc(ncap * D * 4)); HGB_CUDA(B.nlevel.alloc(ncap * 4));
     HGB_CUDA(B.ndead.alloc(ncap * 4)); HGB_CUDA(B.ninst.alloc(ncap * 4)); HGB_CUDA(B.nkey.alloc(ncap * 8));
     return HORA_OK;
   }
@@ -341,13 +349,22 @@ struct Engine {
     if (hctl.err) { err = "device error in the graph store"; return (int)hctl.err; }
     return HORA_OK;
   }
+  // Bytes one stored node takes (zone, its column 0, level, dead flag, instance, key).
+  static constexpr long long kNodeBytes = Z2 * 4 + D * 4 + 20;
+  // Nodes the store budget allows (unbounded without a budget).
+  long long budget_nodes() const {
+    return o.store_budget_bytes ? (long long)(o.store_budget_bytes / 2 / kNodeBytes) : (1LL << 40);
+  }
   int ensure_nodes(int k, long long extra) {
     StoreBufs<D>& B = S[k];
-    if ((long long)hctl.nnodes + extra <= B.ncap) return HORA_OK;
+    const long long need = (long long)hctl.nnodes + extra;
+    if (need <= B.ncap) return HORA_OK;
     long long nc = B.ncap;
-    while ((long long)hctl.nnodes + extra > nc) nc *= 2;
+    while (need > nc) nc *= 2;
+    if (nc > budget_nodes()) nc = std::max(need, budget_nodes());   // no doubling past the budget
     const size_t used = hctl.nnodes;
     HGB_CUDA(B.nzone.grow(nc * Z2 * 4, used * Z2 * 4, s));
+    HGB_CUDA(B.ncol0.grow(nc * D * 4, used * D * 4, s));
     HGB_CUDA(B.nlevel.grow(nc * 4, used * 4, s));
     HGB_CUDA(B.ndead.grow(nc * 4, used * 4, s));
     HGB_CUDA(B.ninst.grow(nc * 4, used * 4, s));
@@ -402,6 +419,7 @@ struct Engine {
     h_nfront.assign(ninst, 0); h_nkeys.assign(ninst, 0); h_gen.assign(ninst, 0);
     h_nlive.assign(ninst, 0); explored.assign(ninst, 0); levels.assign(ninst, 0);
     t_fin.assign(ninst, -1.0);
+    h_budget.assign(ninst, 0);
     HGB_CUDA(cudaEventCreate(&ev0));
     HGB_CUDA(cudaEventCreate(&ev1));
     HGB_CUDA(cudaEventRecord(ev0, s));
@@ -494,6 +512,7 @@ struct Engine {
         }
       }
       if ((rc = read_ctl())) return rc;
+      if (o.store_budget_bytes && (rc = enforce_budget(mode))) return rc;
       nf = (long long)hctl.nfront;
       cur ^= 1;
       roots = false;
@@ -501,6 +520,31 @@ struct Engine {
     return HORA_OK;
   }
   unsigned long long gen_total = 0, exp_total = 0;   // successors / expanded states so far (fan-out)
+  double last_fan = 0;                               // successors per frontier state, recent levels
+
+  // The group's store may hold about store_budget_bytes: an instance past a quarter of it stops,
+  // and once the store is past it every instance still running stops (status HORA_E_BUDGET, no
+  // verdict). The store grows by at most one level past the check.
+  int enforce_budget(int mode) {
+    const size_t ni4 = (size_t)ninst * 4, ni8 = (size_t)ninst * 8;
+    InstState is = istate();
+    if (mode == 1) {
+      HGB_CUDA(cudaMemcpyAsync(h_nlive.data(), is.nlive, ni8, cudaMemcpyDeviceToHost, s));
+      HGB_CUDA(cudaStreamSynchronize(s));
+    }
+    const double allowed = (double)budget_nodes();
+    const bool all = (double)hctl.nnodes > allowed;
+    bool changed = false;
+    for (int q = 0; q < ninst; ++q) {
+      if (h_done[q]) continue;
+      if (all || (double)h_nlive[q] > allowed / 4) { h_done[q] = 1; h_budget[q] = 1; changed = true; }
+    }
+    if (changed) {
+      HGB_CUDA(cudaMemcpyAsync(is.done, h_done.data(), ni4, cudaMemcpyHostToDevice, s));
+      h2d += ni4;
+    }
+    return HORA_OK;
+  }
 
   // Room for `extra` more entries in frontier buffer b, keeping the `used` ones already there.
   int grow_front(int b, long long used, long long extra) {
@@ -513,14 +557,75 @@ struct Engine {
     return HORA_OK;
   }
 
+  // Keys merged block-wide: sort and gather them, then precompute their pairwise relations.
+  int heavy_relations(const NetView* V, int k) {
+    const long long nh = (long long)hctl.nheavy;
+    if (nh == 0) return HORA_OK;
+    InstState is = istate();
+    const long long need = (long long)hctl.bm_need;
+    if (need > pool_cap) {
+      long long c = std::max<long long>(pool_cap, 1 << 20);
+      while (c < need) c *= 2;
+      HGB_CUDA(hv_pool.alloc((size_t)c * 4));
+      pool_cap = c;
+    }
+    h_hn.resize(nh); h_ha.resize(nh); h_hbm.resize(nh); h_prefix.resize(nh + 1);
+    HGB_CUDA(cudaMemcpyAsync(h_hn.data(), hv_n.p, nh * 4, cudaMemcpyDeviceToHost, s));
+    HGB_CUDA(cudaMemcpyAsync(h_ha.data(), hv_a.p, nh * 4, cudaMemcpyDeviceToHost, s));
+    HGB_CUDA(cudaMemcpyAsync(h_hbm.data(), hv_bm.p, nh * 8, cudaMemcpyDeviceToHost, s));
+    kt.begin(s);
+    Level<D>::heavy_prep(V, is, succ(), store(k), dctl(), nh, merge_blocks, s);
+    kt.end(s, KT_MERGE);
+    ++launches;
+    HGB_CUDA(cudaGetLastError());
+    HGB_CUDA(cudaStreamSynchronize(s));
+    d2h += nh * 16;
+    // tiles of 32 x 32 pairs: survivors x earlier survivors, survivors x old zones
+    long long tot = 0;
+    for (long long j = 0; j < nh; ++j) {
+      h_prefix[j] = tot;
+      if (h_hbm[j] < 0) continue;
+      const long long bq = (h_hn[j] + 31) / 32, ba = (h_ha[j] + 31) / 32;
+      tot += bq * (bq + 1) / 2 + bq * ba;
+    }
+    h_prefix[nh] = tot;
+    if (tot > 0) {
+      if (nh + 1 > prefix_cap) {
+        long long c = std::max<long long>(prefix_cap, 1 << 12);
+        while (c < nh + 1) c *= 2;
+        HGB_CUDA(hv_prefix.alloc(c * 8));
+        prefix_cap = c;
+      }
+      HGB_CUDA(cudaMemcpyAsync(hv_prefix.p, h_prefix.data(), (nh + 1) * 8, cudaMemcpyHostToDevice, s));
+      h2d += (nh + 1) * 8;
+      kt.begin(s);
+      if (Level<D>::heavy_pairs(V, succ(), store(k), hv_prefix.template as<long long>(), nh, tot, merge_blocks * 4, s)) {
+        err = "cannot size the relation pass's shared memory";
+        return HORA_E_CUDA;
+      }
+      kt.end(s, KT_MERGE);
+      ++launches;
+      HGB_CUDA(cudaGetLastError());
+      HGB_CUDA(cudaStreamSynchronize(s));   // the prefix buffer is host memory
+    }
+    return HORA_OK;
+  }
+
   // One chunk of a level: the frontier entries of instances [i0, i1).
   int run_chunk(int k, int mode, int cur, long long nf, int level, bool roots, const int* roots_src,
                 const NetView* V, int i0, int i1) {
     const size_t ni8 = (size_t)ninst * 8;
     InstState is = istate();
     int rc;
-    // ---- expand; re-run with a larger buffer on overflow (it writes nothing persistent)
+    // ---- expand; re-run with a larger buffer on overflow (it writes nothing persistent). The buffer
+    // is first sized for the chunk's frontier at the last level's fan-out.
     const int* src = roots ? roots_src : S[k].nzone.template as<int>();
+    if (!roots && last_fan > 0) {
+      unsigned long long nfc = 0;
+      for (int q = i0; q < i1; ++q) nfc += h_nfront[q];
+      const long long want = (long long)((double)nfc * last_fan * 1.15) + 1024;
+      if (want > scap && (rc = alloc_succ(want))) return rc;
+    }
     for (;;) {
       HGB_CUDA(cudaMemsetAsync(dctl(), 0, kCtlChunkBytes, s));
       HGB_CUDA(cudaMemcpyAsync(gen_backup.p, is.generated, ni8, cudaMemcpyDeviceToDevice, s));
@@ -537,11 +642,29 @@ struct Engine {
     if (hctl.err) { err = "device error in expand"; return (int)hctl.err; }
     const long long nsucc = (long long)hctl.nsucc;
     if (!roots) {
+      unsigned long long nfc = 0;
+      for (int q = i0; q < i1; ++q) nfc += h_nfront[q];
       gen_total += (unsigned long long)nsucc;
-      for (int q = i0; q < i1; ++q) exp_total += h_nfront[q];
+      exp_total += nfc;
+      if (nfc) last_fan = std::max(last_fan * 0.5, (double)nsucc / (double)nfc);
     }
     if ((rc = ensure_hash(k, (unsigned long long)nsucc))) return rc;
     if (mode == 1) return graph_level(V, k, cur, nsucc, level, roots);   // exact-zone graph
+    // ---- deadlock goal, on every successor before the probe: a successor the probe would drop lies
+    // in a_M of a stored zone, whose valuations were all tested, and a_M is a bisimulation, so the
+    // verdict and its level are those of testing the survivors only; an instance found here skips
+    // the probe and merge of this level
+    bool any_dl = false;
+    for (int q = i0; q < i1; ++q) any_dl |= (nets[q]->kind == HORA_Q_DEADLOCK && !h_done[q]);
+    if (any_dl && nsucc > 0) {
+      kt.begin(s);
+      Level<D>::deadlock(V, is, succ(), dctl(), nsucc, 1, blocks, s);
+      kt.end(s, KT_DEADLOCK);
+      ++launches;
+      HGB_CUDA(cudaGetLastError());
+      if ((rc = read_ctl())) return rc;
+      if (hctl.err) { err = "deadlock test exceeded its escape table"; return (int)hctl.err; }
+    }
     // ---- probe
     if (nsucc > 0) {
       kt.begin(s);
@@ -553,19 +676,34 @@ struct Engine {
     if ((rc = read_ctl())) return rc;
     if (hctl.err) { err = "device error in probe"; return (int)hctl.err; }
     const long long nsurv = (long long)hctl.nsurv, ntouched = (long long)hctl.ntouched;
-    // ---- deadlock goal on the survivors
-    bool any_dl = false;
-    for (int q = i0; q < i1; ++q) any_dl |= (nets[q]->kind == HORA_Q_DEADLOCK && !h_done[q]);
-    if (any_dl && nsurv > 0) {
-      kt.begin(s);
-      Level<D>::deadlock(V, is, succ(), dctl(), nsurv, blocks, s);
-      kt.end(s, KT_DEADLOCK);
-      ++launches;
-      HGB_CUDA(cudaGetLastError());
-      if ((rc = read_ctl())) return rc;
-      if (hctl.err) { err = "deadlock test exceeded its escape table"; return (int)hctl.err; }
+    if (ntouched > hv_cap) {   // per-key arrays of the grouping pass
+      long long c = std::max<long long>(hv_cap, 1 << 12);
+      while (c < ntouched) c *= 2;
+      HGB_CUDA(hv_n.alloc(c * 4)); HGB_CUDA(hv_a.alloc(c * 4)); HGB_CUDA(hv_cb.alloc(c * 8));
+      HGB_CUDA(hv_bm.alloc(c * 8)); HGB_CUDA(hv_bounds.alloc(c * 2 * D * 4));
+      hv_cap = c;
     }
-    // ---- room for the new nodes, their key lists and the next frontier
+    // ---- room for the new nodes, their key lists and the next frontier; a chunk that would take
+    // the store past its budget stops its instances instead (HORA_E_BUDGET)
+    if (o.store_budget_bytes && (long long)hctl.nnodes + nsurv > budget_nodes()) {
+      bool changed = false;
+      for (int q = i0; q < i1; ++q)
+        if (!h_done[q]) { h_done[q] = 1; h_budget[q] = 1; changed = true; }
+      if (changed) {
+        HGB_CUDA(cudaMemcpyAsync(is.done, h_done.data(), (size_t)ninst * 4, cudaMemcpyHostToDevice, s));
+        h2d += (size_t)ninst * 4;
+      }
+      // their pending survivors are dropped: the merge skips finished instances and resets the slots
+      if (ntouched > 0) {
+        kt.begin(s);
+        Level<D>::group(succ(), store(k), dctl(), nsucc, ntouched, s);
+        kt.end(s, KT_GROUP, 2);
+        Level<D>::merge(V, is, succ(), store(k), front(cur ^ 1), dctl(), ntouched, level, merge_blocks, s);
+        launches += 3;
+        HGB_CUDA(cudaGetLastError());
+      }
+      return read_ctl();
+    }
     if ((rc = ensure_nodes(k, nsurv))) return rc;
     if ((rc = ensure_arena(k, std::max<long long>(0, hctl.nlive) + nsurv))) return rc;
     if ((rc = grow_front(cur ^ 1, (long long)hctl.nfront, nsurv))) return rc;
@@ -581,10 +719,14 @@ struct Engine {
       kt.begin(s);
       Level<D>::group(succ(), store(k), dctl(), nsucc, ntouched, s);
       kt.end(s, KT_GROUP, 2);
+      launches += 2;
+      HGB_CUDA(cudaGetLastError());
+      if ((rc = read_ctl())) return rc;
+      if ((rc = heavy_relations(V, k))) return rc;
       kt.begin(s);
       Level<D>::merge(V, is, succ(), store(k), front(cur ^ 1), dctl(), ntouched, level, merge_blocks, s);
       kt.end(s, KT_MERGE);
-      launches += 3;
+      launches += 1;
       HGB_CUDA(cudaGetLastError());
     }
     if ((rc = read_ctl())) return rc;
@@ -693,7 +835,8 @@ struct Engine {
     res.assign(ninst, InstResult{});
     for (int k = 0; k < ninst; ++k) {
       InstResult& r = res[k];
-      const int ist = (status == HORA_E_CANCELLED && !leadsto && t_fin[k] >= 0) ? HORA_OK : status;
+      int ist = (status == HORA_E_CANCELLED && !leadsto && t_fin[k] >= 0) ? HORA_OK : status;
+      if (h_budget[k] && (ist == HORA_OK || ist == HORA_E_CANCELLED)) ist = HORA_E_BUDGET;
       r.status = ist;
       r.verdict = leadsto ? (h_found[k] ? 0 : 1) : (h_found[k] ? 1 : 0);
       r.st.explored = explored[k];

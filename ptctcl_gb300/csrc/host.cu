@@ -552,6 +552,17 @@ int32_t hora_gb_has_deadlock(const hora_net_desc* net, int32_t n, const int32_t*
 
 int32_t hora_gb_batch_run(int32_t n, const hora_net_desc* nets, const hora_query_desc* queries, int32_t* verdicts,
                           hora_stats* stats, const volatile int32_t* cancel) {
+  return hgb::run_batch(n, nets, queries, verdicts, stats, cancel, 0);
+}
+
+}  // extern "C"
+
+namespace hgb {
+
+// The batched form with an explicit store budget for the whole call (0: three quarters of the free
+// device memory), shared by the concurrent groups.
+int32_t run_batch(int32_t n, const hora_net_desc* nets, const hora_query_desc* queries, int32_t* verdicts,
+                  hora_stats* stats, const volatile int32_t* cancel, size_t store_budget) {
   g_last_error.clear();
   if (n < 0 || (n > 0 && (!nets || !queries || !verdicts))) return fail(HORA_E_INVALID, "bad arguments");
   int rc = ensure_device();
@@ -580,6 +591,16 @@ int32_t hora_gb_batch_run(int32_t n, const hora_net_desc* nets, const hora_query
   RunOptions o = run_options(cancel);
   o.t_call = std::chrono::steady_clock::now();
   o.has_t_call = true;
+  const int nthreads = std::max(1, std::min(ng, 16));
+  {
+    // the concurrent groups share three quarters of the free device memory
+    size_t fr = 0, tot = 0;
+    if (!store_budget && cudaMemGetInfo(&fr, &tot) == cudaSuccess && fr > 0) store_budget = (size_t)((double)fr * 0.75);
+    if (store_budget) {
+      o.store_budget_bytes = store_budget / nthreads;
+      o.succ_budget_bytes = std::min(o.succ_budget_bytes, std::max<size_t>(o.store_budget_bytes / 4, 64 << 20));
+    }
+  }
   std::atomic<int> next{0};
   auto worker = [&]() {
     cudaSetDevice(dev);
@@ -590,7 +611,6 @@ int32_t hora_gb_batch_run(int32_t n, const hora_net_desc* nets, const hora_query
       grc[g] = dispatch_group(groups[g].first / 2, v, gres[g], o, gerr[g]);
     }
   };
-  const int nthreads = std::max(1, std::min(ng, 16));
   std::vector<std::thread> pool;
   for (int i = 1; i < nthreads; ++i) pool.emplace_back(worker);
   worker();
@@ -622,6 +642,6 @@ int32_t hora_gb_batch_run(int32_t n, const hora_net_desc* nets, const hora_query
   return cancelled ? HORA_E_CANCELLED : HORA_OK;
 }
 
-// ---- serving form: implemented in server.cu ----
+}  // namespace hgb
 
-}  // extern "C"
+// ---- serving form: implemented in server.cu ----

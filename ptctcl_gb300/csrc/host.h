@@ -49,6 +49,11 @@ int upload_nets(const std::vector<const HostNet*>& nets, int inst_shift, DeviceN
 void build_blob(const HostNet& H, std::vector<int32_t>& blob, std::vector<size_t>& offs);
 NetView make_view(const HostNet& H, const int32_t* device_blob, const std::vector<size_t>& offs, int inst_shift);
 
+// The batched form (hora_gb_batch_run) with an explicit store budget for the whole call, in bytes
+// (0: three quarters of the free device memory).
+int32_t run_batch(int32_t n, const hora_net_desc* nets, const hora_query_desc* queries, int32_t* verdicts,
+                  hora_stats* stats, const volatile int32_t* cancel, size_t store_budget);
+
 // Result of one instance.
 struct InstResult {
   int status = HORA_OK;
@@ -61,6 +66,7 @@ struct RunOptions {
   const volatile int32_t* cancel = nullptr;
   size_t succ_cap0 = 1 << 16; // initial successor-buffer capacity
   size_t succ_budget_bytes = size_t(8) << 30;  // a level's successors beyond this run in instance chunks
+  size_t store_budget_bytes = 0;  // 0: unbounded; else instances stop with HORA_E_BUDGET past it
   bool has_t_call = false;    // per-instance times count from t_call (the batch call) when set
   std::chrono::steady_clock::time_point t_call{};
 };

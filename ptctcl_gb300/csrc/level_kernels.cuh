@@ -19,6 +19,7 @@ struct Store {
   long long acap;
   // passed-store nodes
   int* nzone;                 // [ncap * D*D]
+  int* ncol0;                 // [ncap * D] column 0 of each zone (the probe's first test)
   int* nlevel;                // [ncap]
   int* ndead;                 // [ncap]
   int* ninst;                 // [ncap]
@@ -28,6 +29,14 @@ struct Edges {                // zone-graph edges (leads-to graph mode)
   int* src;
   int* dst;
   long long cap;
+};
+struct HeavyKeys {            // per key merged block-wide (index j of Succ::heavy)
+  int* n;                     // survivors
+  int* a;                     // live zones before the level
+  long long* cb;              // clist offset of the key's list
+  long long* bm;              // offset of its relation block in pool, -1 when it has none
+  int* bounds;                // [2*D] per key: L[] then U[]
+  unsigned* pool;             // relation blocks
 };
 struct Succ {                 // successors of the current level
   unsigned long long* key;    // hash key
@@ -49,6 +58,7 @@ struct Succ {                 // successors of the current level
   long long cap;
   int* clist;                 // per touched key, its live zones gathered for the merge
   long long ccap;
+  HeavyKeys hv;
 };
 struct ZTab {                 // exact-zone table of the graph store: one word per slot,
   unsigned long long* w;      // (32-bit zone hash << 32) | ref, 0 when free; ref = node id, or
@@ -83,12 +93,17 @@ struct Level {
                      int roots, int i0, int i1, int blocks, cudaStream_t s);
   static void probe(const NetView* nets, InstState is, Succ sc, Store st, Ctl* ctl, long long nsucc, int mode,
                     int blocks, cudaStream_t s);
-  static void deadlock(const NetView* nets, InstState is, Succ sc, Ctl* ctl, long long nsurv, int blocks,
+  static void deadlock(const NetView* nets, InstState is, Succ sc, Ctl* ctl, long long n, int all, int blocks,
                        cudaStream_t s);
   static void group(Succ sc, Store st, Ctl* ctl, long long nsucc, long long ntouched, cudaStream_t s);
   static void merge(const NetView* nets, InstState is, Succ sc, Store st, Front out, Ctl* ctl, long long ntouched,
                     int level, int blocks, cudaStream_t s);
   static int merge_blocks_per_sm();
+  // keys merged block-wide: sort + gather + bounds, then their pairwise relations
+  static void heavy_prep(const NetView* nets, InstState is, Succ sc, Store st, Ctl* ctl, long long nheavy,
+                         int blocks, cudaStream_t s);
+  static int heavy_pairs(const NetView* nets, Succ sc, Store st, const long long* prefix, long long nheavy,
+                         long long ntiles, int blocks, cudaStream_t s);
   // exact-zone graph store (leads-to graph mode): deduplicate the successors against the store and
   // each other by zone hash, store the new zones, record one edge per successor
   static void graph_probe(const NetView* nets, InstState is, Succ sc, Store st, ZTab zt, Ctl* ctl, long long nsucc,

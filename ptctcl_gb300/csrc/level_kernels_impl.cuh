@@ -84,6 +84,7 @@ __global__ void __launch_bounds__(kBlock) k_init(const NetView* nets, int ninst,
     node = (long long)t.shfl64((unsigned long long)node, 0);
     if (slot < 0) { if (t.i == 0) atomicMax(&ctl->err, 4u); continue; }
     store_rows(t, z, st.nzone + node * D * D);
+    st.ncol0[node * D + t.i] = z[0];
     if (t.i == 0) {
       st.nlevel[node] = 0; st.ndead[node] = 0; st.ninst[node] = inst; st.nkey[node] = hk;
       const long long off = (long long)atomicAdd(&ctl->arena_alloc, 1ull);
@@ -195,6 +196,9 @@ __global__ void __launch_bounds__(kBlock) k_probe(const NetView* nets, InstState
 #pragma unroll
       for (int x = 0; x < D; ++x) Lall[x] = t.shfl(Ly, x);
       const int* zs = sc.zone + s * D * D;
+      int zc0[D];   // column 0 of the successor: x_y - x_0 bounds
+#pragma unroll
+      for (int y = 0; y < D; ++y) zc0[y] = t.shfl(z[0], y);
       const int nl = __ldg(st.klive + slot);
       const int* lst = st.arena + __ldg(st.kloff + slot);
       bool mine = false;
@@ -202,7 +206,10 @@ __global__ void __launch_bounds__(kBlock) k_probe(const NetView* nets, InstState
         const int k = k0 - t.i;
         if (k >= 0) {
           ++nprobe;
-          mine = alu_le_lane<D>(zs, st.nzone + (long long)__ldg(lst + k) * D * D, Lall, U);
+          const int m = __ldg(lst + k);
+          // most failing tests fail on column 0: decide those from the stored zone's column copy
+          mine = !alu_col0_witness<D>(zc0, st.ncol0 + (long long)m * D, Lall) &&
+                 alu_le_lane<D>(zs, st.nzone + (long long)m * D * D, Lall, U);
         }
         killed = t.any(mine);
       }
@@ -223,17 +230,18 @@ __global__ void __launch_bounds__(kBlock) k_probe(const NetView* nets, InstState
 }
 
 // ---------------------------------------------------------------------------------------------
-// deadlock: the goal test of the deadlock query, on the probe's survivors
+// deadlock: the goal test of the deadlock query, on every successor of the level (all = 1) or on
+// the probe's survivors
 // ---------------------------------------------------------------------------------------------
 template <int D>
 __global__ void __launch_bounds__(kBlock) k_deadlock(const NetView* nets, InstState is, Succ sc, Ctl* ctl,
-                                                     long long nsurv) {
+                                                     long long n, int all) {
   Tile<D> t;
   if (!make_tile(t, threadIdx.x & 31)) return;
   DlScratch<D> S;
   const int ishift = nets[0].inst_shift;
-  for (long long w = tile_id<D>(); w < nsurv; w += tile_count<D>()) {
-    const int s = sc.surv[w];
+  for (long long w = tile_id<D>(); w < n; w += tile_count<D>()) {
+    const int s = all ? (int)w : sc.surv[w];
     const unsigned long long hk = sc.key[s];
     const int inst = (int)(hk >> ishift);
     const NetView& N = nets[inst];
@@ -255,14 +263,30 @@ __global__ void __launch_bounds__(kBlock) k_deadlock(const NetView* nets, InstSt
 // survivors against a long antichain) go to the block-wide merge, the rest to the tile merge
 // ---------------------------------------------------------------------------------------------
 constexpr long long kHeavyMerge = 2048;   // survivors x (live zones + survivors) of a block-wide key
+constexpr int kRelMaxN = 1 << 16;         // larger keys fold without precomputed relations
+
+// Words of a heavy key's relation block (layout at k_heavy_prep).
+__device__ __forceinline__ long long rel_words(long long n, long long a) {
+  return 3 * n + n * ((n + 31) / 32 + (a + 31) / 32);
+}
 
 static __global__ void k_seg_alloc(Succ sc, Store st, Ctl* ctl, long long ntouched) {
   for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < ntouched; j += (long long)gridDim.x * blockDim.x) {
     const int s = sc.touched[j];
     const unsigned n = st.pend[s];
     st.pend_base[s] = (unsigned)atomicAdd(&ctl->seg_alloc, (unsigned long long)n);
-    if ((long long)n * ((long long)st.klive[s] + n) >= kHeavyMerge) sc.heavy[atomicAdd(&ctl->nheavy, 1ull)] = s;
-    else sc.light[atomicAdd(&ctl->nlight, 1ull)] = s;
+    const int a = st.klive[s];
+    if (n >= 2 && (long long)n * ((long long)a + n) >= kHeavyMerge) {
+      const unsigned long long j = atomicAdd(&ctl->nheavy, 1ull);
+      sc.heavy[j] = s;
+      sc.hv.n[j] = (int)n;
+      sc.hv.a[j] = a;
+      sc.hv.cb[j] = -1;
+      sc.hv.bm[j] = n <= (unsigned)kRelMaxN
+                        ? (long long)atomicAdd(&ctl->bm_need, (unsigned long long)rel_words(n, a)) : -1;
+    } else {
+      sc.light[atomicAdd(&ctl->nlight, 1ull)] = s;
+    }
   }
 }
 static __global__ void k_seg_scatter(Succ sc, Store st, long long nsucc) {
@@ -380,18 +404,226 @@ struct MergeShared {
   int L[D], U[D];       // the key's per-clock bounds
   int win[kMergeScan];  // list positions of the newest live zones, newest first
   long long cb;
-  int nw, best, node, retired, clen, job;
+  int nw, best, node, retired, clen, job, unioned, nhull;
 };
 
-// One key merged by a whole block.
+// ---------------------------------------------------------------------------------------------
+// Keys merged block-wide ("heavy"): their pairwise a_LU relations are precomputed by a grid-wide
+// pass, so the ordered fold reads its drop and retire decisions from bitmaps.
+//
+// Relation block of heavy key j at pool + hv.bm[j] (n survivors in canonical order, a live zones
+// before the level):
+//   drop[n]      1 if s_q ≼ s_q' for some q' < q
+//   tpos[n]      list position (past the old zones) where s_q was stored unchanged, else -1
+//   hull[n]      list positions of zones stored as convex hulls (the first nhull entries)
+//   rt[n][rtw]   bit q' of row q: s_q' ≼ s_q, q' < q              (rtw = ceil(n / 32))
+//   r0[n][r0w]   bit m of row q: old zone m ≼ s_q                  (r0w = ceil(a / 32))
+// Why drop[] decides the fold's first test exactly: if s_q ≼ s_q' for an earlier q', then s_q'
+// was stored (and a zone stored this level that simulates it is still live: zones only die when
+// a later one simulates or contains them), or s_q' was dropped because such a zone simulated it;
+// simulation is transitive, so s_q is dropped either way. Conversely a live zone stored this
+// level that simulates s_q is either some s_q' stored unchanged (then drop[q] is set) or a hull,
+// which the fold tests directly.
+// ---------------------------------------------------------------------------------------------
+
+// Canonical order of a long segment by one block: chunks of kSortChunk entries are bitonic-sorted in
+// shared memory and written back in place (keys and successor indices), then every entry's final
+// rank is its rank in its chunk plus, per other chunk, the number of smaller keys (binary search).
+// The order keys of one segment are distinct (parent key, parent rank, emission ordinal).
+constexpr int kSortChunk = 1024;
+
+__device__ __forceinline__ bool ok_less(unsigned long long ah, unsigned long long al, unsigned long long bh,
+                                        unsigned long long bl) {
+  return ah < bh || (ah == bh && al < bl);
+}
+
+static __device__ void sort_segment_block(const Succ& sc, unsigned base, unsigned n) {
+  __shared__ unsigned long long skh[kSortChunk], skl[kSortChunk];
+  __shared__ int sv[kSortChunk];
+  const unsigned nc = (n + kSortChunk - 1) / kSortChunk;
+  for (unsigned c = 0; c < nc; ++c) {
+    const unsigned c0 = c * kSortChunk, len = min((unsigned)kSortChunk, n - c0);
+    for (unsigned e = threadIdx.x; e < kSortChunk; e += blockDim.x) {
+      if (e < len) { skh[e] = sc.skh[base + c0 + e]; skl[e] = sc.skl[base + c0 + e]; sv[e] = sc.seg[base + c0 + e]; }
+      else { skh[e] = ~0ull; skl[e] = ~0ull; sv[e] = -1; }
+    }
+    __syncthreads();
+    for (unsigned k = 2; k <= (unsigned)kSortChunk; k <<= 1)
+      for (unsigned jj = k >> 1; jj > 0; jj >>= 1) {
+        for (unsigned i = threadIdx.x; i < (unsigned)kSortChunk; i += blockDim.x) {
+          const unsigned l = i ^ jj;
+          if (l > i) {
+            const bool up = (i & k) == 0;
+            const bool gt = ok_less(skh[l], skl[l], skh[i], skl[i]);
+            if (gt == up) {
+              const unsigned long long th = skh[i], tl = skl[i];
+              const int tv = sv[i];
+              skh[i] = skh[l]; skl[i] = skl[l]; sv[i] = sv[l];
+              skh[l] = th; skl[l] = tl; sv[l] = tv;
+            }
+          }
+        }
+        __syncthreads();
+      }
+    for (unsigned e = threadIdx.x; e < len; e += blockDim.x) {
+      sc.skh[base + c0 + e] = skh[e]; sc.skl[base + c0 + e] = skl[e]; sc.seg[base + c0 + e] = sv[e];
+    }
+    __syncthreads();
+  }
+  for (unsigned p = threadIdx.x; p < n; p += blockDim.x) {
+    const unsigned c = p / kSortChunk;
+    const unsigned long long kh = sc.skh[base + p], kl = sc.skl[base + p];
+    unsigned r = p - c * kSortChunk;
+    for (unsigned o = 0; o < nc; ++o) {
+      if (o == c) continue;
+      unsigned lo = o * kSortChunk, hi = min((o + 1) * kSortChunk, n);   // first entry not less than key
+      while (lo < hi) {
+        const unsigned mid = (lo + hi) >> 1;
+        if (ok_less(sc.skh[base + mid], sc.skl[base + mid], kh, kl)) lo = mid + 1; else hi = mid;
+      }
+      r += lo - o * kSortChunk;
+    }
+    sc.sorted[base + r] = sc.seg[base + p];
+  }
+}
+
+// Sort the key's survivors, gather its live list, its bounds, and clear its relation block.
+template <int D>
+__global__ void __launch_bounds__(kMergeBlock) k_heavy_prep(const NetView* nets, InstState is, Succ sc, Store st,
+                                                            Ctl* ctl, long long nheavy) {
+  Tile<D> t;
+  const bool in_tile = make_tile(t, threadIdx.x & 31);
+  const int ishift = nets[0].inst_shift;
+  for (long long j = blockIdx.x; j < nheavy; j += gridDim.x) {
+    const int s = sc.heavy[j];
+    const unsigned long long hk = st.hkey[s];
+    const int inst = (int)(hk >> ishift);
+    if (is.found[inst] || is.done[inst]) continue;
+    const int n = sc.hv.n[j], a = sc.hv.a[j];
+    const unsigned base = st.pend_base[s];
+    if (n <= 128) rank_segment(sc, base, (unsigned)n, threadIdx.x, blockDim.x);
+    else sort_segment_block(sc, base, (unsigned)n);
+    __shared__ long long cb_sh;
+    if (threadIdx.x == 0) { cb_sh = alloc_clist(sc, st, s, (unsigned)n, ctl); sc.hv.cb[j] = cb_sh; }
+    __syncthreads();
+    const long long cb = cb_sh;
+    if (cb >= 0) {
+      const int* lst = st.arena + st.kloff[s];
+      for (int k = threadIdx.x; k < a; k += blockDim.x) sc.clist[cb + k] = lst[k];
+    }
+    if (threadIdx.x < 32 && in_tile && t.base == 0) {
+      int locs[kMaxProcs], ints[kMaxInts];
+      key_decode(nets[inst], key_part(hk, ishift), locs, ints);
+      int Ly, U[D];
+      key_bounds(nets[inst], t, locs, Ly, U);
+      sc.hv.bounds[j * 2 * D + t.i] = Ly;
+      sc.hv.bounds[j * 2 * D + D + t.i] = U[t.i];
+    }
+    const long long bm = sc.hv.bm[j];
+    if (bm >= 0) {
+      unsigned* R = sc.hv.pool + bm;
+      const long long w = rel_words(n, a);
+      for (long long k = threadIdx.x; k < w; k += blockDim.x) R[k] = (k >= n && k < 2LL * n) ? 0xffffffffu : 0u;
+    }
+    __syncthreads();
+  }
+}
+
+// One 32 x 32 tile of pairs per block iteration: survivors x earlier survivors, or survivors x old
+// zones. Zones are staged in shared memory (row stride made odd against bank conflicts); lane c of
+// a warp tests column c against the warp's rows and a ballot writes the 32 relation bits at once.
+template <int D>
+__global__ void __launch_bounds__(kMergeBlock) k_heavy_pairs(const NetView* nets, Succ sc, Store st,
+                                                             const long long* prefix, long long nheavy,
+                                                             long long ntiles) {
+  constexpr int Z2 = D * D;
+  constexpr int P = (Z2 & 1) ? Z2 : Z2 + 1;
+  extern __shared__ int smz[];
+  int* A = smz;            // 32 survivors (rows)
+  int* B = smz + 32 * P;   // 32 columns
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  for (long long tt = blockIdx.x; tt < ntiles; tt += gridDim.x) {
+    long long lo = 0, hi = nheavy;   // prefix[lo] <= tt < prefix[lo + 1]
+    while (hi - lo > 1) {
+      const long long mid = (lo + hi) >> 1;
+      if (prefix[mid] <= tt) lo = mid; else hi = mid;
+    }
+    const long long j = lo;
+    const int n = sc.hv.n[j], a = sc.hv.a[j];
+    const long long bm = sc.hv.bm[j], cb = sc.hv.cb[j];
+    const int s = sc.heavy[j];
+    const unsigned base = st.pend_base[s];
+    const long long bq = (n + 31) / 32, ba = (a + 31) / 32, ss = bq * (bq + 1) / 2;
+    const long long u = tt - prefix[j];
+    long long bi, bj;
+    const bool pairs_ss = u < ss;
+    if (pairs_ss) {
+      bi = (long long)((sqrt(8.0 * (double)u + 1.0) - 1.0) * 0.5);
+      while (bi * (bi + 1) / 2 > u) --bi;
+      while ((bi + 1) * (bi + 2) / 2 <= u) ++bi;
+      bj = u - bi * (bi + 1) / 2;
+    } else {
+      const long long v = u - ss;
+      bi = v / ba;
+      bj = v % ba;
+    }
+    const bool skip = bm < 0 || cb < 0;
+    if (!skip) {
+      for (int e = threadIdx.x; e < 32 * Z2; e += blockDim.x) {
+        const int r = e / Z2, k = e - r * Z2;
+        const long long q = bi * 32 + r;
+        if (q < n) A[r * P + k] = sc.zone[(long long)sc.sorted[base + q] * Z2 + k];
+        const long long c = bj * 32 + r;
+        if (pairs_ss) {
+          if (c < n) B[r * P + k] = sc.zone[(long long)sc.sorted[base + c] * Z2 + k];
+        } else if (c < a) {
+          B[r * P + k] = st.nzone[(long long)sc.clist[cb + c] * Z2 + k];
+        }
+      }
+    }
+    __syncthreads();
+    if (!skip) {
+      int L[D], U[D];
+#pragma unroll
+      for (int x = 0; x < D; ++x) { L[x] = sc.hv.bounds[j * 2 * D + x]; U[x] = sc.hv.bounds[j * 2 * D + D + x]; }
+      unsigned* R = sc.hv.pool + bm;
+      const long long rtw = bq, r0w = ba;
+      unsigned* drop = R;
+      unsigned* rt = R + 3LL * n;
+      unsigned* r0 = rt + (long long)n * rtw;
+      for (int r = warp; r < 32; r += nwarps) {
+        const long long q = bi * 32 + r;
+        if (q >= n) continue;   // warp-uniform
+        const long long c = bj * 32 + lane;
+        if (pairs_ss) {
+          const bool ok = c < q;
+          const bool dq = ok && alu_le_ptr<D>(A + r * P, B + lane * P, L, U);   // s_q ≼ s_c
+          const bool rq = ok && alu_le_ptr<D>(B + lane * P, A + r * P, L, U);   // s_c ≼ s_q
+          const unsigned bd = __ballot_sync(0xffffffffu, dq), br = __ballot_sync(0xffffffffu, rq);
+          if (lane == 0) {
+            if (bd) drop[q] = 1u;
+            if (br) rt[q * rtw + bj] = br;
+          }
+        } else {
+          const bool rq = c < a && alu_le_ptr<D>(B + lane * P, A + r * P, L, U);   // old zone c ≼ s_q
+          const unsigned br = __ballot_sync(0xffffffffu, rq);
+          if (lane == 0 && br) r0[q * r0w + bj] = br;
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// One heavy key merged by a whole block, in canonical order (sorted and gathered by k_heavy_prep).
 template <int D>
 __device__ void merge_key_block(const NetView* nets, const InstState& is, const Succ& sc, const Store& st,
-                                const Front& out, Ctl* ctl, int s, int level, bool in_tile, const Tile<D>& t,
+                                const Front& out, Ctl* ctl, long long j, int level, bool in_tile, const Tile<D>& t,
                                 MergeShared<D>& sh) {
   constexpr int TPW = 32 / D;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int ishift = nets[0].inst_shift;
-  const unsigned n = st.pend[s];
+  const int s = sc.heavy[j];
   const unsigned base = st.pend_base[s];
   const unsigned long long hk = st.hkey[s];
   const int inst = (int)(hk >> ishift);
@@ -400,55 +632,75 @@ __device__ void merge_key_block(const NetView* nets, const InstState& is, const 
     if (tid == 0) st.pend[s] = 0;
     return;
   }
-  const NetView& N = nets[inst];
-  rank_segment(sc, base, n, tid, blockDim.x);
-  if (tid == 0) {
-    sh.cb = alloc_clist(sc, st, s, n, ctl);
-    sh.clen = st.klive[s];
-    sh.retired = 0;
-  }
-  __syncthreads();
-  if (sh.cb >= 0) {
-    const int* lst = st.arena + st.kloff[s];
-    for (int k = tid; k < sh.clen; k += blockDim.x) sc.clist[sh.cb + k] = lst[k];
-  }
-  if (warp == 0 && in_tile && t.base == 0) {
-    int locs[kMaxProcs], ints[kMaxInts];
-    key_decode(N, key_part(hk, ishift), locs, ints);
-    int Ly, U[D];
-    key_bounds(N, t, locs, Ly, U);
-    sh.L[t.i] = Ly;
-    sh.U[t.i] = U[t.i];
-  }
-  __syncthreads();
-  if (sh.cb < 0) { __syncthreads(); return; }
+  const unsigned n = (unsigned)sc.hv.n[j];
+  const int a = sc.hv.a[j];
+  const long long cb = sc.hv.cb[j], bm = sc.hv.bm[j];
+  if (cb < 0) { __syncthreads(); return; }
+  if (tid == 0) { sh.clen = a; sh.retired = 0; sh.nhull = 0; }
   int Lr[D], Ur[D];
 #pragma unroll
-  for (int x = 0; x < D; ++x) { Lr[x] = sh.L[x]; Ur[x] = sh.U[x]; }
-  int* cl = sc.clist + sh.cb;
-  const int clen0 = sh.clen;
+  for (int x = 0; x < D; ++x) { Lr[x] = sc.hv.bounds[j * 2 * D + x]; Ur[x] = sc.hv.bounds[j * 2 * D + D + x]; }
+  __syncthreads();
+  int* cl = sc.clist + cb;
+  const int clen0 = a;
+  const bool rel = bm >= 0;
+  unsigned* R = rel ? sc.hv.pool + bm : nullptr;
+  const long long rtw = ((long long)n + 31) / 32, r0w = ((long long)a + 31) / 32;
+  unsigned* drop = R;
+  int* tpos = rel ? (int*)(R + n) : nullptr;
+  int* hull = rel ? (int*)(R + 2LL * n) : nullptr;
+  const unsigned* rt = rel ? R + 3LL * n : nullptr;
+  const unsigned* r0 = rel ? rt + (long long)n * rtw : nullptr;
   long long dlive = 0;   // meaningful on thread 0
   const int tile_idx = warp * TPW + lane / D, ntiles = (blockDim.x >> 5) * TPW;
   for (unsigned q = 0; q < n; ++q) {
-    const int a = sc.sorted[base + q];
-    for (int e = tid; e < D * D; e += blockDim.x) sh.z[e] = sc.zone[(long long)a * D * D + e];
+    if (rel && drop[q]) continue;   // every thread reads the same word: uniform
+    const int a_s = sc.sorted[base + q];
+    for (int e = tid; e < D * D; e += blockDim.x) sh.z[e] = sc.zone[(long long)a_s * D * D + e];
+    if (tid == 0) sh.unioned = 0;
     __syncthreads();
-    const int clen = sh.clen;
-    // (1)+(2)
-    bool drop = false;
-    for (int k = clen0 + tid; k < clen && !drop; k += blockDim.x) {
-      const int m = cl[k];
-      if (m >= 0) drop = alu_le_ptr<D>(sh.z, st.nzone + (long long)m * D * D, Lr, Ur);
+    const int clen = sh.clen, nhull = sh.nhull;
+    // (1)+(2): with relations only the hulls stored this level remain to test; without, every
+    // zone stored this level
+    bool dropped = false;
+    if (rel) {
+      for (int h = tid; h < nhull && !dropped; h += blockDim.x) {
+        const int m = cl[clen0 + hull[h]];
+        if (m >= 0) dropped = alu_le_ptr<D>(sh.z, st.nzone + (long long)m * D * D, Lr, Ur);
+      }
+    } else {
+      for (int k = clen0 + tid; k < clen && !dropped; k += blockDim.x) {
+        const int m = cl[k];
+        if (m >= 0) dropped = alu_le_ptr<D>(sh.z, st.nzone + (long long)m * D * D, Lr, Ur);
+      }
     }
-    if (__syncthreads_or(drop)) continue;
-    // (3)
+    if (__syncthreads_or(dropped)) continue;
+    // (3): retire the zones s_q simulates
     int ret = 0;
-    for (int k = tid; k < clen; k += blockDim.x) {
+    auto kill = [&](int k) {
       const int m = cl[k];
-      if (m >= 0 && alu_le_ptr<D>(st.nzone + (long long)m * D * D, sh.z, Lr, Ur)) {
-        st.ndead[m] = 1;
-        cl[k] = -1;
-        ++ret;
+      if (m >= 0) { st.ndead[m] = 1; cl[k] = -1; ++ret; }
+    };
+    if (rel) {
+      const unsigned* row0 = r0 + (long long)q * r0w;
+      for (long long w = tid; w < r0w; w += blockDim.x)
+        for (unsigned b = row0[w]; b; b &= b - 1) kill((int)(w * 32 + __ffs(b) - 1));
+      const unsigned* rowt = rt + (long long)q * rtw;
+      const long long wq = ((long long)q + 31) / 32;
+      for (long long w = tid; w < wq; w += blockDim.x)
+        for (unsigned b = rowt[w]; b; b &= b - 1) {
+          const int p = tpos[w * 32 + __ffs(b) - 1];
+          if (p >= 0) kill(clen0 + p);
+        }
+      for (int h = tid; h < nhull; h += blockDim.x) {
+        const int k = clen0 + hull[h];
+        const int m = cl[k];
+        if (m >= 0 && alu_le_ptr<D>(st.nzone + (long long)m * D * D, sh.z, Lr, Ur)) kill(k);
+      }
+    } else {
+      for (int k = tid; k < clen; k += blockDim.x) {
+        const int m = cl[k];
+        if (m >= 0 && alu_le_ptr<D>(st.nzone + (long long)m * D * D, sh.z, Lr, Ur)) kill(k);
       }
     }
     if (ret) atomicAdd(&sh.retired, ret);
@@ -476,17 +728,17 @@ __device__ void merge_key_block(const NetView* nets, const InstState& is, const 
       const int nw = sh.nw;
       if (nw == 0) break;
       int mybest = 0x7fffffff;
-      int hull[D];
+      int hl[D];
       if (in_tile) {
         for (int c = tile_idx; c < nw; c += ntiles) {
           int za[D], zb[D];
 #pragma unroll
-          for (int j = 0; j < D; ++j) za[j] = sh.z[t.i * D + j];
+          for (int e = 0; e < D; ++e) za[e] = sh.z[t.i * D + e];
           load_rows_rw(t, zb, st.nzone + (long long)cl[sh.win[c]] * D * D);
           if (try_union(t, za, zb)) {
             mybest = c;
 #pragma unroll
-            for (int j = 0; j < D; ++j) hull[j] = za[j];
+            for (int e = 0; e < D; ++e) hl[e] = za[e];
             break;
           }
         }
@@ -497,13 +749,14 @@ __device__ void merge_key_block(const NetView* nets, const InstState& is, const 
       if (best == 0x7fffffff) break;
       if (in_tile && mybest == best) {
 #pragma unroll
-        for (int j = 0; j < D; ++j) sh.z[t.i * D + j] = hull[j];
+        for (int e = 0; e < D; ++e) sh.z[t.i * D + e] = hl[e];
       }
       if (tid == 0) {
         const int k = sh.win[best];
         st.ndead[cl[k]] = 1;
         cl[k] = -1;
         --dlive;
+        sh.unioned = 1;
       }
     }
     // (5)
@@ -512,12 +765,17 @@ __device__ void merge_key_block(const NetView* nets, const InstState& is, const 
       sh.node = (int)node;
       node_meta(st, node, level, inst, hk);
       cl[clen] = (int)node;
+      if (rel) {
+        if (sh.unioned) hull[sh.nhull++] = clen - clen0;
+        else tpos[q] = clen - clen0;
+      }
       sh.clen = clen + 1;
       ++dlive;
     }
     __syncthreads();
     const long long node = sh.node;
     for (int e = tid; e < D * D; e += blockDim.x) st.nzone[node * D * D + e] = sh.z[e];
+    if (tid < D) st.ncol0[node * D + tid] = sh.z[tid * D];
     __syncthreads();   // the zone is written before the next survivor replaces sh.z
   }
   __syncthreads();
@@ -607,6 +865,7 @@ __device__ void merge_key_tile(const NetView* nets, const InstState& is, const S
     if (t.i == 0) node = (long long)atomicAdd(&ctl->nnodes, 1ull);
     node = (long long)t.shfl64((unsigned long long)node, 0);
     store_rows(t, z, st.nzone + node * D * D);
+    st.ncol0[node * D + t.i] = z[0];
     if (t.i == 0) {
       node_meta(st, node, level, inst, hk);
       cl[clen] = (int)node;
@@ -633,7 +892,7 @@ __global__ void __launch_bounds__(kMergeBlock) k_merge(const NetView* nets, Inst
     const long long j = sh.job;
     __syncthreads();
     if (j >= nheavy) break;
-    merge_key_block<D>(nets, is, sc, st, out, ctl, sc.heavy[j], level, in_tile, t, sh);
+    merge_key_block<D>(nets, is, sc, st, out, ctl, j, level, in_tile, t, sh);
   }
   // the rest: one tile each, taken in turn
   if (!in_tile) return;
@@ -753,6 +1012,7 @@ __global__ void __launch_bounds__(kBlock) k_graph_store(const NetView* nets, Ins
     int z[D];
     load_rows(t, z, sc.zone + (long long)s * D * D);
     store_rows(t, z, st.nzone + node * D * D);
+    st.ncol0[node * D + t.i] = z[0];
     if (t.i == 0) {
       st.nlevel[node] = level;
       st.ndead[node] = 0;
@@ -982,15 +1242,34 @@ void Level<D>::probe(const NetView* nets, InstState is, Succ sc, Store st, Ctl* 
   k_probe<D><<<grid_for(nsucc, TPB, blocks), kBlock, 0, s>>>(nets, is, sc, st, ctl, nsucc, mode);
 }
 template <int D>
-void Level<D>::deadlock(const NetView* nets, InstState is, Succ sc, Ctl* ctl, long long nsurv, int blocks,
+void Level<D>::deadlock(const NetView* nets, InstState is, Succ sc, Ctl* ctl, long long n, int all, int blocks,
                         cudaStream_t s) {
   constexpr int TPB = (kBlock / 32) * (32 / D);
-  k_deadlock<D><<<grid_for(nsurv, TPB, blocks), kBlock, 0, s>>>(nets, is, sc, ctl, nsurv);
+  k_deadlock<D><<<grid_for(n, TPB, blocks), kBlock, 0, s>>>(nets, is, sc, ctl, n, all);
 }
 template <int D>
 void Level<D>::group(Succ sc, Store st, Ctl* ctl, long long nsucc, long long ntouched, cudaStream_t s) {
   k_seg_alloc<<<grid_for(ntouched, 256, 1024), 256, 0, s>>>(sc, st, ctl, ntouched);
   k_seg_scatter<<<grid_for(nsucc, 256, 4096), 256, 0, s>>>(sc, st, nsucc);
+}
+template <int D>
+void Level<D>::heavy_prep(const NetView* nets, InstState is, Succ sc, Store st, Ctl* ctl, long long nheavy,
+                          int blocks, cudaStream_t s) {
+  const long long g = nheavy < blocks ? nheavy : blocks;
+  if (g > 0) k_heavy_prep<D><<<(int)g, kMergeBlock, 0, s>>>(nets, is, sc, st, ctl, nheavy);
+}
+template <int D>
+int Level<D>::heavy_pairs(const NetView* nets, Succ sc, Store st, const long long* prefix, long long nheavy,
+                          long long ntiles, int blocks, cudaStream_t s) {
+  constexpr int Z2 = D * D;
+  constexpr int P = (Z2 & 1) ? Z2 : Z2 + 1;
+  constexpr size_t smem = 2 * 32 * P * sizeof(int);
+  static const bool attr_ok =
+      cudaFuncSetAttribute(k_heavy_pairs<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) == cudaSuccess;
+  if (!attr_ok) return 1;
+  const long long g = ntiles < blocks ? ntiles : blocks;
+  if (g > 0) k_heavy_pairs<D><<<(int)g, kMergeBlock, smem, s>>>(nets, sc, st, prefix, nheavy, ntiles);
+  return 0;
 }
 template <int D>
 int Level<D>::merge_blocks_per_sm() {

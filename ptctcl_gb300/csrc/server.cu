@@ -1,10 +1,11 @@
 // server.cu -- the serving form of the C ABI: continuous admission of verification requests.
 //
 // Requests are copied at submit time (the caller's descriptor arrays may be freed afterwards) and
-// admitted in arrival order while their estimated passed/waiting-store footprint fits the
-// device-memory budget and the in-flight limit allows. Admitted requests run as batched
-// level-synchronous searches on worker threads, each on its own CUDA stream, so requests admitted
-// while others are running overlap with them on the device.
+// admitted in arrival order while a slot of the in-flight limit and its share of the device-memory
+// budget are free. Each admitted request runs on its own worker thread and CUDA stream, so requests
+// admitted while others are running overlap with them on the device, and a short request is not
+// held back by a long one. A request whose passed store outgrows its share stops with
+// HORA_E_BUDGET.
 #include <cuda_runtime.h>
 
 #include <chrono>
@@ -78,11 +79,8 @@ struct Request {
 
 }  // namespace hgb
 
-// The serving loop: worker threads, each of which repeatedly takes every queued request that still
-// fits the device-memory budget (up to its share of the in-flight limit), runs them together as one
-// batch on its own CUDA stream, and publishes the results. Several workers keep several batches on
-// the device at once, so a request that arrives while others are running starts as soon as a worker
-// and budget are free instead of waiting for the running batches to end.
+// The serving loop: one worker thread per in-flight slot; each takes the oldest queued request whose
+// budget share fits, runs it, publishes the result and takes the next.
 struct hora_server {
   uint64_t budget = 0;
   uint64_t in_use = 0;                 // estimated bytes of the requests on the device
@@ -100,10 +98,13 @@ struct hora_server {
 
 using namespace hgb;
 
-// A request's store estimate: a floor of 64 Ki zones of its dimension plus the hash table.
-static uint64_t estimate_bytes(const hora_net_desc* n) {
+// A request's share of the budget: an equal part per in-flight slot, but at least 64 Ki zones of its
+// dimension.
+static uint64_t share_bytes(const hora_server* s, const hora_net_desc* n) {
   const uint64_t d = (uint64_t)n->nclocks + 1;
-  return (1ull << 16) * (d * d * 4 + 32);
+  const uint64_t floor_bytes = (1ull << 16) * (d * d * 4 + 32);
+  const uint64_t share = s->budget / (uint64_t)s->max_inflight;
+  return share > floor_bytes ? share : floor_bytes;
 }
 
 static void worker_main(hora_server* s, int per_batch) {
@@ -130,8 +131,10 @@ static void worker_main(hora_server* s, int per_batch) {
     for (auto& r : batch) { nets.push_back(r->net.d); qs.push_back(r->net.q); }
     std::vector<int32_t> verdicts(batch.size());
     std::vector<hora_stats> st(batch.size());
-    const int rc = hora_gb_batch_run((int32_t)batch.size(), nets.data(), qs.data(), verdicts.data(), st.data(),
-                                     nullptr);
+    uint64_t share = 0;
+    for (auto& r : batch) share += r->est_bytes;
+    const int rc = run_batch((int32_t)batch.size(), nets.data(), qs.data(), verdicts.data(), st.data(), nullptr,
+                             (size_t)share);
     const auto now = std::chrono::steady_clock::now();
     {
       std::lock_guard<std::mutex> g(s->mu);
@@ -163,8 +166,8 @@ int32_t hora_gb_server_create(uint64_t budget_bytes, int32_t max_inflight, hora_
   s->budget = budget_bytes;
   s->max_inflight = max_inflight;
   cudaGetDevice(&s->device);
-  const int nworkers = std::min(8, max_inflight);
-  const int per_batch = (max_inflight + nworkers - 1) / nworkers;
+  const int nworkers = std::min(64, max_inflight);
+  const int per_batch = 1;
   for (int w = 0; w < nworkers; ++w) s->workers.emplace_back(worker_main, s, per_batch);
   *out = s;
   return HORA_OK;
@@ -172,7 +175,7 @@ int32_t hora_gb_server_create(uint64_t budget_bytes, int32_t max_inflight, hora_
 
 int32_t hora_gb_server_submit(hora_server* s, const hora_net_desc* net, const hora_query_desc* q, int64_t* ticket) {
   if (!s || !net || !q || !ticket) return HORA_E_INVALID;
-  const uint64_t est = estimate_bytes(net);
+  const uint64_t est = share_bytes(s, net);
   if (est > s->budget) return HORA_E_BUDGET;
   auto r = std::make_unique<Request>();
   r->net.copy(net, q);
