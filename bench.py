@@ -38,6 +38,11 @@ METRIC = "zone successors/s"
 UNIT = "successors/s"
 
 
+def workload_name(seed: int) -> str:
+    return (f"config2: 8 automata x 10 locations, 8 clocks (9x9 DBM), 4 binary + 1 broadcast channels, "
+            f"A[] not deadlock, seed {seed}")
+
+
 def workload(seed: int):
     from ptctcl_gb300.generator import config_instance
     return config_instance(WORKLOAD_CONFIG, seed)
@@ -106,22 +111,36 @@ def run_reference(args, rank, world):
         return
     net, kind, p, q = workload(args.seed)
     vals, samples = [], []
+    per_step = max(2.0, min(CPU_SAMPLE_SECONDS, 150.0 / max(1, args.steps)))   # whole run within minutes
     for _ in range(args.warmup):
-        cpu_baseline(net, min(2.0, CPU_SAMPLE_SECONDS))
+        cpu_baseline(net, min(2.0, per_step))
     t_all = time.perf_counter()
     for _ in range(args.steps):
-        b = cpu_baseline(net, CPU_SAMPLE_SECONDS)
+        b = cpu_baseline(net, per_step)
         vals.append(b["value"]); samples.append(b["sample"])
     dt = time.perf_counter() - t_all
     v = statistics.mean(vals) if vals else 0.0
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * dt / max(1, args.steps), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-            "config": {"workload": f"config2 A[] not deadlock, seed {args.seed}", "sample": samples[-1] if samples else ""},
+            "config": {"workload": workload_name(args.seed), "sample": samples[-1] if samples else ""},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
                              "sample": samples[-1] if samples else ""},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def combine_ranks(gen, dev, wall, total, dist, device):
+    """Whole-job figures of N replicas: successors summed over ranks, times the max over ranks."""
+    import torch
+    if dist is None:
+        return gen, dev, wall, total
+    vals = torch.tensor([gen, dev, wall, total], dtype=torch.float64, device=device)
+    g = vals.clone()
+    dist.all_reduce(g, op=dist.ReduceOp.SUM)
+    m = vals.clone()
+    dist.all_reduce(m, op=dist.ReduceOp.MAX)
+    return g[0].item(), m[1].item(), m[2].item(), m[3].item()
 
 
 def percentile(xs, q):
@@ -132,14 +151,15 @@ def percentile(xs, q):
     return xs[k]
 
 
-def run_batched(args):
-    """Config 4: N seeded networks in one batched run vs the same instances one at a time, each form
-    given the same wall-time budget (some generated instances have millions of zones)."""
+def batched_compare(instances: int, budget: float) -> dict:
+    """Config 4: `instances` seeded networks in one batched run vs the same instances one at a time
+    (the plain form), each form given the same wall-time budget (some generated instances have
+    millions of zones, so neither form finishes them all). Time to verdict counts from the start of
+    the form's run; verdicts of instances both forms finished must agree."""
     import ctypes
     from ptctcl_gb300 import engine
     from ptctcl_gb300.generator import config_instance
-    items = [config_instance(4, s) for s in range(args.instances)]
-    budget = args.budget
+    items = [config_instance(4, s) for s in range(instances)]
 
     def timed(fn):
         cancel = ctypes.c_int32(0)
@@ -155,7 +175,8 @@ def run_batched(args):
     b_done = [s for v, s in zip(bv, bst) if v >= 0]
     b_gen = sum(s["generated"] for s in bst)
     plain_gen, plain_done, plain_lat, t0 = 0, 0, [], time.perf_counter()
-    for it in items:
+    plain_v = {}
+    for k, it in enumerate(items):
         left = budget - (time.perf_counter() - t0)
         if left <= 0:
             break
@@ -168,16 +189,23 @@ def run_batched(args):
         if v[0] >= 0:
             plain_done += 1
             plain_lat.append(time.perf_counter() - t0)
+            plain_v[k] = v[0]
     pdt = time.perf_counter() - t0
     lat = [s["seconds"] for s in b_done]
-    line = {"metric": METRIC, "workload": f"config4: {args.instances} seeded networks (clocks U[2,16], automata "
+    both = [k for k in plain_v if bv[k] >= 0]
+    return {"workload": f"config4: {instances} seeded networks (clocks U[2,16], automata "
             f"U[2,10], locations U[4,12], c in [0,40], query mix 60/30/10), {budget:.0f} s budget per form",
             "batched": {"value": b_gen / bdt, "unit": UNIT, "seconds": bdt, "verdicts": len(b_done),
                         "p50_time_to_verdict_s": percentile(lat, 50), "p99_time_to_verdict_s": percentile(lat, 99)},
             "plain_one_at_a_time": {"value": plain_gen / pdt, "unit": UNIT, "seconds": pdt, "verdicts": plain_done,
                                     "p50_time_to_verdict_s": percentile(plain_lat, 50),
                                     "p99_time_to_verdict_s": percentile(plain_lat, 99)},
-            "speedup_successors_per_s": (b_gen / bdt) / max(1e-9, plain_gen / pdt)}
+            "speedup_successors_per_s": (b_gen / bdt) / max(1e-9, plain_gen / pdt),
+            "verdicts_compared": len(both), "verdicts_agree": all(plain_v[k] == bv[k] for k in both)}
+
+
+def run_batched(args):
+    line = {"metric": METRIC, **batched_compare(args.instances, args.budget)}
     print(json.dumps(line), flush=True)
 
 
@@ -252,6 +280,9 @@ def main():
     ap.add_argument("--budget-gb", type=float, default=64.0)
     ap.add_argument("--inflight", type=int, default=64)
     ap.add_argument("--serve-config", type=int, default=3)
+    ap.add_argument("--batched-budget", type=float, default=10.0,
+                    help="seconds per form of the config-4 batched-vs-plain comparison added to the default "
+                         "line (0: leave it out)")
     args = ap.parse_args()
     if args.workload == "batched":
         run_batched(args)
@@ -302,6 +333,7 @@ def main():
         v = engine.deadlock_reachable(net, Backend.Cuda, st)
         walls.append(time.perf_counter() - tw)
         assert verdict is None or v == verdict
+        verdict = v
         stats.append(st)
     barrier()
     total = time.perf_counter() - t0
@@ -309,13 +341,7 @@ def main():
     gen = sum(s.generated for s in stats)
     dev = sum(s.device_seconds for s in stats)
     wall = sum(walls)
-    vals = torch.tensor([gen, dev, wall, total], dtype=torch.float64, device="cuda")
-    if dist is not None:
-        g = vals.clone(); dist.all_reduce(g, op=dist.ReduceOp.SUM)
-        m = vals.clone(); dist.all_reduce(m, op=dist.ReduceOp.MAX)
-        gen_all, dev_max, wall_max, total_max = g[0].item(), m[1].item(), m[2].item(), m[3].item()
-    else:
-        gen_all, dev_max, wall_max, total_max = gen, dev, wall, total
+    gen_all, dev_max, wall_max, total_max = combine_ranks(gen, dev, wall, total, dist, "cuda")
     if rank != 0:
         dist.destroy_process_group()
         return
@@ -328,8 +354,7 @@ def main():
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * total_max / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-        "config": {"workload": f"config2: 8 automata x 10 locations, 8 clocks (9x9 DBM), 4 binary + 1 broadcast "
-                               f"channels, A[] not deadlock, seed {args.seed}",
+        "config": {"workload": workload_name(args.seed),
                    "stored_zones": s0.stored, "successors_per_query": s0.generated, "levels": s0.levels,
                    "verdict_deadlock_reachable": bool(verdict), "l2": "flushed (256 MB write) between steps; "
                    "passed store exceeds L2", "parallelism": f"replicas x{world}"},
@@ -359,6 +384,8 @@ def main():
         line["clocks"] = cs
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(net, CPU_SAMPLE_SECONDS)
+    if args.batched_budget > 0 and world == 1:
+        line["batched"] = batched_compare(args.instances, args.batched_budget)
     print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
