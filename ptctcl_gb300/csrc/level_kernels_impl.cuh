@@ -400,11 +400,12 @@ __device__ __forceinline__ void node_meta(const Store& st, long long node, int l
 
 template <int D>
 struct MergeShared {
-  int z[D * D];         // the survivor being added (becomes the hull on a union)
+  int zbuf[2][D * D];   // the survivor being added (becomes the hull on a union), double-buffered
+  long long node_base;  // node ids reserved for the key's stored zones
   int L[D], U[D];       // the key's per-clock bounds
   int win[kMergeScan];  // list positions of the newest live zones, newest first
   long long cb;
-  int nw, best, node, retired, clen, job, unioned, nhull;
+  int nw, best, node, retired, clen, job, unioned, nhull, nkeep;
 };
 
 // ---------------------------------------------------------------------------------------------
@@ -637,6 +638,14 @@ __device__ void merge_key_block(const NetView* nets, const InstState& is, const 
   const long long cb = sc.hv.cb[j], bm = sc.hv.bm[j];
   if (cb < 0) { __syncthreads(); return; }
   if (tid == 0) { sh.clen = a; sh.retired = 0; sh.nhull = 0; }
+  // node ids for every survivor that can be stored (the relations' drops excluded), reserved at once
+  if (warp == 0) {
+    int keep = 0;
+    for (unsigned q0 = 0; q0 < n; q0 += 32)
+      keep += __popc(__ballot_sync(0xffffffffu, q0 + lane < n && !(bm >= 0 && sc.hv.pool[bm + q0 + lane])));
+    if (lane == 0) sh.node_base = keep ? (long long)atomicAdd(&ctl->nnodes, (unsigned long long)keep) : 0;
+    if (lane == 0) sh.nkeep = keep;
+  }
   int Lr[D], Ur[D];
 #pragma unroll
   for (int x = 0; x < D; ++x) { Lr[x] = sc.hv.bounds[j * 2 * D + x]; Ur[x] = sc.hv.bounds[j * 2 * D + D + x]; }
@@ -653,10 +662,14 @@ __device__ void merge_key_block(const NetView* nets, const InstState& is, const 
   const unsigned* r0 = rel ? rt + (long long)n * rtw : nullptr;
   long long dlive = 0;   // meaningful on thread 0
   const int tile_idx = warp * TPW + lane / D, ntiles = (blockDim.x >> 5) * TPW;
+  const long long node_base = sh.node_base;
+  int used = 0, cur = 0;
   for (unsigned q = 0; q < n; ++q) {
     if (rel && drop[q]) continue;   // every thread reads the same word: uniform
+    int* const zc = sh.zbuf[cur];
+    cur ^= 1;
     const int a_s = sc.sorted[base + q];
-    for (int e = tid; e < D * D; e += blockDim.x) sh.z[e] = sc.zone[(long long)a_s * D * D + e];
+    for (int e = tid; e < D * D; e += blockDim.x) zc[e] = sc.zone[(long long)a_s * D * D + e];
     if (tid == 0) sh.unioned = 0;
     __syncthreads();
     const int clen = sh.clen, nhull = sh.nhull;
@@ -666,12 +679,12 @@ __device__ void merge_key_block(const NetView* nets, const InstState& is, const 
     if (rel) {
       for (int h = tid; h < nhull && !dropped; h += blockDim.x) {
         const int m = cl[clen0 + hull[h]];
-        if (m >= 0) dropped = alu_le_ptr<D>(sh.z, st.nzone + (long long)m * D * D, Lr, Ur);
+        if (m >= 0) dropped = alu_le_ptr<D>(zc, st.nzone + (long long)m * D * D, Lr, Ur);
       }
     } else {
       for (int k = clen0 + tid; k < clen && !dropped; k += blockDim.x) {
         const int m = cl[k];
-        if (m >= 0) dropped = alu_le_ptr<D>(sh.z, st.nzone + (long long)m * D * D, Lr, Ur);
+        if (m >= 0) dropped = alu_le_ptr<D>(zc, st.nzone + (long long)m * D * D, Lr, Ur);
       }
     }
     if (__syncthreads_or(dropped)) continue;
@@ -695,12 +708,12 @@ __device__ void merge_key_block(const NetView* nets, const InstState& is, const 
       for (int h = tid; h < nhull; h += blockDim.x) {
         const int k = clen0 + hull[h];
         const int m = cl[k];
-        if (m >= 0 && alu_le_ptr<D>(st.nzone + (long long)m * D * D, sh.z, Lr, Ur)) kill(k);
+        if (m >= 0 && alu_le_ptr<D>(st.nzone + (long long)m * D * D, zc, Lr, Ur)) kill(k);
       }
     } else {
       for (int k = tid; k < clen; k += blockDim.x) {
         const int m = cl[k];
-        if (m >= 0 && alu_le_ptr<D>(st.nzone + (long long)m * D * D, sh.z, Lr, Ur)) kill(k);
+        if (m >= 0 && alu_le_ptr<D>(st.nzone + (long long)m * D * D, zc, Lr, Ur)) kill(k);
       }
     }
     if (ret) atomicAdd(&sh.retired, ret);
@@ -733,7 +746,7 @@ __device__ void merge_key_block(const NetView* nets, const InstState& is, const 
         for (int c = tile_idx; c < nw; c += ntiles) {
           int za[D], zb[D];
 #pragma unroll
-          for (int e = 0; e < D; ++e) za[e] = sh.z[t.i * D + e];
+          for (int e = 0; e < D; ++e) za[e] = zc[t.i * D + e];
           load_rows_rw(t, zb, st.nzone + (long long)cl[sh.win[c]] * D * D);
           if (try_union(t, za, zb)) {
             mybest = c;
@@ -749,7 +762,7 @@ __device__ void merge_key_block(const NetView* nets, const InstState& is, const 
       if (best == 0x7fffffff) break;
       if (in_tile && mybest == best) {
 #pragma unroll
-        for (int e = 0; e < D; ++e) sh.z[t.i * D + e] = hl[e];
+        for (int e = 0; e < D; ++e) zc[t.i * D + e] = hl[e];
       }
       if (tid == 0) {
         const int k = sh.win[best];
@@ -759,10 +772,11 @@ __device__ void merge_key_block(const NetView* nets, const InstState& is, const 
         sh.unioned = 1;
       }
     }
-    // (5)
+    // (5): store under the next reserved id. No barrier: the next survivor fills the other buffer,
+    // and this one is reused only after the next survivor's barriers.
+    const long long node = node_base + used;
+    ++used;
     if (tid == 0) {
-      const long long node = (long long)atomicAdd(&ctl->nnodes, 1ull);
-      sh.node = (int)node;
       node_meta(st, node, level, inst, hk);
       cl[clen] = (int)node;
       if (rel) {
@@ -772,11 +786,12 @@ __device__ void merge_key_block(const NetView* nets, const InstState& is, const 
       sh.clen = clen + 1;
       ++dlive;
     }
-    __syncthreads();
-    const long long node = sh.node;
-    for (int e = tid; e < D * D; e += blockDim.x) st.nzone[node * D * D + e] = sh.z[e];
-    if (tid < D) st.ncol0[node * D + tid] = sh.z[tid * D];
-    __syncthreads();   // the zone is written before the next survivor replaces sh.z
+    for (int e = tid; e < D * D; e += blockDim.x) st.nzone[node * D * D + e] = zc[e];
+    if (tid < D) st.ncol0[node * D + tid] = zc[tid * D];
+  }
+  for (int u = used + tid; u < sh.nkeep; u += blockDim.x) {   // ids a drop by a hull left unused
+    const long long node = node_base + u;
+    st.ndead[node] = 1; st.nlevel[node] = -1; st.ninst[node] = inst; st.nkey[node] = hk;
   }
   __syncthreads();
   if (tid == 0) finish_key(sc, st, out, is, ctl, s, hk, inst, cl, clen0, sh.clen, dlive);
