@@ -215,8 +215,9 @@ typedef struct {
   int has_diag;
   /* optional restriction to !q (leads-to): at states matching q's discrete part the successor
      must stay outside q's clock region, which is a single atom (convex complement) */
-  const hora_pred_desc* avoid;   /* q, or NULL */
+  const hora_pred_desc* avoid;   /* q (leads-to) or psi (E[] psi), or NULL */
   int32_t avoid_neg[3];          /* complement of q's clock atom */
+  int avoid_psi;                 /* 1: the run must stay in the conjunction psi (E[] psi) */
 } Model;
 
 static int ceil_log2(long n) { int b = 0; while ((1L << b) < n) ++b; return b; }
@@ -498,8 +499,14 @@ static void reset_inactive(const Model* m, const int32_t* locs, int32_t* z, cons
  * invariant is unsatisfiable; the caller tests emptiness. */
 static int ints_ok(const int32_t* atoms, int na, const int32_t* ints);
 static int disc_match(const hora_pred_desc* t, const int32_t* locs, const int32_t* ints);
-/* Restrict z to the complement of q where q's discrete part holds; 0 when nothing is left. */
+/* Restrict z to the complement of q where q's discrete part holds (leads-to), or to psi (E[] psi:
+ * psi's discrete part must hold and its clock conjunction is adjoined, exists_invariant_run.cpp:
+ * 70-91); 0 when nothing is left. */
 static int avoid_cut(const Model* m, int32_t* z, const int32_t* tl, const int32_t* ti) {
+  if (m->avoid && m->avoid_psi) {
+    if (!disc_match(m->avoid, tl, ti)) return 0;
+    return apply_cons(z, m->dim, m->avoid->clk_cond, 0, m->avoid->nclk);
+  }
   if (!m->avoid || !disc_match(m->avoid, tl, ti)) return 1;
   if (m->avoid->nclk == 0) return 0;   /* a purely discrete q: the whole state is in q */
   return orc_dbm_constrain(z, m->dim, m->avoid_neg[0], m->avoid_neg[1], m->avoid_neg[2]);
@@ -1266,8 +1273,12 @@ int32_t orc_initial_state(const hora_net_desc* net, const uint8_t* qmask, int32_
  *  3. on that graph, node-level emptiness of W is exact: W starts as every node and repeatedly
  *     loses the nodes with no stop valuation and no successor left in W.
  * ============================================================================================ */
+/* A location requirement (p, l) with l >= 0 asks for location l; l < 0 for any location but -l-1. */
 static int disc_match(const hora_pred_desc* t, const int32_t* locs, const int32_t* ints) {
-  for (int k = 0; k < t->nloc; ++k) if (locs[t->loc_req[2 * k]] != t->loc_req[2 * k + 1]) return 0;
+  for (int k = 0; k < t->nloc; ++k) {
+    const int l = t->loc_req[2 * k + 1], at = locs[t->loc_req[2 * k]];
+    if (l >= 0 ? at != l : at == -l - 1) return 0;
+  }
   return ints_ok(t->int_cond, t->nint, ints);
 }
 static int has_upper_invariant(const Model* m, const int32_t* locs) {
@@ -1351,10 +1362,13 @@ static void count_emit(void* c, const int32_t* l, const int32_t* i, const int32_
   ((CountCtx*)c)->count++;
 }
 
-int32_t orc_leads_to(const hora_net_desc* net, const hora_pred_desc* p, const hora_pred_desc* q,
-                     hora_stats* st, int32_t* result) {
+/* p --> q (psi NULL), or E[] psi (p, q NULL): the two share the restricted exact zone graph, its
+ * stop sets and the greatest fixpoint. E[] psi roots the graph at the initial state of the
+ * psi-restricted network instead of at the p-states of a reachability pass. */
+static int32_t liveness_core(const hora_net_desc* net, const hora_pred_desc* p, const hora_pred_desc* q,
+                             const hora_pred_desc* psi, hora_stats* st, int32_t* result) {
   double t0 = now_s();
-  if (q->nclk > 1) return HORA_E_NOT_SUPPORTED;   /* !q must be convex: at most one clock atom */
+  if (!psi && q->nclk > 1) return HORA_E_NOT_SUPPORTED;   /* !q must be convex: at most one clock atom */
   Model m;
   int rc = model_build(net, &m);
   if (rc) { model_free(&m); return rc; }
@@ -1364,8 +1378,8 @@ int32_t orc_leads_to(const hora_net_desc* net, const hora_pred_desc* p, const ho
   uint8_t qmask[64] = {0};
   int32_t Lq[64], Uq[64];
   for (int c = 0; c < dim; ++c) Lq[c] = Uq[c] = ORC_ALU_NEG_INF;
-  const hora_pred_desc* preds[2] = {p, q};
-  for (int w = 0; w < 2; ++w)
+  const hora_pred_desc* preds[2] = {psi ? psi : p, psi ? psi : q};
+  for (int w = 0; w < (psi ? 1 : 2); ++w)
     for (int k = 0; k < preds[w]->nclk; ++k) {
       const int i = preds[w]->clk_cond[3 * k], j = preds[w]->clk_cond[3 * k + 1];
       const int v = r_bound(preds[w]->clk_cond[3 * k + 2]);
@@ -1393,7 +1407,7 @@ int32_t orc_leads_to(const hora_net_desc* net, const hora_pred_desc* p, const ho
   for (int v = 0; v < ni; ++v) ints[v] = net->int_init[v];
   orc_dbm_init(zone, dim);
   int violated = 0;
-  if (close_succ_zone(&m, locs, ints, zone, qmask, m.L, m.U, 0) && !orc_dbm_empty(zone, dim)) {
+  if (!psi && close_succ_zone(&m, locs, ints, zone, qmask, m.L, m.U, 0) && !orc_dbm_empty(zone, dim)) {
     const uint64_t k0 = key_encode(&m, locs, ints);
     int id = store_add(&R, k0, zone, 0, dim, m.L, m.U, NULL);
     capfr = 16; fr = (FItem*)malloc(sizeof(FItem) * capfr);
@@ -1426,16 +1440,31 @@ int32_t orc_leads_to(const hora_net_desc* net, const hora_pred_desc* p, const ho
     nfr = collect_frontier(&R, level, &fr, &capfr);
     if (emode == 0 && R.nkeys && (double)R.nlive >= 4.0 * (double)R.nkeys) emode = 1;
   }
-  /* ---- roots: the p-part of every stored zone, cut to !q ---- */
-  m.avoid = q;
-  if (q->nclk == 1) {
+  /* ---- roots: the p-part of every stored zone, cut to !q; for E[] psi, the initial state ---- */
+  m.avoid = psi ? psi : q;
+  m.avoid_psi = psi != NULL;
+  if (!psi && q->nclk == 1) {
     m.avoid_neg[0] = q->clk_cond[1]; m.avoid_neg[1] = q->clk_cond[0]; m.avoid_neg[2] = r_negate(q->clk_cond[2]);
   }
   Store G;
   store_init(&G, d2);
   IVec roots = {0}, efrom = {0}, eto = {0};
   nfr = 0;
-  for (uint64_t i = 0; i <= R.smask; ++i) {
+  if (psi) {
+    for (int pp = 0; pp < np; ++pp) locs[pp] = net->proc_init[pp];
+    for (int v = 0; v < ni; ++v) ints[v] = net->int_init[v];
+    orc_dbm_init(z2, dim);
+    if (close_succ_zone(&m, locs, ints, z2, qmask, m.L, m.U, 0) && !orc_dbm_empty(z2, dim)) {
+      int is_new;
+      const uint64_t k0 = key_encode(&m, locs, ints);
+      const int id = store_find_or_add_exact(&G, k0, z2, 0, &is_new);
+      iv_push(&roots, id);
+      capfr = capfr ? capfr : 16;
+      fr = (FItem*)realloc(fr, sizeof(FItem) * capfr);
+      fr[0].key = k0; fr[0].node = id; nfr = 1;
+    }
+  }
+  for (uint64_t i = 0; !psi && i <= R.smask; ++i) {
     if (R.shead[i] == -2) continue;
     key_decode(&m, R.skey[i], locs, ints);
     if (!disc_match(p, locs, ints)) continue;
@@ -1498,7 +1527,7 @@ int32_t orc_leads_to(const hora_net_desc* net, const hora_pred_desc* p, const ho
     key_decode(&m, nkey[u], locs, ints);
     const int32_t* zu = G.zones + (size_t)u * d2;
     m.avoid = NULL;   /* deadlock and any-successor are judged in the unrestricted network */
-    if (q->nclk == 0) {
+    if ((psi ? psi->nclk : q->nclk) == 0) {
       CountCtx cc = {NULL, 0};
       successors(&m, locs, ints, zu, m.L, m.U, qmask, 1, count_emit, &cc);
       stop[u] = cc.count == 0 || time_diverges(&m, locs, ints, zu, 0) || state_has_deadlock(&m, locs, ints, zu);
@@ -1540,11 +1569,24 @@ int32_t orc_leads_to(const hora_net_desc* net, const hora_pred_desc* p, const ho
   S0.seconds = now_s() - t0;
   if (timed_out) S0.status = HORA_E_TIMEOUT;
   if (st) *st = S0;
-  *result = !violated;
+  *result = psi ? violated : !violated;   /* E[] psi holds iff its root keeps a maximal psi-run */
   free(off); free(dst); free(stop); free(inW); free(nkey);
   free(roots.a); free(efrom.a); free(eto.a); free(fr);
   free(B.locs); free(B.ints); free(B.zones);
   store_free(&G);
   model_free(&m);
   return HORA_OK;
+}
+
+int32_t orc_leads_to(const hora_net_desc* net, const hora_pred_desc* p, const hora_pred_desc* q,
+                     hora_stats* st, int32_t* result) {
+  return liveness_core(net, p, q, NULL, st, result);
+}
+
+/* E[] psi (exists_invariant_run, include/hora/liveness.hpp:35-46): psi a conjunction of location,
+ * integer and clock atoms; holds iff the initial state admits a maximal run whose states all
+ * satisfy psi. */
+int32_t orc_exists_invariant(const hora_net_desc* net, const hora_pred_desc* psi, hora_stats* st,
+                             int32_t* result) {
+  return liveness_core(net, NULL, NULL, psi, st, result);
 }

@@ -66,6 +66,8 @@ int32_t orc_reachable_net(const hora_net_desc* net, const hora_pred_desc* target
 int32_t orc_deadlock_reachable(const hora_net_desc* net, hora_stats* st, int32_t* result);
 int32_t orc_leads_to(const hora_net_desc* net, const hora_pred_desc* p, const hora_pred_desc* q,
                      hora_stats* st, int32_t* result);
+int32_t orc_exists_invariant(const hora_net_desc* net, const hora_pred_desc* psi, hora_stats* st,
+                             int32_t* result);
 
 /* Stop whole-query runs after the first BFS level that ends past `seconds` (0 = no limit); the run
  * then reports status HORA_E_TIMEOUT with the counters reached so far. Used to bound the CPU

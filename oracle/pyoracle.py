@@ -54,6 +54,7 @@ def lib():
         L.orc_reachable_net.argtypes = [VP, VP, VP, P32]; L.orc_reachable_net.restype = I32
         L.orc_deadlock_reachable.argtypes = [VP, VP, P32]; L.orc_deadlock_reachable.restype = I32
         L.orc_leads_to.argtypes = [VP, VP, VP, VP, P32]; L.orc_leads_to.restype = I32
+        L.orc_exists_invariant.argtypes = [VP, VP, VP, P32]; L.orc_exists_invariant.restype = I32
         L.orc_initial_state.argtypes = [VP, ctypes.POINTER(ctypes.c_uint8), P32, P32, P32]
         L.orc_initial_state.restype = I32
         L.orc_set_time_limit.argtypes = [ctypes.c_double]
@@ -214,6 +215,17 @@ def deadlock_reachable(net: Network):
     rc = lib().orc_deadlock_reachable(ctypes.addressof(na.desc), ctypes.byref(st), ctypes.byref(res))
     if rc or st.status not in (0, 5):
         raise RuntimeError(f"oracle deadlock_reachable status {rc}")
+    return bool(res.value), st.as_dict()
+
+
+def exists_invariant(net: Network, psi: Pred):
+    """E[] psi from the initial state (psi a conjunction)."""
+    na, pa = NetArrays(net), PredArrays(psi)
+    st = Stats(); res = ctypes.c_int32(0)
+    rc = lib().orc_exists_invariant(ctypes.addressof(na.desc), ctypes.addressof(pa.desc), ctypes.byref(st),
+                                    ctypes.byref(res))
+    if rc or st.status not in (0, 5):
+        raise RuntimeError(f"oracle exists_invariant status {rc}")
     return bool(res.value), st.as_dict()
 
 

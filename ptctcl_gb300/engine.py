@@ -164,17 +164,26 @@ def has_deadlock(net: Network, locs, ints, zones) -> np.ndarray:
     return out.astype(bool)
 
 
-def batch_run(items: Sequence[Tuple[Network, int, Pred, Pred]], cancel: Optional[ctypes.c_int32] = None):
-    """Run (network, kind, p, q) instances together; returns (verdicts, [stats dict]).
+class BatchInput:
+    """The descriptors of a batch, built once (their arrays stay alive with this object)."""
+
+    def __init__(self, items: Sequence[Tuple[Network, int, Pred, Pred]]):
+        self.n = len(items)
+        self.nas = [NetArrays(it[0]) for it in items]
+        self.qas = [QueryArrays(it[1], it[2], it[3]) for it in items]
+        self.nets = (NetDesc * max(self.n, 1))(*[a.desc for a in self.nas])
+        self.qs = (QueryDesc * max(self.n, 1))(*[a.desc for a in self.qas])
+
+
+def batch_run(items, cancel: Optional[ctypes.c_int32] = None):
+    """Run (network, kind, p, q) instances together; returns (verdicts, [stats dict]). `items` is a
+    sequence of tuples or a prepared BatchInput.
 
     cancel: a ctypes.c_int32 another thread may set to 1; instances without a verdict by then come
     back with verdict -1 and stats status E_CANCELLED (no exception is raised for that)."""
     lib = capi.load()
-    n = len(items)
-    nas = [NetArrays(it[0]) for it in items]
-    qas = [QueryArrays(it[1], it[2], it[3]) for it in items]
-    nets = (NetDesc * max(n, 1))(*[a.desc for a in nas])
-    qs = (QueryDesc * max(n, 1))(*[a.desc for a in qas])
+    b = items if isinstance(items, BatchInput) else BatchInput(items)
+    n, nets, qs = b.n, b.nets, b.qs
     verdicts = np.zeros(max(n, 1), np.int32)
     stats = (Stats * max(n, 1))()
     rc = lib.hora_gb_batch_run(n, ctypes.addressof(nets), ctypes.addressof(qs), capi.p32(verdicts),

@@ -314,7 +314,7 @@ class PredArrays:
         return ctypes.byref(self.desc)
 
 
-Q_REACH, Q_DEADLOCK, Q_LEADSTO = 0, 1, 2
+Q_REACH, Q_DEADLOCK, Q_LEADSTO, Q_EG = 0, 1, 2, 3
 
 
 class QueryArrays:

@@ -12,8 +12,9 @@ verifyta 5.0.0 agreed) and the recorded explored-state counts
 Only the flat subset of the modelling language is converted: clock / bounded-int / channel
 declarations, location invariants, `var OP const` and clock guards joined by `&&`, `clock = 0`
 resets, `var = const` updates and one synchronisation per edge -- exactly what the engine's
-descriptor holds. Models or formulas outside it (functions, arrays, disjunctions, E[] / A<>) are
-skipped and listed on stdout.
+descriptor holds. `E[] psi` is kept when psi is a conjunction; `A<> phi` (= not E[] not phi) when
+phi is a single atom, whose negation is again a conjunction. Models or formulas outside it
+(functions, arrays, disjunctions) are skipped and listed on stdout.
 
 Usage:  python tests/golden/make_fixtures.py [/path/to/reference]
 """
@@ -30,7 +31,7 @@ sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 
 from ptctcl_gb300.model import (Network, Process, Location, Edge, IntVar, Pred, clock_atom,  # noqa: E402
                                 IOP, CHAN_BROADCAST, CHAN_URGENT, query_to_json,
-                                Q_REACH, Q_DEADLOCK, Q_LEADSTO)
+                                Q_REACH, Q_DEADLOCK, Q_LEADSTO, Q_EG)
 
 
 class Unsupported(Exception):
@@ -169,22 +170,38 @@ def load_flat(path: str) -> Network:
     return Network(len(clocks), procs, ints, chans, ["0"] + clocks)
 
 
-def parse_conj(text, net: Network):
-    """Conjunction of Proc.Loc, int and clock atoms -> Pred. Raises Unsupported otherwise."""
+NEG_OP = {"<": ">=", "<=": ">", ">": "<=", ">=": "<", "==": "!=", "!=": "=="}
+
+
+def parse_conj(text, net: Network, negate: bool = False, allow_neg: bool = False):
+    """Conjunction of Proc.Loc, int and clock atoms -> Pred; with allow_neg also !Proc.Loc / negated
+    atoms (the E[] route's restriction takes them). With negate, `text` must be a single atom and
+    the Pred is its negation. Raises Unsupported otherwise."""
     p = Pred()
     text = text.strip()
     while text.startswith("(") and text.endswith(")"):
         text = text[1:-1].strip()
-    for atom in re.split(r"&&|\band\b", text):
-        atom = atom.strip()
+    atoms = [a.strip() for a in re.split(r"&&|\band\b", text)]
+    if negate and len(atoms) != 1:
+        raise Unsupported("negated conjunction")
+    for atom in atoms:
+        neg = negate
+        m = re.match(r"^(?:!|not\s+)\s*(.*)$", atom)
+        if m:
+            if not allow_neg:
+                raise Unsupported("negation")
+            atom, neg = m.group(1).strip(), not neg
         m = re.match(r"^([A-Za-z_]\w*)\.([A-Za-z_]\w*)$", atom)
         if m:
-            p.loc_req.append(net.loc_index(m.group(1), m.group(2)))
+            proc, loc = net.loc_index(m.group(1), m.group(2))
+            p.loc_req.append((proc, -loc - 1) if neg else (proc, loc))   # negative: any other location
             continue
         m = ATOM.match(atom)
         if not m:
             raise Unsupported(f"atom {atom}")
         name, op, v = m.group(1), m.group(2), int(m.group(3))
+        if neg:
+            op = NEG_OP[op]
         cl = net.clock_names[1:]
         if name in cl:
             x = cl.index(name) + 1
@@ -204,8 +221,12 @@ def parse_conj(text, net: Network):
 def parse_formula(f: str, net: Network):
     """-> (kind, p, q, negate) where the verdict 'satisfied' = (engine result) xor negate."""
     f = f.strip()
-    if "||" in f or re.search(r"\bor\b", f) or f.startswith("E[]") or f.startswith("A<>"):
+    if "||" in f or re.search(r"\bor\b", f):
         raise Unsupported("formula form")
+    if f.startswith("E[]"):
+        return Q_EG, parse_conj(f[3:], net, allow_neg=True), Pred(), False
+    if f.startswith("A<>"):
+        return Q_EG, parse_conj(f[3:], net, negate=True, allow_neg=True), Pred(), True
     if f == "A[] not deadlock":
         return Q_DEADLOCK, Pred(), Pred(), True
     if f.startswith("E<>"):
@@ -264,7 +285,8 @@ def main(ref: str):
                 nets.setdefault(key, None)
                 continue
             sat = v[0] == "SAT"
-            # engine result convention: reach -> reachable; deadlock -> deadlock reachable; leadsto -> holds
+            # engine result convention: reach -> reachable; deadlock -> deadlock reachable; leadsto -> holds;
+            # E[] psi -> holds (A<> phi is run as E[] not phi)
             result = (not sat) if neg else sat
             rows.append({"model": key, "formula": formula, "table": tab,
                          "query": query_to_json(kind, p, q), "result": result})
