@@ -13,6 +13,8 @@
  *                              const std::atomic<bool>* cancel)     include/hora/liveness.hpp:144-146
  *   hora_gb_leads_to           bool leads_to_clocks / leads_to_otf(const Network&, const DiscPred& p,
  *                              const DiscPred& q, GfpStats*)        include/hora/liveness.hpp:120-124
+ *   hora_gb_exists_invariant   bool exists_invariant_run(const Network&, const std::vector<Constraint>&
+ *                              psi_clocks, const DiscPred& nq, ReachStats*)  include/hora/liveness.hpp:35-46
  *   hora_gb_expand             NetGpuExpander::expand(...)          include/hora/gpu/network.hpp:52-58
  *   hora_gb_batch_run          no reference counterpart (the reference runs one query at a time);
  *                              same verdict contract as the three entry points above, per instance
@@ -115,7 +117,7 @@ typedef struct hora_net_desc {
  * two sides of a leads-to. */
 typedef struct hora_pred_desc {
   int32_t nloc;
-  const int32_t* loc_req;       /* pairs (proc, local location) */
+  const int32_t* loc_req;       /* pairs (proc, l): location l, or for l < 0 any location but -l-1 */
   int32_t nint;
   const int32_t* int_cond;      /* triples (var, op, val) */
   int32_t nclk;
@@ -127,12 +129,13 @@ typedef struct hora_pred_desc {
 enum {
   HORA_Q_REACH = 0,     /* E<> target  (A[] not target is its negation) */
   HORA_Q_DEADLOCK = 1,  /* is a deadlocked state reachable?  (A[] not deadlock is its negation) */
-  HORA_Q_LEADSTO = 2    /* p --> q */
+  HORA_Q_LEADSTO = 2,   /* p --> q */
+  HORA_Q_EG = 3         /* E[] p  (A<> phi is not E[] not phi) */
 };
 
 typedef struct hora_query_desc {
   int32_t kind;
-  hora_pred_desc p;             /* target for HORA_Q_REACH; p for HORA_Q_LEADSTO */
+  hora_pred_desc p;             /* target for HORA_Q_REACH; p for HORA_Q_LEADSTO; psi for HORA_Q_EG */
   hora_pred_desc q;             /* q for HORA_Q_LEADSTO */
 } hora_query_desc;
 
@@ -185,6 +188,12 @@ HORA_GB_API int32_t hora_gb_deadlock_reachable(const hora_net_desc* net, int32_t
 /* p --> q. On HORA_OK, *result = 1 iff the property holds. */
 HORA_GB_API int32_t hora_gb_leads_to(const hora_net_desc* net, const hora_pred_desc* p, const hora_pred_desc* q,
                          int32_t backend, hora_stats* stats, int32_t* result);
+
+/* E[] psi, psi a conjunction of location (also "not at location"), integer and clock atoms. On
+ * HORA_OK, *result = 1 iff the initial state admits a maximal run all of whose states satisfy psi.
+ * A<> phi for a single atom phi is !E[] (not phi). */
+HORA_GB_API int32_t hora_gb_exists_invariant(const hora_net_desc* net, const hora_pred_desc* psi, int32_t backend,
+                                 hora_stats* stats, int32_t* result);
 
 /* Successor pipeline on host buffers, for differential testing against a CPU implementation.
  * Inputs: n source states (locs[n*nprocs], ints[n*nints], zones[n*dim*dim] canonical, non-empty),

@@ -59,6 +59,9 @@ struct NetView {
   const int* av_loc;
   const int* av_int;
   int av_neg[3];               // complement of q's single clock atom
+  int av_psi;                  // 1: E[] psi -- keep only psi: its discrete part must hold, its clock
+                               // conjunction (av_clk, av_nclk atoms) is adjoined to the invariant
+  const int* av_clk;
   int p_nloc, p_nint, p_nclk;
   const int* p_loc;
   const int* p_int;

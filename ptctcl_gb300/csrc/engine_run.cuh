@@ -427,10 +427,13 @@ struct Engine {
   }
 
   // Level 0 of store 0: every instance's initial state. Returns the frontier size in *nf.
+  // Level 0 of store 0. For E[] psi the initial state is the psi-restricted network's (it becomes
+  // the graph's root); otherwise the unrestricted network's.
   int init(long long* nf) {
     InstState is = istate();
+    const bool eg = !nets.empty() && nets[0]->kind == HORA_Q_EG;
     kt.begin(s);
-    Level<D>::init(dn.views_plain, ninst, dn.ok, store(0), front(0), is, dctl(), s);
+    Level<D>::init(eg ? dn.views : dn.views_plain, ninst, dn.ok, store(0), front(0), is, dctl(), s);
     kt.end(s, KT_OTHER);
     ++launches;
     HGB_CUDA(cudaGetLastError());
@@ -838,7 +841,9 @@ struct Engine {
       int ist = (status == HORA_E_CANCELLED && !leadsto && t_fin[k] >= 0) ? HORA_OK : status;
       if (h_budget[k] && (ist == HORA_OK || ist == HORA_E_CANCELLED)) ist = HORA_E_BUDGET;
       r.status = ist;
-      r.verdict = leadsto ? (h_found[k] ? 0 : 1) : (h_found[k] ? 1 : 0);
+      // leads-to: a surviving root violates it; E[] psi: a surviving root is its witness
+      const bool eg = nets[k]->kind == HORA_Q_EG;
+      r.verdict = (leadsto && !eg) ? (h_found[k] ? 0 : 1) : (h_found[k] ? 1 : 0);
       r.st.explored = explored[k];
       r.st.expanded = explored[k];
       r.st.generated = h_gen[k];
@@ -870,8 +875,10 @@ int run_group(const std::vector<const HostNet*>& nets, std::vector<InstResult>& 
   long long nf = 0;
   if ((rc = E.init(&nf))) return rc;
   int cur = 0, level = 0;
-  const bool leadsto = !nets.empty() && nets[0]->kind == HORA_Q_LEADSTO;
-  int status = E.run_levels(0, 0, cur, nf, level, nullptr);
+  const bool eg = !nets.empty() && nets[0]->kind == HORA_Q_EG;
+  const bool leadsto = !nets.empty() && (nets[0]->kind == HORA_Q_LEADSTO || eg);
+  // E[] psi has no reachability pass: its graph is rooted at the (restricted) initial state
+  int status = eg ? HORA_OK : E.run_levels(0, 0, cur, nf, level, nullptr);
   if (status == HORA_OK && leadsto) status = E.leadsto_phase2(cur);
   if (status != HORA_OK && status != HORA_E_CANCELLED) {
     E.finish(res, status, leadsto);

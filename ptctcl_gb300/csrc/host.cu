@@ -31,7 +31,8 @@ static int check_pred(const hora_net_desc* n, const hora_pred_desc* t, std::stri
   if (t->nloc < 0 || t->nint < 0 || t->nclk < 0) { err = "negative predicate sizes"; return HORA_E_INVALID; }
   for (int k = 0; k < t->nloc; ++k) {
     const int p = t->loc_req[2 * k], l = t->loc_req[2 * k + 1];
-    if (p < 0 || p >= n->nprocs || l < 0 || l >= n->proc_nlocs[p]) { err = "predicate location out of range"; return HORA_E_INVALID; }
+    const int ll = l >= 0 ? l : -l - 1;   // l < 0: any location but -l-1
+    if (p < 0 || p >= n->nprocs || ll >= n->proc_nlocs[p]) { err = "predicate location out of range"; return HORA_E_INVALID; }
   }
   for (int k = 0; k < t->nint; ++k)
     if (t->int_cond[3 * k] < 0 || t->int_cond[3 * k] >= n->nints || t->int_cond[3 * k + 1] < 0 || t->int_cond[3 * k + 1] > 5) {
@@ -280,6 +281,30 @@ int compile_net(const hora_net_desc* n, int kind, const hora_pred_desc* target, 
       H.av_neg[2] = (r & 1) ? ((-v) << 1) : (((-v) << 1) | 1);
     }
   }
+  if (kind == HORA_Q_EG) {
+    // E[] psi: psi's clock constants join the bounds, collapsed to a_M as for leads-to; the graph is
+    // the psi-restricted network's from its initial state (exists_invariant_run.cpp:67-91)
+    if (!target) { err = "E[] needs psi"; return HORA_E_INVALID; }
+    if (target->never) { err = "E[] false"; return HORA_E_NOT_SUPPORTED; }
+    for (int k = 0; k < target->nclk; ++k) {
+      const int i = target->clk_cond[3 * k], j = target->clk_cond[3 * k + 1], v = raw_bound(target->clk_cond[3 * k + 2]);
+      const int x = i > 0 ? i : j;
+      if (x <= 0) continue;
+      H.qmask |= 1ull << x;
+      const int a = v < 0 ? -v : v;
+      H.L[x] = std::max(H.L[x], a); H.U[x] = std::max(H.U[x], a);
+      H.Lq[x] = std::max(H.Lq[x], a); H.Uq[x] = std::max(H.Uq[x], a);
+    }
+    for (int c = 0; c < dim; ++c) { H.L[c] = H.U[c] = std::max(H.L[c], H.U[c]); H.Lq[c] = H.Uq[c] = std::max(H.Lq[c], H.Uq[c]); }
+    for (size_t k = 0; k < H.Lloc.size(); ++k) H.Lloc[k] = H.Uloc[k] = std::max(H.Lloc[k], H.Uloc[k]);
+    H.L[0] = H.U[0] = 0;
+    H.av_on = 1;
+    H.av_psi = 1;
+    H.av_loc.assign(target->loc_req, target->loc_req + 2 * target->nloc);
+    H.av_int.assign(target->int_cond, target->int_cond + 3 * target->nint);
+    H.av_clk.assign(target->clk_cond, target->clk_cond + 3 * target->nclk);
+    H.av_nclk = target->nclk;
+  }
   if (kind == HORA_Q_REACH && target) {
     H.t_never = target->never;
     H.t_loc.assign(target->loc_req, target->loc_req + 2 * target->nloc);
@@ -324,7 +349,7 @@ void build_blob(const HostNet& H, std::vector<int32_t>& blob, std::vector<size_t
                                         &H.edge_reset_off, &H.edge_iupd_off, &H.cons, &H.iatoms, &H.resets,
                                         &H.iupds, &H.Lloc, &H.Uloc, &act32, &H.kshift, &H.kwidth, &H.L, &H.U,
                                         &H.Lq, &H.Uq, &H.t_loc, &H.t_int, &H.t_clk, &H.av_loc, &H.av_int,
-                                        &H.p_loc, &H.p_int, &H.p_clk};
+                                        &H.p_loc, &H.p_int, &H.p_clk, &H.av_clk};
   for (auto* a : arrs) add(*a);
   while (blob.size() % 4) blob.push_back(0);
 }
@@ -356,6 +381,8 @@ NetView make_view(const HostNet& H, const int32_t* b, const std::vector<size_t>&
   V.av_loc = b + offs[q++]; V.av_int = b + offs[q++];
   V.p_nloc = (int)H.p_loc.size() / 2; V.p_nint = (int)H.p_int.size() / 3; V.p_nclk = (int)H.p_clk.size() / 3;
   V.p_loc = b + offs[q++]; V.p_int = b + offs[q++]; V.p_clk = b + offs[q++];
+  V.av_clk = b + offs[q++];
+  V.av_psi = H.av_psi;
   return V;
 }
 
@@ -501,6 +528,12 @@ int32_t hora_gb_leads_to(const hora_net_desc* net, const hora_pred_desc* p, cons
   return run_single(net, HORA_Q_LEADSTO, p, q, backend, stats, nullptr, result);
 }
 
+int32_t hora_gb_exists_invariant(const hora_net_desc* net, const hora_pred_desc* psi, int32_t backend,
+                                 hora_stats* stats, int32_t* result) {
+  if (!psi) return fail(HORA_E_INVALID, "null predicate");
+  return run_single(net, HORA_Q_EG, psi, nullptr, backend, stats, nullptr, result);
+}
+
 int32_t hora_gb_expand(const hora_net_desc* net, int32_t n, const int32_t* locs, const int32_t* ints,
                        const int32_t* zones, const int32_t* L, const int32_t* U, const uint8_t* qmask,
                        int32_t emode, int64_t cap, int32_t* out_src, int32_t* out_ord, int32_t* out_locs,
@@ -568,16 +601,34 @@ int32_t run_batch(int32_t n, const hora_net_desc* nets, const hora_query_desc* q
   int rc = ensure_device();
   if (rc) return rc;
   std::vector<HostNet> H(n);
-  // one device group per (dimension, leads-to or not): a group runs one level loop
+  std::vector<int> crc(n, HORA_OK);
+  {
+    // compile the networks on the host threads the machine has (each compile is independent)
+    std::atomic<int> next{0};
+    auto work = [&]() {
+      for (int k; (k = next.fetch_add(1)) < n;) {
+        std::string err;
+        const hora_query_desc& q = queries[k];
+        crc[k] = compile_net(&nets[k], q.kind, q.kind == HORA_Q_DEADLOCK ? nullptr : &q.p,
+                             q.kind == HORA_Q_LEADSTO ? &q.q : nullptr, H[k], err);
+      }
+    };
+    const int nt = std::max(1, std::min<int>((int)std::thread::hardware_concurrency(), std::min(n, 32)));
+    std::vector<std::thread> th;
+    for (int i = 1; i < nt; ++i) th.emplace_back(work);
+    work();
+    for (auto& t : th) t.join();
+  }
+  // one device group per (dimension, route: forward search / leads-to / E[]): a group runs one
+  // level loop
   std::map<int, std::vector<int>> by_dim;
   for (int k = 0; k < n; ++k) {
     verdicts[k] = -1;
-    std::string err;
     const hora_query_desc& q = queries[k];
-    const int r = compile_net(&nets[k], q.kind, q.kind == HORA_Q_DEADLOCK ? nullptr : &q.p,
-                              q.kind == HORA_Q_LEADSTO ? &q.q : nullptr, H[k], err);
+    const int r = crc[k];
     if (stats) { std::memset(&stats[k], 0, sizeof(hora_stats)); stats[k].status = r; }
-    if (r == HORA_OK) by_dim[H[k].dim * 2 + (q.kind == HORA_Q_LEADSTO ? 1 : 0)].push_back(k);
+    const int route = q.kind == HORA_Q_LEADSTO ? 1 : q.kind == HORA_Q_EG ? 2 : 0;
+    if (r == HORA_OK) by_dim[H[k].dim * 4 + route].push_back(k);
   }
   // the groups run concurrently, each on its own host thread and CUDA stream
   std::vector<std::pair<int, std::vector<int>>> groups(by_dim.begin(), by_dim.end());
@@ -608,7 +659,7 @@ int32_t run_batch(int32_t n, const hora_net_desc* nets, const hora_query_desc* q
       if (cancel && *cancel) { gskipped[g] = 1; continue; }   // groups not yet started are not started
       std::vector<const HostNet*> v;
       for (int k : groups[g].second) v.push_back(&H[k]);
-      grc[g] = dispatch_group(groups[g].first / 2, v, gres[g], o, gerr[g]);
+      grc[g] = dispatch_group(groups[g].first / 4, v, gres[g], o, gerr[g]);
     }
   };
   std::vector<std::thread> pool;

@@ -24,9 +24,9 @@ struct HostNet {
       iatoms, resets, iupds, Lloc, Uloc, kshift, kwidth, L, U, Lq, Uq, t_loc, t_int, t_clk;
   std::vector<unsigned long long> act;
   // leads-to
-  int av_on = 0, av_nclk = 0;
+  int av_on = 0, av_nclk = 0, av_psi = 0;
   int av_neg[3] = {0, 0, 0};
-  std::vector<int32_t> av_loc, av_int, p_loc, p_int, p_clk;
+  std::vector<int32_t> av_loc, av_int, av_clk, p_loc, p_int, p_clk;
 };
 
 // Compile `net` for query `kind` (HORA_Q_*): `p` is the reach target or the left side of a

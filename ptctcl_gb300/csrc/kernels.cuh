@@ -131,8 +131,10 @@ __device__ __forceinline__ void apply_resets(const NetView& N, const Tile<D>& t,
 }
 __device__ __forceinline__ bool pred_disc(const int* loc, int nloc, const int* ia, int nint, const int* locs,
                                           const int* ints) {
-  for (int k = 0; k < nloc; ++k)
-    if (locs[loc[2 * k]] != loc[2 * k + 1]) return false;
+  for (int k = 0; k < nloc; ++k) {   // l >= 0: at location l; l < 0: anywhere but -l-1
+    const int l = loc[2 * k + 1], at = locs[loc[2 * k]];
+    if (l >= 0 ? at != l : at == -l - 1) return false;
+  }
   return iatoms_ok(ia, nint, ints);
 }
 // Leads-to restriction to !q: where q's discrete part holds, cut the zone to the complement of
@@ -141,6 +143,10 @@ __device__ __forceinline__ bool pred_disc(const int* loc, int nloc, const int* i
 template <int D>
 __device__ __forceinline__ bool avoid_cut(const NetView& N, const Tile<D>& t, int (&r)[D], const int* tl,
                                           const int* ti) {
+  if (N.av_on && N.av_psi) {   // E[] psi (exists_invariant_run.cpp:70-91)
+    if (!pred_disc(N.av_loc, N.av_nloc, N.av_int, N.av_nint, tl, ti)) return false;
+    return apply_cons(t, r, N.av_clk, 0, N.av_nclk);
+  }
   if (!N.av_on || !pred_disc(N.av_loc, N.av_nloc, N.av_int, N.av_nint, tl, ti)) return true;
   if (N.av_nclk == 0) return false;
   return constrain(t, r, N.av_neg[0], N.av_neg[1], N.av_neg[2]);
@@ -178,7 +184,8 @@ template <int D>
 __device__ bool target_hit(const NetView& N, const Tile<D>& t, const int (&r)[D], const int* locs, const int* ints) {
   if (N.t_never) return false;
   for (int k = 0; k < N.t_nloc; ++k)
-    if (locs[N.t_loc[2 * k]] != N.t_loc[2 * k + 1]) return false;
+    if (N.t_loc[2 * k + 1] >= 0 ? locs[N.t_loc[2 * k]] != N.t_loc[2 * k + 1]
+                                : locs[N.t_loc[2 * k]] == -N.t_loc[2 * k + 1] - 1) return false;
   if (!iatoms_ok(N.t_int, N.t_nint, ints)) return false;
   int z[D];
 #pragma unroll

@@ -262,7 +262,7 @@ __global__ void __launch_bounds__(kBlock) k_deadlock(const NetView* nets, InstSt
 // group: one contiguous segment of survivors per touched slot; keys whose merge is long (many
 // survivors against a long antichain) go to the block-wide merge, the rest to the tile merge
 // ---------------------------------------------------------------------------------------------
-constexpr long long kHeavyMerge = 2048;   // survivors x (live zones + survivors) of a block-wide key
+constexpr long long kHeavyMerge = 512;    // survivors x (live zones + survivors) of a block-wide key
 constexpr int kRelMaxN = 1 << 16;         // larger keys fold without precomputed relations
 
 // Words of a heavy key's relation block (layout at k_heavy_prep).
@@ -1093,7 +1093,7 @@ static __global__ void k_collect_p(const NetView* nets, Store st, long long nnod
     const unsigned long long hk = st.nkey[n];
     const int inst = (int)(hk >> ishift);
     const NetView& N = nets[inst];
-    if (N.kind != 2) continue;
+    if (N.kind != 2 && N.kind != 3) continue;   // leads-to p-nodes; E[]: the initial state
     int locs[kMaxProcs], ints[kMaxInts];
     key_decode(N, key_part(hk, ishift), locs, ints);
     if (!pred_disc(N.p_loc, N.p_nloc, N.p_int, N.p_nint, locs, ints)) continue;

@@ -16,7 +16,7 @@ import numpy as np
 
 from . import capi
 from .model import (Network, Pred, NetArrays, PredArrays, QueryArrays, Stats, QueryDesc, NetDesc,
-                    Q_REACH, Q_DEADLOCK, Q_LEADSTO)
+                    Q_REACH, Q_DEADLOCK, Q_LEADSTO, Q_EG)
 
 
 class Backend(enum.IntEnum):
@@ -101,12 +101,29 @@ def leads_to_clocks(net: Network, p: Pred, q: Pred, backend: Backend = Backend.C
     return bool(res.value)
 
 
+def exists_invariant_run(net: Network, psi: Pred, backend: Backend = Backend.Cuda,
+                         stats: Optional[ReachStats] = None) -> bool:
+    """E[] psi (exists_invariant_run, include/hora/liveness.hpp:35-46): psi a conjunction of
+    location (a negative location l stands for "not at -l-1"), integer and clock atoms."""
+    L = capi.load()
+    na, pa = NetArrays(net), PredArrays(psi)
+    st = Stats()
+    res = ctypes.c_int32(0)
+    rc = L.hora_gb_exists_invariant(ctypes.addressof(na.desc), ctypes.addressof(pa.desc), int(backend),
+                                    ctypes.byref(st), ctypes.byref(res))
+    if stats is not None:
+        stats.fill(st)
+    capi.check(rc, "exists_invariant")
+    return bool(res.value)
+
+
 def check_network_query(net: Network, kind: int, p: Pred, q: Optional[Pred] = None, negate: bool = False,
                         backend: Backend = Backend.Cuda, stats: Optional[ReachStats] = None) -> bool:
     """Route one lowered query (check_network_query, src/query/dispatch.cpp:109-607).
 
     ``kind`` is Q_REACH (E<> p; ``negate`` gives A[] not p), Q_DEADLOCK (``negate`` gives
-    A[] not deadlock) or Q_LEADSTO (p --> q). Returns whether the formula is satisfied.
+    A[] not deadlock), Q_LEADSTO (p --> q) or Q_EG (E[] p; ``negate`` with p = not phi gives
+    A<> phi). Returns whether the formula is satisfied.
     """
     if kind == Q_REACH:
         r = reachable_net(net, p, backend, stats)
@@ -114,6 +131,8 @@ def check_network_query(net: Network, kind: int, p: Pred, q: Optional[Pred] = No
         r = deadlock_reachable(net, backend, stats)
     elif kind == Q_LEADSTO:
         r = leads_to_clocks(net, p, q or Pred(), backend, stats)
+    elif kind == Q_EG:
+        r = exists_invariant_run(net, p, backend, stats)
     else:
         raise ValueError(kind)
     return (not r) if negate else r

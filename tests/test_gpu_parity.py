@@ -178,3 +178,30 @@ def test_leadsto_config3(seed):
     assert got == want
     for k in LT_COUNTS:
         assert getattr(st, k) == wst[k], (k, getattr(st, k), wst[k])
+
+
+EG_ROWS = verdict_rows(kinds=(3,))
+EG_SLOW_ORACLE = {("grc4", "E[] x0 >= 0"), ("single4", "E[] x0 <= 3"), ("single4", "E[] x0 >= 0"),
+                  ("single4", "A<> x0 >= 3")}
+
+
+@pytest.mark.parametrize("model,formula,kind,p,q,result", EG_ROWS, ids=[f"{r[0]}:{r[1]}" for r in EG_ROWS])
+def test_reference_eg_verdicts_gpu(model, formula, kind, p, q, result):
+    """E[] psi rows of the reference's verdict tables (A<> phi run as E[] not phi): the verdict,
+    and the graph's counts equal to the oracle's."""
+    net = load_model(model)
+    st = ReachStats()
+    got = engine.exists_invariant_run(net, p, Backend.Cuda, st)
+    assert got == result
+    if (model, formula) not in EG_SLOW_ORACLE:
+        want, wst = pyoracle.exists_invariant(net, p)
+        for k in LT_COUNTS:
+            assert getattr(st, k) == wst[k], (k, getattr(st, k), wst[k])
+
+
+def test_eg_batched_matches_single():
+    rows = [r for r in EG_ROWS if (r[0], r[1]) not in EG_SLOW_ORACLE][:24]
+    items = [(load_model(m), 3, p, Pred()) for (m, f, k, p, q, res) in rows]
+    verdicts, stats = engine.batch_run(items)
+    for (m, f, k, p, q, res), v in zip(rows, verdicts):
+        assert v == int(res), (m, f)
