@@ -18,6 +18,10 @@ namespace hgb {
     cudaError_t e_ = (call);                                                       \
     if (e_ != cudaSuccess) {                                                       \
       err = std::string("CUDA: ") + #call + ": " + cudaGetErrorString(e_);         \
+      if (e_ == cudaErrorMemoryAllocation) {  /* not sticky: the context lives on */ \
+        (void)cudaGetLastError();                                                  \
+        return HORA_E_NOMEM;                                                       \
+      }                                                                            \
       return HORA_E_CUDA;                                                          \
     }                                                                              \
   } while (0)
