@@ -243,7 +243,7 @@ def run_serving(args):
             time.sleep(min(0.002, next_t - now))
     submitted = time.perf_counter() - t0
     # drain
-    lat, gen, done = [], 0, 0
+    lat, gen, done, stopped = [], 0, 0, 0
     active = ctypes.c_int32(1)
     while active.value > 0 and time.perf_counter() - t0 < args.duration + args.drain:
         lib.hora_gb_server_step(srv, ctypes.byref(active))
@@ -252,13 +252,17 @@ def run_serving(args):
         d, v, st = ctypes.c_int32(0), ctypes.c_int32(0), Stats()
         lib.hora_gb_server_poll(srv, tk, ctypes.byref(d), ctypes.byref(v), ctypes.byref(st))
         if d.value:
-            done += 1
-            lat.append(st.seconds)
             gen += st.generated
+            if st.status == capi.OK:
+                done += 1
+                lat.append(st.seconds)
+            else:
+                stopped += 1   # outgrew its memory share (HORA_E_BUDGET) or failed
     lib.hora_gb_server_destroy(srv)
     line = {"metric": METRIC, "workload": f"config{args.serve_config} requests, Poisson {args.rate}/s for "
             f"{args.duration:.0f} s, budget {args.budget_gb} GB, {args.inflight} in flight",
-            "offered": len(tickets), "finished": done, "value": gen / total, "unit": UNIT,
+            "offered": len(tickets), "verdicts": done, "stopped_over_budget": stopped, "value": gen / total,
+            "unit": UNIT,
             "p50_time_to_verdict_s": percentile(lat, 50), "p99_time_to_verdict_s": percentile(lat, 99),
             "seconds": total, "submit_seconds": submitted}
     print(json.dumps(line), flush=True)

@@ -1,7 +1,7 @@
 """Build libhora_gb300.so for sm_103a with nvcc, in-tree (ptctcl_gb300/_build/).
 
 Every kernel is a template on the DBM dimension D (clocks + 1). One translation unit per D in
-[2, 17] is generated and compiled in parallel, then linked with the host/C-ABI unit into one
+[1, 17] is generated and compiled in parallel, then linked with the host/C-ABI unit into one
 shared library whose exported surface is exactly include/hora_gb300.h.
 """
 from __future__ import annotations
@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 GEN = os.path.join(BUILD, "gen")
 LIB = os.path.join(BUILD, "libhora_gb300.so")
-DIMS = list(range(2, 18))
+DIMS = list(range(1, 18))
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
               "--expt-relaxed-constexpr", "-Xptxas", "-O3", *ARCH]

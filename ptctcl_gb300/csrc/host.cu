@@ -419,7 +419,7 @@ int upload_nets(const std::vector<const HostNet*>& nets, int inst_shift, DeviceN
 // ---------------------------------------------------------------------------------------------
 // dimension dispatch
 // ---------------------------------------------------------------------------------------------
-#define HGB_FOR_DIMS(X) X(2) X(3) X(4) X(5) X(6) X(7) X(8) X(9) X(10) X(11) X(12) X(13) X(14) X(15) X(16) X(17)
+#define HGB_FOR_DIMS(X) X(1) X(2) X(3) X(4) X(5) X(6) X(7) X(8) X(9) X(10) X(11) X(12) X(13) X(14) X(15) X(16) X(17)
 #define HGB_DECL(D)                                                                                         \
   extern template int run_group<D>(const std::vector<const HostNet*>&, std::vector<InstResult>&,           \
                                    const RunOptions&, std::string&);                                       \

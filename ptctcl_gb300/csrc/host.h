@@ -84,7 +84,7 @@ template <int D>
 int run_has_deadlock(const HostNet& net, int n, const int* locs, const int* ints, const int* zones, int* out,
                      std::string& err);
 
-constexpr int kMinDim = 2;
+constexpr int kMinDim = 1;
 constexpr int kMaxDim = 17;
 
 }  // namespace hgb

@@ -57,7 +57,7 @@ static int noalloc_scratch(unsigned char** out, std::string& err) {
   return HORA_OK;
 }
 
-#define HGB_FOR_DIMS_NA(X) X(2) X(3) X(4) X(5) X(6) X(7) X(8) X(9) X(10) X(11) X(12) X(13) X(14) X(15) X(16) X(17)
+#define HGB_FOR_DIMS_NA(X) X(1) X(2) X(3) X(4) X(5) X(6) X(7) X(8) X(9) X(10) X(11) X(12) X(13) X(14) X(15) X(16) X(17)
 
 }  // namespace hgb
 
