@@ -158,8 +158,10 @@ __global__ void __launch_bounds__(kBlock) k_expand(const NetView* nets, InstStat
 // ---------------------------------------------------------------------------------------------
 // probe: drop successors a stored zone simulates; group the rest by hash slot
 // ---------------------------------------------------------------------------------------------
+// At most 64 registers (8 blocks of 128 threads per SM): the scan waits on dependent loads, and the
+// extra resident warps hide more of that latency than the spills cost (19% faster on config 2).
 template <int D>
-__global__ void __launch_bounds__(kBlock) k_probe(const NetView* nets, InstState is, Succ sc, Store st, Ctl* ctl,
+__global__ void __launch_bounds__(kBlock, 8) k_probe(const NetView* nets, InstState is, Succ sc, Store st, Ctl* ctl,
                                                   long long nsucc, int mode) {
   Tile<D> t;
   if (!make_tile(t, threadIdx.x & 31)) return;
