@@ -195,6 +195,19 @@ HORA_GB_API int32_t hora_gb_leads_to(const hora_net_desc* net, const hora_pred_d
 HORA_GB_API int32_t hora_gb_exists_invariant(const hora_net_desc* net, const hora_pred_desc* psi, int32_t backend,
                                  hora_stats* stats, int32_t* result);
 
+/* E[] psi with a witness when it holds. No reference counterpart (the reference emits no traces).
+ * The witness is a path of symbolic states of the psi-restricted zone graph from the initial state:
+ * step 0 is the initial state (ords[0] = -1), step i is the successor of step i-1 with emission
+ * ordinal ords[i] (the order of hora_gb_expand with Extra_M+ under the query's bounds), and the run
+ * either ends in a state where it may stop (*loop_to = -1: time diverges inside psi, or a deadlock)
+ * or closes a cycle: the successor of the last step with ordinal *loop_ord is step *loop_to.
+ * Buffers hold cap steps: ords[cap], locs[cap*nprocs], ints[cap*nints], zones[cap*dim*dim];
+ * *nsteps is set (also on HORA_E_OVERFLOW, when the witness needs more). *nsteps = 0 when psi fails. */
+HORA_GB_API int32_t hora_gb_exists_invariant_trace(const hora_net_desc* net, const hora_pred_desc* psi,
+                                       int32_t backend, hora_stats* stats, int32_t* result, int32_t cap,
+                                       int32_t* nsteps, int32_t* ords, int32_t* locs, int32_t* ints,
+                                       int32_t* zones, int32_t* loop_to, int32_t* loop_ord);
+
 /* Successor pipeline on host buffers, for differential testing against a CPU implementation.
  * Inputs: n source states (locs[n*nprocs], ints[n*nints], zones[n*dim*dim] canonical, non-empty),
  * the per-clock bounds L, U [dim] used by Extra_LU+, the query clock mask qmask [dim] (1 = the

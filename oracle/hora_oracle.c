@@ -1102,8 +1102,7 @@ static int goal_hit(const Model* m, const Goal* g, const int32_t* locs, const in
   if (g->kind == 1) return state_has_deadlock(m, locs, ints, zone);
   const hora_pred_desc* t = g->target;
   if (t->never) return 0;
-  for (int k = 0; k < t->nloc; ++k) if (locs[t->loc_req[2 * k]] != t->loc_req[2 * k + 1]) return 0;
-  if (!ints_ok(t->int_cond, t->nint, ints)) return 0;
+  if (!disc_match(t, locs, ints)) return 0;
   int32_t z[64 * 64];
   memcpy(z, zone, sizeof(int32_t) * m->dim * m->dim);
   return apply_cons(z, m->dim, t->clk_cond, 0, t->nclk);
@@ -1589,4 +1588,62 @@ int32_t orc_leads_to(const hora_net_desc* net, const hora_pred_desc* p, const ho
 int32_t orc_exists_invariant(const hora_net_desc* net, const hora_pred_desc* psi, hora_stats* st,
                              int32_t* result) {
   return liveness_core(net, NULL, NULL, psi, st, result);
+}
+
+/* ---- E[] psi witness replay: the psi-restricted model the E[] route explores ---- */
+static int eg_model(const hora_net_desc* net, const hora_pred_desc* psi, Model* m, uint8_t* qmask) {
+  int rc = model_build(net, m);
+  if (rc) return rc;
+  const int dim = m->dim;
+  memset(qmask, 0, 64);
+  for (int k = 0; k < psi->nclk; ++k) {
+    const int i = psi->clk_cond[3 * k], j = psi->clk_cond[3 * k + 1], v = r_bound(psi->clk_cond[3 * k + 2]);
+    if (i > 0) qmask[i] = 1;
+    if (j > 0) qmask[j] = 1;
+    const int a = v < 0 ? -v : v, x = i > 0 ? i : j;
+    m->L[x] = imax(m->L[x], a); m->U[x] = imax(m->U[x], a);
+  }
+  for (int c = 0; c < dim; ++c) m->L[c] = m->U[c] = imax(m->L[c], m->U[c]);
+  for (int k = 0; k < m->nlocs_total * dim; ++k) m->Lloc[k] = m->Uloc[k] = imax(m->Lloc[k], m->Uloc[k]);
+  m->L[0] = m->U[0] = 0;
+  m->avoid = psi;
+  m->avoid_psi = 1;
+  return HORA_OK;
+}
+
+/* Step 0 of an E[] psi witness: the psi-restricted initial state. Returns 1 when it exists. */
+int32_t orc_eg_initial(const hora_net_desc* net, const hora_pred_desc* psi, int32_t* locs, int32_t* ints,
+                       int32_t* zone) {
+  Model m;
+  uint8_t qmask[64];
+  if (eg_model(net, psi, &m, qmask)) { model_free(&m); return 0; }
+  for (int p = 0; p < net->nprocs; ++p) locs[p] = net->proc_init[p];
+  for (int v = 0; v < net->nints; ++v) ints[v] = net->int_init[v];
+  orc_dbm_init(zone, m.dim);
+  const int ok = close_succ_zone(&m, locs, ints, zone, qmask, m.L, m.U, 0) && !orc_dbm_empty(zone, m.dim);
+  model_free(&m);
+  return ok;
+}
+
+/* The successors the E[] psi graph gives a state, in emission order (Extra_M+ under the query's
+ * bounds, the psi restriction applied). Writes at most cap of them; *n = their number. */
+int32_t orc_eg_successors(const hora_net_desc* net, const hora_pred_desc* psi, const int32_t* locs,
+                          const int32_t* ints, const int32_t* zone, int32_t cap, int32_t* out_locs,
+                          int32_t* out_ints, int32_t* out_zones, int32_t* n) {
+  Model m;
+  uint8_t qmask[64];
+  int rc = eg_model(net, psi, &m, qmask);
+  if (rc) { model_free(&m); return rc; }
+  SuccBuf B = {0};
+  B.np = net->nprocs; B.ni = net->nints; B.d2 = m.dim * m.dim;
+  successors(&m, locs, ints, zone, m.L, m.U, qmask, 1, sb_emit, &B);
+  *n = B.n;
+  for (int k = 0; k < B.n && k < cap; ++k) {
+    memcpy(out_locs + (size_t)k * B.np, B.locs + (size_t)k * B.np, sizeof(int32_t) * B.np);
+    if (B.ni) memcpy(out_ints + (size_t)k * B.ni, B.ints + (size_t)k * B.ni, sizeof(int32_t) * B.ni);
+    memcpy(out_zones + (size_t)k * B.d2, B.zones + (size_t)k * B.d2, sizeof(int32_t) * B.d2);
+  }
+  free(B.locs); free(B.ints); free(B.zones);
+  model_free(&m);
+  return HORA_OK;
 }

@@ -68,6 +68,13 @@ int32_t orc_leads_to(const hora_net_desc* net, const hora_pred_desc* p, const ho
                      hora_stats* st, int32_t* result);
 int32_t orc_exists_invariant(const hora_net_desc* net, const hora_pred_desc* psi, hora_stats* st,
                              int32_t* result);
+/* Replay of an E[] psi witness: the restricted initial state, and a state's successors in the
+ * restricted graph in emission order. */
+int32_t orc_eg_initial(const hora_net_desc* net, const hora_pred_desc* psi, int32_t* locs, int32_t* ints,
+                       int32_t* zone);
+int32_t orc_eg_successors(const hora_net_desc* net, const hora_pred_desc* psi, const int32_t* locs,
+                          const int32_t* ints, const int32_t* zone, int32_t cap, int32_t* out_locs,
+                          int32_t* out_ints, int32_t* out_zones, int32_t* n);
 
 /* Stop whole-query runs after the first BFS level that ends past `seconds` (0 = no limit); the run
  * then reports status HORA_E_TIMEOUT with the counters reached so far. Used to bound the CPU

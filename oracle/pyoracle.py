@@ -55,6 +55,9 @@ def lib():
         L.orc_deadlock_reachable.argtypes = [VP, VP, P32]; L.orc_deadlock_reachable.restype = I32
         L.orc_leads_to.argtypes = [VP, VP, VP, VP, P32]; L.orc_leads_to.restype = I32
         L.orc_exists_invariant.argtypes = [VP, VP, VP, P32]; L.orc_exists_invariant.restype = I32
+        L.orc_eg_initial.argtypes = [VP, VP, P32, P32, P32]; L.orc_eg_initial.restype = I32
+        L.orc_eg_successors.argtypes = [VP, VP, P32, P32, P32, I32, P32, P32, P32, P32]
+        L.orc_eg_successors.restype = I32
         L.orc_initial_state.argtypes = [VP, ctypes.POINTER(ctypes.c_uint8), P32, P32, P32]
         L.orc_initial_state.restype = I32
         L.orc_set_time_limit.argtypes = [ctypes.c_double]
@@ -227,6 +230,34 @@ def exists_invariant(net: Network, psi: Pred):
     if rc or st.status not in (0, 5):
         raise RuntimeError(f"oracle exists_invariant status {rc}")
     return bool(res.value), st.as_dict()
+
+
+def eg_initial(net: Network, psi: Pred):
+    """The psi-restricted initial state (locs, ints, zone), or None."""
+    na, pa = NetArrays(net), PredArrays(psi)
+    locs = np.zeros(max(len(net.procs), 1), np.int32)
+    ints = np.zeros(max(len(net.ints), 1), np.int32)
+    zone = np.zeros(net.dim * net.dim, np.int32)
+    ok = lib().orc_eg_initial(ctypes.addressof(na.desc), ctypes.addressof(pa.desc), _p(locs), _p(ints), _p(zone))
+    return (locs[:len(net.procs)], ints[:len(net.ints)], zone.reshape(net.dim, net.dim)) if ok else None
+
+
+def eg_successors(net: Network, psi: Pred, locs, ints, zone):
+    """Successors of one state in the psi-restricted graph, in emission order: (locs, ints, zones)."""
+    na, pa = NetArrays(net), PredArrays(psi)
+    np_, ni, d2 = len(net.procs), len(net.ints), net.dim * net.dim
+    l = np.ascontiguousarray(locs, np.int32).reshape(-1)
+    i = np.ascontiguousarray(ints, np.int32).reshape(-1) if ni else np.zeros(1, np.int32)
+    z = np.ascontiguousarray(zone, np.int32).reshape(-1)
+    cap = 4096
+    ol, oi, oz = np.zeros(cap * max(np_, 1), np.int32), np.zeros(cap * max(ni, 1), np.int32), np.zeros(cap * d2, np.int32)
+    n = ctypes.c_int32(0)
+    rc = lib().orc_eg_successors(ctypes.addressof(na.desc), ctypes.addressof(pa.desc), _p(l), _p(i), _p(z), cap,
+                                 _p(ol), _p(oi), _p(oz), ctypes.byref(n))
+    if rc or n.value > cap:
+        raise RuntimeError(f"oracle eg_successors status {rc}")
+    k = n.value
+    return ol[:k * np_].reshape(k, np_), oi[:k * ni].reshape(k, ni), oz[:k * d2].reshape(k, net.dim, net.dim)
 
 
 def leads_to(net: Network, p: Pred, q: Pred):

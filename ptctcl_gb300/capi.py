@@ -16,7 +16,8 @@ BACKEND_SEQ, BACKEND_OMP, BACKEND_CUDA, BACKEND_METAL = range(4)
 
 EXPORTS = (
     "hora_gb_last_error", "hora_gb_abi_version", "hora_gb_device_count", "hora_gb_reachable_net",
-    "hora_gb_deadlock_reachable", "hora_gb_leads_to", "hora_gb_exists_invariant", "hora_gb_expand",
+    "hora_gb_deadlock_reachable", "hora_gb_leads_to", "hora_gb_exists_invariant",
+    "hora_gb_exists_invariant_trace", "hora_gb_expand",
     "hora_gb_has_deadlock",
     "hora_gb_batch_run", "hora_gb_server_create", "hora_gb_server_submit", "hora_gb_server_step",
     "hora_gb_server_poll", "hora_gb_server_destroy", "hora_gb_has_deadlock_noalloc",
@@ -56,6 +57,9 @@ def load(build_if_missing: bool = True):
     L.hora_gb_leads_to.restype = I32
     L.hora_gb_exists_invariant.argtypes = [VP, VP, I32, VP, ctypes.POINTER(I32)]
     L.hora_gb_exists_invariant.restype = I32
+    L.hora_gb_exists_invariant_trace.argtypes = [VP, VP, I32, VP, ctypes.POINTER(I32), I32, ctypes.POINTER(I32),
+                                                 P32, P32, P32, P32, ctypes.POINTER(I32), ctypes.POINTER(I32)]
+    L.hora_gb_exists_invariant_trace.restype = I32
     L.hora_gb_expand.argtypes = [VP, I32, P32, P32, P32, P32, P32, ctypes.POINTER(ctypes.c_uint8), I32, I64,
                                  P32, P32, P32, P32, P32, ctypes.POINTER(I64)]
     L.hora_gb_expand.restype = I32

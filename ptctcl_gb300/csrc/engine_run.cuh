@@ -132,7 +132,7 @@ struct Engine {
   long long ccap = 0;
   DBuf fkey[2], fnode[2], frank[2], finst[2];
   long long fcapb[2] = {0, 0};
-  DBuf esrc, edst;
+  DBuf esrc, edst, eord;
   long long ecap = 0;
   int merge_blocks = 0;         // resident blocks of the merge kernel (it schedules keys itself)
   DBuf hv_n, hv_a, hv_cb, hv_bm, hv_bounds, hv_pool, hv_prefix;   // keys merged block-wide
@@ -195,7 +195,7 @@ struct Engine {
     f.rank = frank[b].template as<int>(); f.inst = finst[b].template as<int>();
     return f;
   }
-  Edges edges() { return Edges{esrc.template as<int>(), edst.template as<int>(), ecap}; }
+  Edges edges() { return Edges{esrc.template as<int>(), edst.template as<int>(), eord.template as<int>(), ecap}; }
   ZTab ztab() { return ZTab{zw.template as<unsigned long long>(), zcap - 1}; }
   InstState istate() {
     InstState is;
@@ -383,6 +383,7 @@ struct Engine {
     const size_t used = (size_t)std::min<unsigned long long>(hctl.nedges, (unsigned long long)ecap);
     HGB_CUDA(esrc.grow(c * 4, used * 4, s));
     HGB_CUDA(edst.grow(c * 4, used * 4, s));
+    HGB_CUDA(eord.grow(c * 4, used * 4, s));
     ecap = c;
     return HORA_OK;
   }
@@ -814,6 +815,74 @@ struct Engine {
     if ((rc = read_ctl())) return rc;
     gfp_iters = iters;
     pre_calls = (unsigned long long)ne;
+    if (o.trace && ninst == 1 && nets[0]->kind == HORA_Q_EG)
+      return extract_trace(n2, ne, W.template as<int>(), stop.template as<int>());
+    return HORA_OK;
+  }
+
+  // E[] psi witness: from a surviving root, follow edges into W until a stop node or a node seen
+  // before. Every node of W is a stop node or has an edge into W (the fixpoint), so the walk ends.
+  int extract_trace(long long n2, long long ne, const int* dW, const int* dstop) {
+    Trace& T = *o.trace;
+    std::vector<int> hW((size_t)n2), hstop((size_t)n2), hlev((size_t)n2), es((size_t)ne), ed((size_t)ne), eo((size_t)ne);
+    std::vector<unsigned long long> hkey((size_t)n2);
+    if (n2 > 0) {
+      HGB_CUDA(cudaMemcpyAsync(hW.data(), dW, n2 * 4, cudaMemcpyDeviceToHost, s));
+      HGB_CUDA(cudaMemcpyAsync(hstop.data(), dstop, n2 * 4, cudaMemcpyDeviceToHost, s));
+      HGB_CUDA(cudaMemcpyAsync(hlev.data(), S[1].nlevel.p, n2 * 4, cudaMemcpyDeviceToHost, s));
+      HGB_CUDA(cudaMemcpyAsync(hkey.data(), S[1].nkey.p, n2 * 8, cudaMemcpyDeviceToHost, s));
+    }
+    if (ne > 0) {
+      HGB_CUDA(cudaMemcpyAsync(es.data(), esrc.p, ne * 4, cudaMemcpyDeviceToHost, s));
+      HGB_CUDA(cudaMemcpyAsync(ed.data(), edst.p, ne * 4, cudaMemcpyDeviceToHost, s));
+      HGB_CUDA(cudaMemcpyAsync(eo.data(), eord.p, ne * 4, cudaMemcpyDeviceToHost, s));
+    }
+    HGB_CUDA(cudaStreamSynchronize(s));
+    d2h += (size_t)n2 * 20 + (size_t)ne * 12;
+    int root = -1;
+    for (long long u = 0; u < n2 && root < 0; ++u)
+      if (hW[u] && hlev[u] == 0) root = (int)u;
+    T = Trace{};
+    if (root < 0) return HORA_OK;
+    std::vector<long long> off((size_t)n2 + 1, 0);   // edges by source
+    for (long long e = 0; e < ne; ++e) off[es[e] + 1]++;
+    for (long long u = 0; u < n2; ++u) off[u + 1] += off[u];
+    std::vector<long long> fill(off.begin(), off.end() - 1), byu((size_t)ne);
+    for (long long e = 0; e < ne; ++e) byu[fill[es[e]]++] = e;
+    std::vector<int> path, pord;
+    std::vector<int> seen((size_t)n2, -1);
+    int u = root, ord = -1;
+    for (;;) {
+      seen[u] = (int)path.size();
+      path.push_back(u);
+      pord.push_back(ord);
+      if (hstop[u]) break;
+      long long pick = -1;
+      for (long long k = off[u]; k < off[u + 1] && pick < 0; ++k)
+        if (hW[ed[byu[k]]]) pick = byu[k];
+      if (pick < 0) { err = "witness walk left the fixpoint"; return HORA_E_CUDA; }
+      const int v = ed[pick];
+      if (seen[v] >= 0) { T.loop_to = seen[v]; T.loop_ord = eo[pick]; break; }
+      u = v;
+      ord = eo[pick];
+    }
+    const HostNet& H = *nets[0];
+    const int np = H.nprocs, ni = H.nints;
+    T.nsteps = (int)path.size();
+    T.ords = pord;
+    T.locs.resize((size_t)T.nsteps * np);
+    T.ints.resize((size_t)T.nsteps * std::max(ni, 0));
+    T.zones.resize((size_t)T.nsteps * Z2);
+    for (int i = 0; i < T.nsteps; ++i) {
+      HGB_CUDA(cudaMemcpyAsync(T.zones.data() + (size_t)i * Z2, S[1].nzone.template as<int>() + (long long)path[i] * Z2,
+                               Z2 * 4, cudaMemcpyDeviceToHost, s));
+      const unsigned long long k = hkey[path[i]] & ((1ull << inst_shift) - 1);
+      for (int p = 0; p < np; ++p)
+        T.locs[(size_t)i * np + p] = (int)((k >> H.kshift[p]) & ((1ull << H.kwidth[p]) - 1));
+      for (int v = 0; v < ni; ++v)
+        T.ints[(size_t)i * ni + v] = (int)((k >> H.kshift[np + v]) & ((1ull << H.kwidth[np + v]) - 1)) + H.int_lo[v];
+    }
+    HGB_CUDA(cudaStreamSynchronize(s));
     return HORA_OK;
   }
   unsigned long long gfp_iters = 0, pre_calls = 0;

@@ -492,7 +492,7 @@ int32_t hora_gb_device_count(int32_t* count) {
 
 static int32_t run_single(const hora_net_desc* net, int kind, const hora_pred_desc* target,
                           const hora_pred_desc* qpred, int32_t backend, hora_stats* stats,
-                          const volatile int32_t* cancel, int32_t* result) {
+                          const volatile int32_t* cancel, int32_t* result, Trace* trace = nullptr) {
   g_last_error.clear();
   if (!result) return fail(HORA_E_INVALID, "null result pointer");
   if (backend != HORA_BACKEND_CUDA) return fail(HORA_E_NOT_SUPPORTED, "this library implements the cuda backend only");
@@ -503,7 +503,8 @@ static int32_t run_single(const hora_net_desc* net, int kind, const hora_pred_de
   if ((rc = ensure_device())) return rc;
   std::vector<const HostNet*> v{&H};
   std::vector<InstResult> res;
-  const RunOptions o = run_options(cancel);
+  RunOptions o = run_options(cancel);
+  o.trace = trace;
   rc = dispatch_group(H.dim, v, res, o, err);
   if (!res.empty()) stats_out(stats, res[0].st);
   if (rc) return fail(rc, err);
@@ -532,6 +533,27 @@ int32_t hora_gb_exists_invariant(const hora_net_desc* net, const hora_pred_desc*
                                  hora_stats* stats, int32_t* result) {
   if (!psi) return fail(HORA_E_INVALID, "null predicate");
   return run_single(net, HORA_Q_EG, psi, nullptr, backend, stats, nullptr, result);
+}
+
+int32_t hora_gb_exists_invariant_trace(const hora_net_desc* net, const hora_pred_desc* psi, int32_t backend,
+                                       hora_stats* stats, int32_t* result, int32_t cap, int32_t* nsteps,
+                                       int32_t* ords, int32_t* locs, int32_t* ints, int32_t* zones,
+                                       int32_t* loop_to, int32_t* loop_ord) {
+  if (!psi || !nsteps || !loop_to || !loop_ord || cap < 0) return fail(HORA_E_INVALID, "bad arguments");
+  Trace T;
+  const int32_t rc = run_single(net, HORA_Q_EG, psi, nullptr, backend, stats, nullptr, result, &T);
+  if (rc) return rc;
+  *nsteps = T.nsteps;
+  *loop_to = T.loop_to;
+  *loop_ord = T.loop_ord;
+  if (T.nsteps > cap) return fail(HORA_E_OVERFLOW, "the witness has more steps than the buffers hold");
+  if (T.nsteps > 0 && (!ords || !locs || !zones || (T.ints.size() && !ints)))
+    return fail(HORA_E_INVALID, "null trace buffer");
+  std::copy(T.ords.begin(), T.ords.end(), ords);
+  std::copy(T.locs.begin(), T.locs.end(), locs);
+  if (!T.ints.empty()) std::copy(T.ints.begin(), T.ints.end(), ints);
+  std::copy(T.zones.begin(), T.zones.end(), zones);
+  return HORA_OK;
 }
 
 int32_t hora_gb_expand(const hora_net_desc* net, int32_t n, const int32_t* locs, const int32_t* ints,

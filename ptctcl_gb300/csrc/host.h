@@ -61,6 +61,14 @@ struct InstResult {
   hora_stats st{};
 };
 
+// A witness of E[] psi read back from the exact zone graph: the states of a path from the root, each
+// reached from the previous one by its emission ordinal, ending in a stop state (loop_to = -1) or
+// closing a cycle into state loop_to by ordinal loop_ord.
+struct Trace {
+  std::vector<int32_t> ords, locs, ints, zones;
+  int loop_to = -1, loop_ord = -1, nsteps = 0;
+};
+
 struct RunOptions {
   int blocks = 0;             // grid cap for the level kernels (0: derived from the SM count)
   const volatile int32_t* cancel = nullptr;
@@ -69,6 +77,7 @@ struct RunOptions {
   size_t store_budget_bytes = 0;  // 0: unbounded; else instances stop with HORA_E_BUDGET past it
   bool has_t_call = false;    // per-instance times count from t_call (the batch call) when set
   std::chrono::steady_clock::time_point t_call{};
+  Trace* trace = nullptr;     // E[] psi, one instance: fill with a witness when it holds
 };
 
 // Run a group of instances that share the DBM dimension D (one level-synchronous BFS over all of

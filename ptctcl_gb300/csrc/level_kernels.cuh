@@ -28,6 +28,7 @@ struct Store {
 struct Edges {                // zone-graph edges (leads-to graph mode)
   int* src;
   int* dst;
+  int* ord;                   // emission ordinal of the successor the edge came from
   long long cap;
 };
 struct HeavyKeys {            // per key merged block-wide (index j of Succ::heavy)

@@ -1059,7 +1059,7 @@ static __global__ void k_graph_edges(Succ sc, Front fr, Edges ed, Ctl* ctl, long
       node = (r & kZRefSucc) ? sc.rank[r & ~kZRefSucc] : (int)r;
     }
     const unsigned long long e = atomicAdd(&ctl->nedges, 1ull);
-    if ((long long)e < ed.cap) { ed.src[e] = fr.node[sc.parent[s]]; ed.dst[e] = node; }
+    if ((long long)e < ed.cap) { ed.src[e] = fr.node[sc.parent[s]]; ed.dst[e] = node; ed.ord[e] = sc.ord[s]; }
     else atomicMax(&ctl->err, 4u);
   }
 }

@@ -117,6 +117,31 @@ def exists_invariant_run(net: Network, psi: Pred, backend: Backend = Backend.Cud
     return bool(res.value)
 
 
+def exists_invariant_trace(net: Network, psi: Pred, backend: Backend = Backend.Cuda, cap: int = 1 << 16):
+    """E[] psi with a witness: (holds, trace) where trace = dict(ords, locs, ints, zones, loop_to,
+    loop_ord) or None when psi fails (see hora_gb_exists_invariant_trace)."""
+    L = capi.load()
+    na, pa = NetArrays(net), PredArrays(psi)
+    np_, ni, d2 = len(net.procs), len(net.ints), net.dim * net.dim
+    st = Stats()
+    res, n, lt, lo = ctypes.c_int32(0), ctypes.c_int32(0), ctypes.c_int32(0), ctypes.c_int32(0)
+    ords = np.zeros(max(cap, 1), np.int32)
+    locs = np.zeros(max(cap * np_, 1), np.int32)
+    ints = np.zeros(max(cap * ni, 1), np.int32)
+    zones = np.zeros(max(cap * d2, 1), np.int32)
+    rc = L.hora_gb_exists_invariant_trace(ctypes.addressof(na.desc), ctypes.addressof(pa.desc), int(backend),
+                                          ctypes.byref(st), ctypes.byref(res), cap, ctypes.byref(n),
+                                          capi.p32(ords), capi.p32(locs), capi.p32(ints), capi.p32(zones),
+                                          ctypes.byref(lt), ctypes.byref(lo))
+    capi.check(rc, "exists_invariant_trace")
+    k = n.value
+    if not res.value or k == 0:
+        return bool(res.value), None
+    return True, {"ords": ords[:k].tolist(), "locs": locs[:k * np_].reshape(k, np_),
+                  "ints": ints[:k * ni].reshape(k, ni), "zones": zones[:k * d2].reshape(k, net.dim, net.dim),
+                  "loop_to": lt.value, "loop_ord": lo.value}
+
+
 def check_network_query(net: Network, kind: int, p: Pred, q: Optional[Pred] = None, negate: bool = False,
                         backend: Backend = Backend.Cuda, stats: Optional[ReachStats] = None) -> bool:
     """Route one lowered query (check_network_query, src/query/dispatch.cpp:109-607).
