@@ -676,7 +676,7 @@ struct Engine {
     // ---- probe
     if (nsucc > 0) {
       kt.begin(s);
-      Level<D>::probe(V, is, succ(), store(k), dctl(), nsucc, mode, blocks, s);
+      Level<D>::probe(V, is, succ(), store(k), dctl(), nsucc, blocks, s);
       kt.end(s, KT_PROBE);
       ++launches;
       HGB_CUDA(cudaGetLastError());

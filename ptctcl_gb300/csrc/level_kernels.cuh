@@ -85,15 +85,15 @@ struct InstState {            // per-instance device state (one entry per instan
 
 template <int D>
 struct Level {
-  // mode: 0 = a_LU subsumption store (reach, deadlock, leads-to phase 1),
-  //       1 = exact-zone graph store with edges (leads-to phase 2)
+  // Store 0 is the a_LU subsumption store (reach, deadlock, leads-to phase 1) fed by probe, group and
+  // merge; store 1 the exact-zone graph (leads-to phase 2, E[]) fed by the graph_* kernels.
   static void init(const NetView* nets, int ninst, const int* inst_dim_ok, Store st, Front out, InstState is,
                    Ctl* ctl, cudaStream_t s);
   // expands the frontier entries of instances [i0, i1)
   static void expand(const NetView* nets, InstState is, Front fr, int nfront, const int* src_zone, Succ sc, Ctl* ctl,
                      int roots, int i0, int i1, int blocks, cudaStream_t s);
-  static void probe(const NetView* nets, InstState is, Succ sc, Store st, Ctl* ctl, long long nsucc, int mode,
-                    int blocks, cudaStream_t s);
+  static void probe(const NetView* nets, InstState is, Succ sc, Store st, Ctl* ctl, long long nsucc, int blocks,
+                    cudaStream_t s);
   static void deadlock(const NetView* nets, InstState is, Succ sc, Ctl* ctl, long long n, int all, int blocks,
                        cudaStream_t s);
   static void group(Succ sc, Store st, Ctl* ctl, long long nsucc, long long ntouched, cudaStream_t s);

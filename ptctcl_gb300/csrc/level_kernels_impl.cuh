@@ -162,7 +162,7 @@ __global__ void __launch_bounds__(kBlock) k_expand(const NetView* nets, InstStat
 // extra resident warps hide more of that latency than the spills cost (19% faster on config 2).
 template <int D>
 __global__ void __launch_bounds__(kBlock, 8) k_probe(const NetView* nets, InstState is, Succ sc, Store st, Ctl* ctl,
-                                                  long long nsucc, int mode) {
+                                                  long long nsucc) {
   Tile<D> t;
   if (!make_tile(t, threadIdx.x & 31)) return;
   const int ishift = nets[0].inst_shift;
@@ -192,7 +192,7 @@ __global__ void __launch_bounds__(kBlock, 8) k_probe(const NetView* nets, InstSt
     if (slot < 0) { if (t.i == 0) { atomicMax(&ctl->err, 4u); sc.slot[s] = -1; } continue; }
     bool killed = false;
     unsigned long long nprobe = 0;
-    if (!inserted && mode == 0) {
+    if (!inserted) {
       // the lanes take the key's live zones in turn, newest first, each deciding a whole a_LU test
       int Lall[D];
 #pragma unroll
@@ -1253,10 +1253,10 @@ void Level<D>::expand(const NetView* nets, InstState is, Front fr, int nfront, c
   k_expand<D><<<grid_for(nfront, TPB, blocks), kBlock, 0, s>>>(nets, is, fr, nfront, src_zone, sc, ctl, roots, i0, i1);
 }
 template <int D>
-void Level<D>::probe(const NetView* nets, InstState is, Succ sc, Store st, Ctl* ctl, long long nsucc, int mode,
-                     int blocks, cudaStream_t s) {
+void Level<D>::probe(const NetView* nets, InstState is, Succ sc, Store st, Ctl* ctl, long long nsucc, int blocks,
+                     cudaStream_t s) {
   constexpr int TPB = (kBlock / 32) * (32 / D);
-  k_probe<D><<<grid_for(nsucc, TPB, blocks), kBlock, 0, s>>>(nets, is, sc, st, ctl, nsucc, mode);
+  k_probe<D><<<grid_for(nsucc, TPB, blocks), kBlock, 0, s>>>(nets, is, sc, st, ctl, nsucc);
 }
 template <int D>
 void Level<D>::deadlock(const NetView* nets, InstState is, Succ sc, Ctl* ctl, long long n, int all, int blocks,
