@@ -135,9 +135,9 @@ struct Engine {
   DBuf esrc, edst, eord;
   long long ecap = 0;
   int merge_blocks = 0;         // resident blocks of the merge kernel (it schedules keys itself)
-  DBuf hv_n, hv_a, hv_cb, hv_bm, hv_bounds, hv_pool, hv_prefix;   // keys merged block-wide
+  DBuf hv_n, hv_a, hv_cb, hv_bm, hv_bounds, hv_pool, hv_prefix, hv_order;   // keys merged block-wide
   long long hv_cap = 0, pool_cap = 0, prefix_cap = 0;
-  std::vector<int> h_hn, h_ha;
+  std::vector<int> h_hn, h_ha, h_order;
   std::vector<long long> h_hbm, h_prefix;
   DBuf zw;                      // exact-zone table of the graph store
   unsigned long long zcap = 0;
@@ -581,8 +581,18 @@ struct Engine {
     HGB_CUDA(cudaMemcpyAsync(h_hn.data(), hv_n.p, nh * 4, cudaMemcpyDeviceToHost, s));
     HGB_CUDA(cudaMemcpyAsync(h_ha.data(), hv_a.p, nh * 4, cudaMemcpyDeviceToHost, s));
     HGB_CUDA(cudaMemcpyAsync(h_hbm.data(), hv_bm.p, nh * 8, cudaMemcpyDeviceToHost, s));
+    HGB_CUDA(cudaStreamSynchronize(s));
+    // Largest keys first: a key's ordered fold is serial, so the level's merge ends no earlier than
+    // its longest key; started first, it runs alongside all the others.
+    h_order.resize(nh);
+    for (long long j = 0; j < nh; ++j) h_order[j] = (int)j;
+    std::stable_sort(h_order.begin(), h_order.end(), [&](int x, int y) {
+      return h_hn[x] != h_hn[y] ? h_hn[x] > h_hn[y] : h_ha[x] > h_ha[y];
+    });
+    HGB_CUDA(cudaMemcpyAsync(hv_order.p, h_order.data(), nh * 4, cudaMemcpyHostToDevice, s));
+    h2d += nh * 4;
     kt.begin(s);
-    Level<D>::heavy_prep(V, is, succ(), store(k), dctl(), nh, merge_blocks, s);
+    Level<D>::heavy_prep(V, is, succ(), store(k), dctl(), nh, merge_blocks, hv_order.template as<int>(), s);
     kt.end(s, KT_MERGE);
     ++launches;
     HGB_CUDA(cudaGetLastError());
@@ -688,6 +698,7 @@ struct Engine {
       long long c = std::max<long long>(hv_cap, 1 << 12);
       while (c < ntouched) c *= 2;
       HGB_CUDA(hv_n.alloc(c * 4)); HGB_CUDA(hv_a.alloc(c * 4)); HGB_CUDA(hv_cb.alloc(c * 8));
+      HGB_CUDA(hv_order.alloc(c * 4));
       HGB_CUDA(hv_bm.alloc(c * 8)); HGB_CUDA(hv_bounds.alloc(c * 2 * D * 4));
       hv_cap = c;
     }
@@ -706,7 +717,7 @@ struct Engine {
         kt.begin(s);
         Level<D>::group(succ(), store(k), dctl(), nsucc, ntouched, s);
         kt.end(s, KT_GROUP, 2);
-        Level<D>::merge(V, is, succ(), store(k), front(cur ^ 1), dctl(), ntouched, level, merge_blocks, s);
+        Level<D>::merge(V, is, succ(), store(k), front(cur ^ 1), dctl(), ntouched, level, merge_blocks, nullptr, s);
         launches += 3;
         HGB_CUDA(cudaGetLastError());
       }
@@ -732,7 +743,8 @@ struct Engine {
       if ((rc = read_ctl())) return rc;
       if ((rc = heavy_relations(V, k))) return rc;
       kt.begin(s);
-      Level<D>::merge(V, is, succ(), store(k), front(cur ^ 1), dctl(), ntouched, level, merge_blocks, s);
+      Level<D>::merge(V, is, succ(), store(k), front(cur ^ 1), dctl(), ntouched, level, merge_blocks,
+                      hctl.nheavy ? hv_order.template as<int>() : nullptr, s);
       kt.end(s, KT_MERGE);
       launches += 1;
       HGB_CUDA(cudaGetLastError());

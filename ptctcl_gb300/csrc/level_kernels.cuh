@@ -97,12 +97,13 @@ struct Level {
   static void deadlock(const NetView* nets, InstState is, Succ sc, Ctl* ctl, long long n, int all, int blocks,
                        cudaStream_t s);
   static void group(Succ sc, Store st, Ctl* ctl, long long nsucc, long long ntouched, cudaStream_t s);
+  // order: the heavy keys' merge order (largest first), or null for their index order
   static void merge(const NetView* nets, InstState is, Succ sc, Store st, Front out, Ctl* ctl, long long ntouched,
-                    int level, int blocks, cudaStream_t s);
+                    int level, int blocks, const int* order, cudaStream_t s);
   static int merge_blocks_per_sm();
   // keys merged block-wide: sort + gather + bounds, then their pairwise relations
   static void heavy_prep(const NetView* nets, InstState is, Succ sc, Store st, Ctl* ctl, long long nheavy,
-                         int blocks, cudaStream_t s);
+                         int blocks, const int* order, cudaStream_t s);
   static int heavy_pairs(const NetView* nets, Succ sc, Store st, const long long* prefix, long long nheavy,
                          long long ntiles, int blocks, cudaStream_t s);
   // exact-zone graph store (leads-to graph mode): deduplicate the successors against the store and

@@ -359,18 +359,24 @@ __device__ __forceinline__ long long alloc_clist(const Succ& sc, const Store& st
   return cb;
 }
 
-// End of a key's merge (one thread): frontier entries, live-only chain, counters.
+// End of a key's merge (one thread): frontier entries (contiguous, newest first), live-only chain,
+// counters.
 __device__ __forceinline__ void finish_key(const Succ& sc, const Store& st, const Front& out, const InstState& is,
                                            Ctl* ctl, int s, unsigned long long hk, int inst, const int* cl,
                                            int clen0, int clen, long long dlive) {
-  int r = 0;
-  for (int k = clen - 1; k >= clen0; --k) {
-    const int m = cl[k];
-    if (m < 0) continue;
-    const unsigned long long f = atomicAdd(&ctl->nfront, 1ull);
-    out.key[f] = hk; out.node[f] = m; out.rank[f] = r++; out.inst[f] = inst;
+  int nnew = 0;
+  for (int k = clen0; k < clen; ++k) nnew += cl[k] >= 0 ? 1 : 0;
+  if (nnew) {
+    const unsigned long long f0 = atomicAdd(&ctl->nfront, (unsigned long long)nnew);
+    int r = 0;
+    for (int k = clen - 1; k >= clen0; --k) {
+      const int m = cl[k];
+      if (m < 0) continue;
+      const unsigned long long f = f0 + r;
+      out.key[f] = hk; out.node[f] = m; out.rank[f] = r++; out.inst[f] = inst;
+    }
+    atomicAdd(&is.nfront[inst], (unsigned long long)nnew);
   }
-  if (r) atomicAdd(&is.nfront[inst], (unsigned long long)r);
   const bool was_empty = st.klive[s] == 0;
   int live = 0;
   for (int k = 0; k < clen; ++k) live += cl[k] >= 0 ? 1 : 0;
@@ -408,6 +414,8 @@ struct MergeShared {
   int win[kMergeScan];  // list positions of the newest live zones, newest first
   long long cb;
   int nw, best, node, retired, clen, job, unioned, nhull, nkeep;
+  int wsum[64];         // per-warp sums of the block-wide finish
+  long long scal[4];    // its frontier base, arena offset, live and new counts
 };
 
 // ---------------------------------------------------------------------------------------------
@@ -493,11 +501,12 @@ static __device__ void sort_segment_block(const Succ& sc, unsigned base, unsigne
 // Sort the key's survivors, gather its live list, its bounds, and clear its relation block.
 template <int D>
 __global__ void __launch_bounds__(kMergeBlock) k_heavy_prep(const NetView* nets, InstState is, Succ sc, Store st,
-                                                            Ctl* ctl, long long nheavy) {
+                                                            Ctl* ctl, long long nheavy, const int* order) {
   Tile<D> t;
   const bool in_tile = make_tile(t, threadIdx.x & 31);
   const int ishift = nets[0].inst_shift;
-  for (long long j = blockIdx.x; j < nheavy; j += gridDim.x) {
+  for (long long jj = blockIdx.x; jj < nheavy; jj += gridDim.x) {
+    const long long j = order ? order[jj] : jj;
     const int s = sc.heavy[j];
     const unsigned long long hk = st.hkey[s];
     const int inst = (int)(hk >> ishift);
@@ -618,12 +627,77 @@ __global__ void __launch_bounds__(kMergeBlock) k_heavy_pairs(const NetView* nets
   }
 }
 
+// End of a block-wide key merge, by the whole block: the key's zones stored at this level go to
+// the frontier ranked newest first (contiguous, so the next expand sees a key's zones together),
+// and its live zones (oldest first) to a fresh arena list.
+static __device__ void finish_key_block(const Store& st, const Front& out, const InstState& is, Ctl* ctl, int s,
+                                        unsigned long long hk, int inst, int clen0, int clen, long long dlive,
+                                        const int* cl, int* wsum, long long* scal) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = blockDim.x >> 5;
+  int nall = 0, nnew = 0;
+  for (int k = tid; k < clen; k += blockDim.x)
+    if (cl[k] >= 0) { ++nall; nnew += k >= clen0 ? 1 : 0; }
+  for (int o = 16; o; o >>= 1) {
+    nall += __shfl_xor_sync(0xffffffffu, nall, o);
+    nnew += __shfl_xor_sync(0xffffffffu, nnew, o);
+  }
+  if (lane == 0) { wsum[warp] = nall; wsum[32 + warp] = nnew; }
+  __syncthreads();
+  if (tid == 0) {
+    int ta = 0, tn = 0;
+    for (int w = 0; w < nwarp; ++w) { ta += wsum[w]; tn += wsum[32 + w]; }
+    scal[0] = tn ? (long long)atomicAdd(&ctl->nfront, (unsigned long long)tn) : 0;
+    if (tn) atomicAdd(&is.nfront[inst], (unsigned long long)tn);
+    const bool was_empty = st.klive[s] == 0;
+    const long long off = (long long)atomicAdd(&ctl->arena_alloc, (unsigned long long)ta);
+    const bool ok = off + ta <= st.acap;
+    if (!ok) atomicMax(&ctl->err, 4u);
+    scal[1] = ok ? off : -1;
+    scal[2] = ta;
+    scal[3] = tn;
+    if (ok) { st.kloff[s] = off; st.klive[s] = ta; }
+    if (was_empty && ta > 0) { atomicAdd(&ctl->nkeys, 1ull); atomicAdd(&is.nkeys[inst], 1ull); }
+    if (dlive) {
+      atomicAdd((unsigned long long*)&ctl->nlive, (unsigned long long)dlive);
+      atomicAdd((unsigned long long*)&is.nlive[inst], (unsigned long long)dlive);
+    }
+    st.pend[s] = 0;
+  }
+  __syncthreads();
+  const long long f0 = scal[0], off = scal[1];
+  const int ta = (int)scal[2], tn = (int)scal[3], nold = ta - tn;
+  int carry = 0;   // live entries before the current chunk
+  for (int c0 = 0; c0 < clen; c0 += blockDim.x) {
+    const int k = c0 + tid;
+    const int m = k < clen ? cl[k] : -1;
+    const bool live = m >= 0;
+    const unsigned b = __ballot_sync(0xffffffffu, live);
+    if (lane == 0) wsum[warp] = __popc(b);
+    __syncthreads();
+    int before = carry + __popc(b & ((1u << lane) - 1u));
+    for (int w = 0; w < nwarp; ++w) {
+      if (w < warp) before += wsum[w];
+      carry += wsum[w];
+    }
+    if (live) {
+      if (off >= 0) st.arena[off + before] = m;
+      if (k >= clen0) {
+        const int r = tn - 1 - (before - nold);
+        const long long f = f0 + r;
+        out.key[f] = hk; out.node[f] = m; out.rank[f] = r; out.inst[f] = inst;
+      }
+    }
+    __syncthreads();
+  }
+}
+
 // One heavy key merged by a whole block, in canonical order (sorted and gathered by k_heavy_prep).
 template <int D>
 __device__ void merge_key_block(const NetView* nets, const InstState& is, const Succ& sc, const Store& st,
                                 const Front& out, Ctl* ctl, long long j, int level, bool in_tile, const Tile<D>& t,
                                 MergeShared<D>& sh) {
   constexpr int TPW = 32 / D;
+  constexpr int DD = D * D;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int ishift = nets[0].inst_shift;
   const int s = sc.heavy[j];
@@ -671,7 +745,7 @@ __device__ void merge_key_block(const NetView* nets, const InstState& is, const 
     int* const zc = sh.zbuf[cur];
     cur ^= 1;
     const int a_s = sc.sorted[base + q];
-    for (int e = tid; e < D * D; e += blockDim.x) zc[e] = sc.zone[(long long)a_s * D * D + e];
+    for (int e = tid; e < DD; e += blockDim.x) zc[e] = sc.zone[(long long)a_s * DD + e];
     if (tid == 0) sh.unioned = 0;
     __syncthreads();
     const int clen = sh.clen, nhull = sh.nhull;
@@ -681,12 +755,12 @@ __device__ void merge_key_block(const NetView* nets, const InstState& is, const 
     if (rel) {
       for (int h = tid; h < nhull && !dropped; h += blockDim.x) {
         const int m = cl[clen0 + hull[h]];
-        if (m >= 0) dropped = alu_le_ptr<D>(zc, st.nzone + (long long)m * D * D, Lr, Ur);
+        if (m >= 0) dropped = alu_le_ptr<D>(zc, st.nzone + (long long)m * DD, Lr, Ur);
       }
     } else {
       for (int k = clen0 + tid; k < clen && !dropped; k += blockDim.x) {
         const int m = cl[k];
-        if (m >= 0) dropped = alu_le_ptr<D>(zc, st.nzone + (long long)m * D * D, Lr, Ur);
+        if (m >= 0) dropped = alu_le_ptr<D>(zc, st.nzone + (long long)m * DD, Lr, Ur);
       }
     }
     if (__syncthreads_or(dropped)) continue;
@@ -710,12 +784,12 @@ __device__ void merge_key_block(const NetView* nets, const InstState& is, const 
       for (int h = tid; h < nhull; h += blockDim.x) {
         const int k = clen0 + hull[h];
         const int m = cl[k];
-        if (m >= 0 && alu_le_ptr<D>(st.nzone + (long long)m * D * D, zc, Lr, Ur)) kill(k);
+        if (m >= 0 && alu_le_ptr<D>(st.nzone + (long long)m * DD, zc, Lr, Ur)) kill(k);
       }
     } else {
       for (int k = tid; k < clen; k += blockDim.x) {
         const int m = cl[k];
-        if (m >= 0 && alu_le_ptr<D>(st.nzone + (long long)m * D * D, zc, Lr, Ur)) kill(k);
+        if (m >= 0 && alu_le_ptr<D>(st.nzone + (long long)m * DD, zc, Lr, Ur)) kill(k);
       }
     }
     if (ret) atomicAdd(&sh.retired, ret);
@@ -749,7 +823,7 @@ __device__ void merge_key_block(const NetView* nets, const InstState& is, const 
           int za[D], zb[D];
 #pragma unroll
           for (int e = 0; e < D; ++e) za[e] = zc[t.i * D + e];
-          load_rows_rw(t, zb, st.nzone + (long long)cl[sh.win[c]] * D * D);
+          load_rows_rw(t, zb, st.nzone + (long long)cl[sh.win[c]] * DD);
           if (try_union(t, za, zb)) {
             mybest = c;
 #pragma unroll
@@ -788,7 +862,7 @@ __device__ void merge_key_block(const NetView* nets, const InstState& is, const 
       sh.clen = clen + 1;
       ++dlive;
     }
-    for (int e = tid; e < D * D; e += blockDim.x) st.nzone[node * D * D + e] = zc[e];
+    for (int e = tid; e < DD; e += blockDim.x) st.nzone[node * DD + e] = zc[e];
     if (tid < D) st.ncol0[node * D + tid] = zc[tid * D];
   }
   for (int u = used + tid; u < sh.nkeep; u += blockDim.x) {   // ids a drop by a hull left unused
@@ -796,8 +870,7 @@ __device__ void merge_key_block(const NetView* nets, const InstState& is, const 
     st.ndead[node] = 1; st.nlevel[node] = -1; st.ninst[node] = inst; st.nkey[node] = hk;
   }
   __syncthreads();
-  if (tid == 0) finish_key(sc, st, out, is, ctl, s, hk, inst, cl, clen0, sh.clen, dlive);
-  __syncthreads();
+  finish_key_block(st, out, is, ctl, s, hk, inst, clen0, sh.clen, tid == 0 ? dlive : 0, cl, sh.wsum, sh.scal);
 }
 
 // One key merged by one tile (keys with little work).
@@ -896,8 +969,8 @@ __device__ void merge_key_tile(const NetView* nets, const InstState& is, const S
 }
 
 template <int D>
-__global__ void __launch_bounds__(kMergeBlock) k_merge(const NetView* nets, InstState is, Succ sc, Store st,
-                                                       Front out, Ctl* ctl, int level) {
+__global__ void __launch_bounds__(kMergeBlock, 2) k_merge(const NetView* nets, InstState is, Succ sc, Store st,
+                                                          Front out, Ctl* ctl, int level, const int* order) {
   __shared__ MergeShared<D> sh;
   Tile<D> t;
   const bool in_tile = make_tile(t, threadIdx.x & 31);
@@ -906,9 +979,10 @@ __global__ void __launch_bounds__(kMergeBlock) k_merge(const NetView* nets, Inst
   for (;;) {
     if (threadIdx.x == 0) sh.job = (int)atomicAdd(&ctl->heavy_next, 1ull);
     __syncthreads();
-    const long long j = sh.job;
+    const long long jj = sh.job;
     __syncthreads();
-    if (j >= nheavy) break;
+    if (jj >= nheavy) break;
+    const long long j = order ? order[jj] : jj;
     merge_key_block<D>(nets, is, sc, st, out, ctl, j, level, in_tile, t, sh);
   }
   // the rest: one tile each, taken in turn
@@ -1271,9 +1345,9 @@ void Level<D>::group(Succ sc, Store st, Ctl* ctl, long long nsucc, long long nto
 }
 template <int D>
 void Level<D>::heavy_prep(const NetView* nets, InstState is, Succ sc, Store st, Ctl* ctl, long long nheavy,
-                          int blocks, cudaStream_t s) {
+                          int blocks, const int* order, cudaStream_t s) {
   const long long g = nheavy < blocks ? nheavy : blocks;
-  if (g > 0) k_heavy_prep<D><<<(int)g, kMergeBlock, 0, s>>>(nets, is, sc, st, ctl, nheavy);
+  if (g > 0) k_heavy_prep<D><<<(int)g, kMergeBlock, 0, s>>>(nets, is, sc, st, ctl, nheavy, order);
 }
 template <int D>
 int Level<D>::heavy_pairs(const NetView* nets, Succ sc, Store st, const long long* prefix, long long nheavy,
@@ -1296,9 +1370,9 @@ int Level<D>::merge_blocks_per_sm() {
 }
 template <int D>
 void Level<D>::merge(const NetView* nets, InstState is, Succ sc, Store st, Front out, Ctl* ctl, long long ntouched,
-                     int level, int blocks, cudaStream_t s) {
+                     int level, int blocks, const int* order, cudaStream_t s) {
   const long long g = ntouched < blocks ? ntouched : blocks;
-  k_merge<D><<<(int)(g > 0 ? g : 1), kMergeBlock, 0, s>>>(nets, is, sc, st, out, ctl, level);
+  k_merge<D><<<(int)(g > 0 ? g : 1), kMergeBlock, 0, s>>>(nets, is, sc, st, out, ctl, level, order);
 }template <int D>
 void Level<D>::graph_probe(const NetView* nets, InstState is, Succ sc, Store st, ZTab zt, Ctl* ctl, long long nsucc,
                            int blocks, cudaStream_t s) {
