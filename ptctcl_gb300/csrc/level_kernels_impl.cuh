@@ -752,10 +752,13 @@ __device__ void merge_key_block(const NetView* nets, const InstState& is, const 
     // (1)+(2): with relations only the hulls stored this level remain to test; without, every
     // zone stored this level
     bool dropped = false;
+    // A zone stored at position clen0 + u of this fold has node id node_base + u, so a hull's zone
+    // and liveness load without going through the list.
     if (rel) {
       for (int h = tid; h < nhull && !dropped; h += blockDim.x) {
-        const int m = cl[clen0 + hull[h]];
-        if (m >= 0) dropped = alu_le_ptr<D>(zc, st.nzone + (long long)m * DD, Lr, Ur);
+        const long long m = node_base + hull[h];
+        const bool live = !st.ndead[m];
+        dropped = alu_le_ptr<D>(zc, st.nzone + m * DD, Lr, Ur) && live;
       }
     } else {
       for (int k = clen0 + tid; k < clen && !dropped; k += blockDim.x) {
@@ -782,9 +785,10 @@ __device__ void merge_key_block(const NetView* nets, const InstState& is, const 
           if (p >= 0) kill(clen0 + p);
         }
       for (int h = tid; h < nhull; h += blockDim.x) {
-        const int k = clen0 + hull[h];
-        const int m = cl[k];
-        if (m >= 0 && alu_le_ptr<D>(st.nzone + (long long)m * DD, zc, Lr, Ur)) kill(k);
+        const int u = hull[h];
+        const long long m = node_base + u;
+        const bool live = !st.ndead[m];
+        if (alu_le_ptr<D>(st.nzone + m * DD, zc, Lr, Ur) && live) kill(clen0 + u);
       }
     } else {
       for (int k = tid; k < clen; k += blockDim.x) {
@@ -823,7 +827,9 @@ __device__ void merge_key_block(const NetView* nets, const InstState& is, const 
           int za[D], zb[D];
 #pragma unroll
           for (int e = 0; e < D; ++e) za[e] = zc[t.i * D + e];
-          load_rows_rw(t, zb, st.nzone + (long long)cl[sh.win[c]] * DD);
+          const int k = sh.win[c];
+          const long long m = k >= clen0 ? node_base + (k - clen0) : (long long)cl[k];
+          load_rows_rw(t, zb, st.nzone + m * DD);
           if (try_union(t, za, zb)) {
             mybest = c;
 #pragma unroll
