@@ -240,6 +240,25 @@ HORA_GB_API int32_t hora_gb_has_deadlock(const hora_net_desc* net, int32_t n, co
 HORA_GB_API int32_t hora_gb_has_deadlock_noalloc(const hora_net_desc* net, int32_t n, const int32_t* d_locs,
                                                  const int32_t* d_ints, const int32_t* d_zones, int32_t* d_out);
 
+/* ---- handle form ------------------------------------------------------------------------------- */
+
+/* One (network, query) pair opened once and run on demand; no reference counterpart beyond the
+ * single-query entry points above, which it routes to by the query's kind.
+ * hora_gb_open validates and copies both descriptors (the caller's arrays may be freed afterwards):
+ * out-of-scope input returns HORA_E_NOT_SUPPORTED or HORA_E_INVALID there, before any device is
+ * touched. hora_gb_run runs the query on the CUDA backend; *verdict follows the single-query
+ * convention of hora_gb_batch_run (reach: reachable; deadlock: deadlock reachable; leads-to and
+ * E[]: holds). hora_gb_trace copies the witness of the last run of an E[] query, with the buffers
+ * and conventions of hora_gb_exists_invariant_trace (*nsteps = 0 when psi fails); other kinds
+ * return HORA_E_NOT_SUPPORTED, and a handle that has not run returns HORA_E_INVALID. A handle is
+ * used by one thread at a time. */
+typedef struct hora_handle_s* hora_handle;
+HORA_GB_API int32_t hora_gb_open(const hora_net_desc* net, const hora_query_desc* q, hora_handle* out);
+HORA_GB_API int32_t hora_gb_run(hora_handle h, int32_t* verdict, hora_stats* stats);
+HORA_GB_API int32_t hora_gb_trace(hora_handle h, int32_t cap, int32_t* nsteps, int32_t* ords, int32_t* locs,
+                                  int32_t* ints, int32_t* zones, int32_t* loop_to, int32_t* loop_ord);
+HORA_GB_API int32_t hora_gb_close(hora_handle h);
+
 /* ---- batched form ----------------------------------------------------------------------------- */
 
 /* Run n independent (network, query) instances together on the device. verdicts[k] receives the

@@ -21,6 +21,7 @@ EXPORTS = (
     "hora_gb_has_deadlock",
     "hora_gb_batch_run", "hora_gb_server_create", "hora_gb_server_submit", "hora_gb_server_step",
     "hora_gb_server_poll", "hora_gb_server_destroy", "hora_gb_has_deadlock_noalloc",
+    "hora_gb_open", "hora_gb_run", "hora_gb_trace", "hora_gb_close",
 )
 
 _lib = None
@@ -67,6 +68,15 @@ def load(build_if_missing: bool = True):
     L.hora_gb_has_deadlock.restype = I32
     L.hora_gb_has_deadlock_noalloc.argtypes = [VP, I32, VP, VP, VP, VP]
     L.hora_gb_has_deadlock_noalloc.restype = I32
+    L.hora_gb_open.argtypes = [VP, VP, ctypes.POINTER(VP)]
+    L.hora_gb_open.restype = I32
+    L.hora_gb_run.argtypes = [VP, ctypes.POINTER(I32), VP]
+    L.hora_gb_run.restype = I32
+    L.hora_gb_trace.argtypes = [VP, I32, ctypes.POINTER(I32), P32, P32, P32, P32, ctypes.POINTER(I32),
+                                ctypes.POINTER(I32)]
+    L.hora_gb_trace.restype = I32
+    L.hora_gb_close.argtypes = [VP]
+    L.hora_gb_close.restype = I32
     L.hora_gb_batch_run.argtypes = [I32, VP, VP, P32, VP, VP]
     L.hora_gb_batch_run.restype = I32
     L.hora_gb_server_create.argtypes = [U64, I32, ctypes.POINTER(VP)]

@@ -440,12 +440,55 @@ static int dispatch_group(int dim, const std::vector<const HostNet*>& nets, std:
   return HORA_E_NOT_SUPPORTED;
 }
 
+void OwnedNet::copy(const hora_net_desc* n, const hora_query_desc* qq) {
+  int tot = 0;
+  for (int p = 0; p < n->nprocs; ++p) tot += n->proc_nlocs[p];
+  const int ne = n->nedges;
+  auto cp = [](std::vector<int32_t>& v, const int32_t* s, size_t k) { v.assign(s, s + k); if (v.empty()) v.push_back(0); };
+  cp(chan_flags, n->chan_flags, n->nchans);
+  cp(int_lo, n->int_lo, n->nints); cp(int_hi, n->int_hi, n->nints); cp(int_init, n->int_init, n->nints);
+  cp(proc_nlocs, n->proc_nlocs, n->nprocs); cp(proc_init, n->proc_init, n->nprocs);
+  cp(loc_flags, n->loc_flags, tot); cp(loc_inv_off, n->loc_inv_off, tot + 1);
+  cp(edge_proc, n->edge_proc, ne); cp(edge_src, n->edge_src, ne); cp(edge_tgt, n->edge_tgt, ne);
+  cp(edge_chan, n->edge_chan, ne); cp(edge_dir, n->edge_dir, ne);
+  cp(edge_guard_off, n->edge_guard_off, ne + 1); cp(edge_iguard_off, n->edge_iguard_off, ne + 1);
+  cp(edge_reset_off, n->edge_reset_off, ne + 1); cp(edge_iupd_off, n->edge_iupd_off, ne + 1);
+  const int ncons = std::max(ne ? n->edge_guard_off[ne] : 0, n->loc_inv_off[tot]);
+  cp(cons, n->cons, 3 * (size_t)ncons);
+  cp(iatoms, n->iatoms, ne ? 3 * (size_t)n->edge_iguard_off[ne] : 0);
+  cp(resets, n->resets, ne ? (size_t)n->edge_reset_off[ne] : 0);
+  cp(iupds, n->iupds, ne ? 2 * (size_t)n->edge_iupd_off[ne] : 0);
+  d = *n;
+  d.chan_flags = chan_flags.data(); d.int_lo = int_lo.data(); d.int_hi = int_hi.data(); d.int_init = int_init.data();
+  d.proc_nlocs = proc_nlocs.data(); d.proc_init = proc_init.data(); d.loc_flags = loc_flags.data();
+  d.loc_inv_off = loc_inv_off.data(); d.edge_proc = edge_proc.data(); d.edge_src = edge_src.data();
+  d.edge_tgt = edge_tgt.data(); d.edge_chan = edge_chan.data(); d.edge_dir = edge_dir.data();
+  d.edge_guard_off = edge_guard_off.data(); d.edge_iguard_off = edge_iguard_off.data();
+  d.edge_reset_off = edge_reset_off.data(); d.edge_iupd_off = edge_iupd_off.data(); d.cons = cons.data();
+  d.iatoms = iatoms.data(); d.resets = resets.data(); d.iupds = iupds.data();
+  q = *qq;
+  cp(p_loc, qq->p.loc_req, 2 * (size_t)qq->p.nloc); cp(p_int, qq->p.int_cond, 3 * (size_t)qq->p.nint);
+  cp(p_clk, qq->p.clk_cond, 3 * (size_t)qq->p.nclk);
+  cp(q_loc, qq->q.loc_req, 2 * (size_t)qq->q.nloc); cp(q_int, qq->q.int_cond, 3 * (size_t)qq->q.nint);
+  cp(q_clk, qq->q.clk_cond, 3 * (size_t)qq->q.nclk);
+  q.p.loc_req = p_loc.data(); q.p.int_cond = p_int.data(); q.p.clk_cond = p_clk.data();
+  q.q.loc_req = q_loc.data(); q.q.int_cond = q_int.data(); q.q.clk_cond = q_clk.data();
+}
+
 }  // namespace hgb
 
 // =============================================================================================
 // C ABI
 // =============================================================================================
 using namespace hgb;
+
+// A query handle: the owned request, and the result and E[] witness of its last run.
+struct hora_handle_s {
+  OwnedNet req;
+  bool ran = false;
+  hora_stats st{};
+  Trace trace;
+};
 
 static thread_local std::string g_last_error;
 namespace hgb {
@@ -535,14 +578,9 @@ int32_t hora_gb_exists_invariant(const hora_net_desc* net, const hora_pred_desc*
   return run_single(net, HORA_Q_EG, psi, nullptr, backend, stats, nullptr, result);
 }
 
-int32_t hora_gb_exists_invariant_trace(const hora_net_desc* net, const hora_pred_desc* psi, int32_t backend,
-                                       hora_stats* stats, int32_t* result, int32_t cap, int32_t* nsteps,
-                                       int32_t* ords, int32_t* locs, int32_t* ints, int32_t* zones,
-                                       int32_t* loop_to, int32_t* loop_ord) {
-  if (!psi || !nsteps || !loop_to || !loop_ord || cap < 0) return fail(HORA_E_INVALID, "bad arguments");
-  Trace T;
-  const int32_t rc = run_single(net, HORA_Q_EG, psi, nullptr, backend, stats, nullptr, result, &T);
-  if (rc) return rc;
+// A witness into the caller's buffers (cap steps), *nsteps set also when it does not fit.
+static int32_t copy_trace(const Trace& T, int32_t cap, int32_t* nsteps, int32_t* ords, int32_t* locs,
+                          int32_t* ints, int32_t* zones, int32_t* loop_to, int32_t* loop_ord) {
   *nsteps = T.nsteps;
   *loop_to = T.loop_to;
   *loop_ord = T.loop_ord;
@@ -553,6 +591,73 @@ int32_t hora_gb_exists_invariant_trace(const hora_net_desc* net, const hora_pred
   std::copy(T.locs.begin(), T.locs.end(), locs);
   if (!T.ints.empty()) std::copy(T.ints.begin(), T.ints.end(), ints);
   std::copy(T.zones.begin(), T.zones.end(), zones);
+  return HORA_OK;
+}
+
+int32_t hora_gb_exists_invariant_trace(const hora_net_desc* net, const hora_pred_desc* psi, int32_t backend,
+                                       hora_stats* stats, int32_t* result, int32_t cap, int32_t* nsteps,
+                                       int32_t* ords, int32_t* locs, int32_t* ints, int32_t* zones,
+                                       int32_t* loop_to, int32_t* loop_ord) {
+  if (!psi || !nsteps || !loop_to || !loop_ord || cap < 0) return fail(HORA_E_INVALID, "bad arguments");
+  Trace T;
+  const int32_t rc = run_single(net, HORA_Q_EG, psi, nullptr, backend, stats, nullptr, result, &T);
+  if (rc) return rc;
+  return copy_trace(T, cap, nsteps, ords, locs, ints, zones, loop_to, loop_ord);
+}
+
+// ---- handle form: one (network, query) pair opened once, run on demand ----
+
+// The predicates a query kind reads: p for reach / leads-to / E[], q for leads-to only.
+static const hora_pred_desc* query_p(const hora_query_desc& q) { return q.kind == HORA_Q_DEADLOCK ? nullptr : &q.p; }
+static const hora_pred_desc* query_q(const hora_query_desc& q) { return q.kind == HORA_Q_LEADSTO ? &q.q : nullptr; }
+
+int32_t hora_gb_open(const hora_net_desc* net, const hora_query_desc* q, hora_handle* out) {
+  g_last_error.clear();
+  if (!net || !q || !out) return fail(HORA_E_INVALID, "bad arguments");
+  *out = nullptr;
+  if (q->kind < HORA_Q_REACH || q->kind > HORA_Q_EG) return fail(HORA_E_INVALID, "unknown query kind");
+  HostNet H;
+  std::string err;
+  const int rc = compile_net(net, q->kind, query_p(*q), query_q(*q), H, err);
+  if (rc) return fail(rc, err);
+  hora_handle h = new hora_handle_s;
+  h->req.copy(net, q);
+  *out = h;
+  return HORA_OK;
+}
+
+int32_t hora_gb_run(hora_handle h, int32_t* verdict, hora_stats* stats) {
+  g_last_error.clear();
+  if (!h || !verdict) return fail(HORA_E_INVALID, "bad arguments");
+  const hora_query_desc& q = h->req.q;
+  h->ran = false;
+  h->trace = Trace{};
+  h->st = hora_stats{};
+  int32_t r = -1;
+  const int32_t rc = run_single(&h->req.d, q.kind, query_p(q), query_q(q), HORA_BACKEND_CUDA, &h->st, nullptr, &r,
+                                q.kind == HORA_Q_EG ? &h->trace : nullptr);
+  stats_out(stats, h->st);
+  if (rc) return rc;
+  h->ran = true;
+  *verdict = r;
+  return HORA_OK;
+}
+
+int32_t hora_gb_trace(hora_handle h, int32_t cap, int32_t* nsteps, int32_t* ords, int32_t* locs, int32_t* ints,
+                      int32_t* zones, int32_t* loop_to, int32_t* loop_ord) {
+  g_last_error.clear();
+  if (!h || !nsteps || !loop_to || !loop_ord || cap < 0) return fail(HORA_E_INVALID, "bad arguments");
+  if (h->req.q.kind != HORA_Q_EG)
+    return fail(HORA_E_NOT_SUPPORTED,
+                "traces are kept for E[] queries only: the other routes store convex hulls of zones reached "
+                "along different paths");
+  if (!h->ran) return fail(HORA_E_INVALID, "the handle has not run");
+  return copy_trace(h->trace, cap, nsteps, ords, locs, ints, zones, loop_to, loop_ord);
+}
+
+int32_t hora_gb_close(hora_handle h) {
+  if (!h) return fail(HORA_E_INVALID, "null handle");
+  delete h;
   return HORA_OK;
 }
 

@@ -49,6 +49,18 @@ int upload_nets(const std::vector<const HostNet*>& nets, int inst_shift, DeviceN
 void build_blob(const HostNet& H, std::vector<int32_t>& blob, std::vector<size_t>& offs);
 NetView make_view(const HostNet& H, const int32_t* device_blob, const std::vector<size_t>& offs, int inst_shift);
 
+// Owned copy of a network descriptor and a query: the caller's arrays may be freed afterwards
+// (the serving queue and query handles keep their requests this way).
+struct OwnedNet {
+  std::vector<int32_t> chan_flags, int_lo, int_hi, int_init, proc_nlocs, proc_init, loc_flags, loc_inv_off,
+      edge_proc, edge_src, edge_tgt, edge_chan, edge_dir, edge_guard_off, edge_iguard_off, edge_reset_off,
+      edge_iupd_off, cons, iatoms, resets, iupds;
+  std::vector<int32_t> p_loc, p_int, p_clk, q_loc, q_int, q_clk;
+  hora_net_desc d{};
+  hora_query_desc q{};
+  void copy(const hora_net_desc* n, const hora_query_desc* qq);
+};
+
 // The batched form (hora_gb_batch_run) with an explicit store budget for the whole call, in bytes
 // (0: three quarters of the free device memory).
 int32_t run_batch(int32_t n, const hora_net_desc* nets, const hora_query_desc* queries, int32_t* verdicts,

@@ -23,50 +23,6 @@
 
 namespace hgb {
 
-// Owned copy of a network descriptor and a query.
-struct OwnedNet {
-  std::vector<int32_t> chan_flags, int_lo, int_hi, int_init, proc_nlocs, proc_init, loc_flags, loc_inv_off,
-      edge_proc, edge_src, edge_tgt, edge_chan, edge_dir, edge_guard_off, edge_iguard_off, edge_reset_off,
-      edge_iupd_off, cons, iatoms, resets, iupds;
-  std::vector<int32_t> p_loc, p_int, p_clk, q_loc, q_int, q_clk;
-  hora_net_desc d{};
-  hora_query_desc q{};
-  void copy(const hora_net_desc* n, const hora_query_desc* qq) {
-    int tot = 0;
-    for (int p = 0; p < n->nprocs; ++p) tot += n->proc_nlocs[p];
-    const int ne = n->nedges;
-    auto cp = [](std::vector<int32_t>& v, const int32_t* s, size_t k) { v.assign(s, s + k); if (v.empty()) v.push_back(0); };
-    cp(chan_flags, n->chan_flags, n->nchans);
-    cp(int_lo, n->int_lo, n->nints); cp(int_hi, n->int_hi, n->nints); cp(int_init, n->int_init, n->nints);
-    cp(proc_nlocs, n->proc_nlocs, n->nprocs); cp(proc_init, n->proc_init, n->nprocs);
-    cp(loc_flags, n->loc_flags, tot); cp(loc_inv_off, n->loc_inv_off, tot + 1);
-    cp(edge_proc, n->edge_proc, ne); cp(edge_src, n->edge_src, ne); cp(edge_tgt, n->edge_tgt, ne);
-    cp(edge_chan, n->edge_chan, ne); cp(edge_dir, n->edge_dir, ne);
-    cp(edge_guard_off, n->edge_guard_off, ne + 1); cp(edge_iguard_off, n->edge_iguard_off, ne + 1);
-    cp(edge_reset_off, n->edge_reset_off, ne + 1); cp(edge_iupd_off, n->edge_iupd_off, ne + 1);
-    const int ncons = std::max(ne ? n->edge_guard_off[ne] : 0, n->loc_inv_off[tot]);
-    cp(cons, n->cons, 3 * (size_t)ncons);
-    cp(iatoms, n->iatoms, ne ? 3 * (size_t)n->edge_iguard_off[ne] : 0);
-    cp(resets, n->resets, ne ? (size_t)n->edge_reset_off[ne] : 0);
-    cp(iupds, n->iupds, ne ? 2 * (size_t)n->edge_iupd_off[ne] : 0);
-    d = *n;
-    d.chan_flags = chan_flags.data(); d.int_lo = int_lo.data(); d.int_hi = int_hi.data(); d.int_init = int_init.data();
-    d.proc_nlocs = proc_nlocs.data(); d.proc_init = proc_init.data(); d.loc_flags = loc_flags.data();
-    d.loc_inv_off = loc_inv_off.data(); d.edge_proc = edge_proc.data(); d.edge_src = edge_src.data();
-    d.edge_tgt = edge_tgt.data(); d.edge_chan = edge_chan.data(); d.edge_dir = edge_dir.data();
-    d.edge_guard_off = edge_guard_off.data(); d.edge_iguard_off = edge_iguard_off.data();
-    d.edge_reset_off = edge_reset_off.data(); d.edge_iupd_off = edge_iupd_off.data(); d.cons = cons.data();
-    d.iatoms = iatoms.data(); d.resets = resets.data(); d.iupds = iupds.data();
-    q = *qq;
-    cp(p_loc, qq->p.loc_req, 2 * (size_t)qq->p.nloc); cp(p_int, qq->p.int_cond, 3 * (size_t)qq->p.nint);
-    cp(p_clk, qq->p.clk_cond, 3 * (size_t)qq->p.nclk);
-    cp(q_loc, qq->q.loc_req, 2 * (size_t)qq->q.nloc); cp(q_int, qq->q.int_cond, 3 * (size_t)qq->q.nint);
-    cp(q_clk, qq->q.clk_cond, 3 * (size_t)qq->q.nclk);
-    q.p.loc_req = p_loc.data(); q.p.int_cond = p_int.data(); q.p.clk_cond = p_clk.data();
-    q.q.loc_req = q_loc.data(); q.q.int_cond = q_int.data(); q.q.clk_cond = q_clk.data();
-  }
-};
-
 struct Request {
   int64_t ticket = 0;
   OwnedNet net;

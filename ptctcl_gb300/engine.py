@@ -142,6 +142,66 @@ def exists_invariant_trace(net: Network, psi: Pred, backend: Backend = Backend.C
                   "loop_to": lt.value, "loop_ord": lo.value}
 
 
+class QueryHandle:
+    """One (network, query) pair opened once and run on demand (hora_gb_open / hora_gb_run /
+    hora_gb_trace / hora_gb_close); usable as a context manager. ``kind`` and the predicates follow
+    ``check_network_query`` without ``negate``: run() returns reachable (Q_REACH), deadlock
+    reachable (Q_DEADLOCK), holds (Q_LEADSTO, Q_EG)."""
+
+    def __init__(self, net: Network, kind: int, p: Optional[Pred] = None, q: Optional[Pred] = None):
+        self._lib = capi.load()
+        self.net, self.kind = net, kind
+        na, qa = NetArrays(net), QueryArrays(kind, p or Pred(), q or Pred())
+        h = ctypes.c_void_p()
+        capi.check(self._lib.hora_gb_open(ctypes.addressof(na.desc), ctypes.addressof(qa.desc), ctypes.byref(h)),
+                   "open")
+        self._h = h   # the library copied the descriptors
+
+    def run(self, stats: Optional[ReachStats] = None) -> bool:
+        st = Stats()
+        v = ctypes.c_int32(-1)
+        rc = self._lib.hora_gb_run(self._h, ctypes.byref(v), ctypes.byref(st))
+        if stats is not None:
+            stats.fill(st)
+        capi.check(rc, "run")
+        return bool(v.value)
+
+    def trace(self, cap: int = 1 << 16):
+        """The witness of the last run of an E[] query (as exists_invariant_trace), None when psi fails."""
+        net = self.net
+        np_, ni, d2 = len(net.procs), len(net.ints), net.dim * net.dim
+        n, lt, lo = ctypes.c_int32(0), ctypes.c_int32(0), ctypes.c_int32(0)
+        ords = np.zeros(max(cap, 1), np.int32)
+        locs = np.zeros(max(cap * np_, 1), np.int32)
+        ints = np.zeros(max(cap * ni, 1), np.int32)
+        zones = np.zeros(max(cap * d2, 1), np.int32)
+        rc = self._lib.hora_gb_trace(self._h, cap, ctypes.byref(n), capi.p32(ords), capi.p32(locs), capi.p32(ints),
+                                     capi.p32(zones), ctypes.byref(lt), ctypes.byref(lo))
+        capi.check(rc, "trace")
+        k = n.value
+        if k == 0:
+            return None
+        return {"ords": ords[:k].tolist(), "locs": locs[:k * np_].reshape(k, np_),
+                "ints": ints[:k * ni].reshape(k, ni), "zones": zones[:k * d2].reshape(k, net.dim, net.dim),
+                "loop_to": lt.value, "loop_ord": lo.value}
+
+    def close(self):
+        if self._h:
+            capi.check(self._lib.hora_gb_close(self._h), "close")
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            self._lib.hora_gb_close(self._h)
+            self._h = None
+
+
 def check_network_query(net: Network, kind: int, p: Pred, q: Optional[Pred] = None, negate: bool = False,
                         backend: Backend = Backend.Cuda, stats: Optional[ReachStats] = None) -> bool:
     """Route one lowered query (check_network_query, src/query/dispatch.cpp:109-607).

@@ -68,3 +68,41 @@ def test_no_device_is_an_error_not_a_fallback():
     rc = lib.hora_gb_reachable_net(ctypes.addressof(na.desc), ctypes.addressof(ta.desc), capi.BACKEND_CUDA, None,
                                    ctypes.byref(res))
     assert rc == capi.E_NO_DEVICE
+
+
+def test_handle_open_validates_and_copies_without_a_device():
+    from ptctcl_gb300.model import QueryArrays
+    lib = capi.load()
+    net = load_model("fischer4")
+    na = NetArrays(net)
+    h = ctypes.c_void_p()
+
+    def open_(kind, p, q=None):
+        qa = QueryArrays(kind, p, q)
+        return lib.hora_gb_open(ctypes.addressof(na.desc), ctypes.addressof(qa.desc), ctypes.byref(h))
+
+    assert open_(0, Pred([(0, 3)])) == capi.OK and h.value
+    n, lt, lo = ctypes.c_int32(0), ctypes.c_int32(0), ctypes.c_int32(0)
+    rc = lib.hora_gb_trace(h, 0, ctypes.byref(n), None, None, None, None, ctypes.byref(lt), ctypes.byref(lo))
+    assert rc == capi.E_NOT_SUPPORTED and "E[]" in capi.last_error()
+    assert lib.hora_gb_close(h) == capi.OK
+    assert open_(3, Pred([(0, 3)])) == capi.OK
+    rc = lib.hora_gb_trace(h, 0, ctypes.byref(n), None, None, None, None, ctypes.byref(lt), ctypes.byref(lo))
+    assert rc == capi.E_INVALID   # not run yet
+    assert lib.hora_gb_close(h) == capi.OK
+    assert open_(0, Pred([(0, 99)])) == capi.E_INVALID and not h.value
+    assert open_(7, Pred([(0, 3)])) == capi.E_INVALID
+    diag = NetArrays(Network(2, [Process("P", [Location("A", [(1, 2, (3 << 1) | 1)])], [], 0)]))
+    qa = QueryArrays(1, None, None)
+    assert lib.hora_gb_open(ctypes.addressof(diag.desc), ctypes.addressof(qa.desc), ctypes.byref(h)) == \
+        capi.E_NOT_SUPPORTED
+    assert lib.hora_gb_close(None) == capi.E_INVALID
+
+
+@pytest.mark.skipif(capi.device_count() > 0, reason="needs a machine without a CUDA device")
+def test_handle_run_without_a_device_is_an_error():
+    from ptctcl_gb300.engine import QueryHandle
+    h = QueryHandle(load_model("fischer4"), 1)
+    with pytest.raises(capi.HoraError):
+        h.run()
+    h.close()
