@@ -1,0 +1,32 @@
+"""Whole queries at the bench's full size (config 2, A[] not deadlock, up to 1.45M stored zones and
+20M successors) against the oracle's verdict and counts, recorded by
+tests/golden/make_full_size.py because the single-threaded oracle needs minutes per query; a
+second run must reproduce every count (the merge order is canonical, not scheduling-dependent)."""
+import json
+import os
+
+import pytest
+
+from ptctcl_gb300 import engine
+from ptctcl_gb300.engine import Backend, ReachStats
+from ptctcl_gb300.generator import config_instance
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROWS = json.load(open(os.path.join(HERE, "golden", "full_size_counts.json")))
+KEYS = ("explored", "generated", "stored", "keys", "levels")
+
+
+@pytest.mark.parametrize("row", ROWS, ids=[f"config{r['config']}-seed{r['seed']}" for r in ROWS])
+def test_full_size_deadlock_query_matches_oracle(row):
+    net = config_instance(row["config"], row["seed"])[0]
+    runs = []
+    for _ in range(2):
+        st = ReachStats()
+        got = engine.deadlock_reachable(net, Backend.Cuda, st)
+        assert got == row["deadlock_reachable"]
+        runs.append({k: getattr(st, k) for k in KEYS})
+    for k in KEYS:
+        assert runs[0][k] == row[k], (k, runs[0][k], row[k])
+    assert runs[1] == runs[0]
