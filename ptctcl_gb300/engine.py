@@ -198,7 +198,10 @@ class QueryHandle:
 
     def __del__(self):
         if getattr(self, "_h", None):
-            self._lib.hora_gb_close(self._h)
+            try:
+                self._lib.hora_gb_close(self._h)
+            except Exception:   # interpreter shutdown: the library may already be gone
+                pass
             self._h = None
 
 
