@@ -33,9 +33,8 @@ sys.path.insert(0, ROOT)
 
 WORKLOAD_CONFIG = 2
 WORKLOAD_SEED = int(os.environ.get("HORA_BENCH_SEED", "2483"))
-# The port stops at the first level boundary past this many seconds; the next level can take as
-# long again, so the sample ends within about 10-30 s.
-CPU_SAMPLE_SECONDS = 12.0
+# The port stops within a few hundred items of this limit (it checks its clock inside BFS levels).
+CPU_SAMPLE_SECONDS = 15.0
 METRIC = "zone successors/s"
 UNIT = "successors/s"
 
@@ -104,8 +103,8 @@ def cpu_baseline(net, seconds: float):
     finally:
         pyoracle.set_time_limit(0)
     return {"value": st["generated"] / dt if dt > 0 else 0.0, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": f"{'first ' + str(st['levels']) + ' BFS levels' if st['status'] else 'whole query'} of "
-                      f"the workload, {st['generated']} successors in {dt:.1f} s"}
+            "sample": f"{'BFS levels 1-' + str(st['levels']) + ' (the last in part)' if st['status'] else 'whole query'}"
+                      f" of the workload, {st['generated']} successors in {dt:.1f} s"}
 
 
 def run_reference(args, rank, world):
@@ -153,7 +152,82 @@ def percentile(xs, q):
     return xs[k]
 
 
-def batched_compare(instances: int, budget: float) -> dict:
+def _cpu_batch_worker(wid, nworkers, instances, budget, out, go, t_go):
+    """One process of the CPU sample: once `go` is set, instances wid, wid + n, ... of config 4
+    through the oracle port until t_go + budget (time.time() based; the port checks its clock
+    inside levels too), one (instance, successors, finished, verdict, time) record per instance on
+    `out`."""
+    from oracle import pyoracle
+    from ptctcl_gb300.generator import config_instance
+    pyoracle.lib()
+    out.put("ready")
+    go.wait()
+    deadline = t_go.value + budget
+    for k in range(wid, instances, nworkers):
+        left = deadline - time.time()
+        if left <= 0:
+            break
+        net, kind, p, q = config_instance(4, k)
+        pyoracle.set_time_limit(left)
+        if kind == 0:
+            v, st = pyoracle.reachable_net(net, p)
+        elif kind == 1:
+            v, st = pyoracle.deadlock_reachable(net)
+        else:
+            v, st = pyoracle.leads_to(net, p, q)
+        out.put((k, st["generated"], st["status"] == 0, int(v), time.time()))
+    out.put(None)
+
+
+def cpu_batched_sample(instances: int, budget: float, cores: int = 0) -> dict:
+    """Config 4 on the host cores: the oracle port, one instance per process at a time on every core,
+    for `budget` seconds of wall time. Workers are spawned (the GPU may already be in use) and start
+    together once all have loaded the port. A worker still busy a quarter of the budget after the
+    deadline is stopped and its current instance is not counted."""
+    import multiprocessing as mp
+    import queue
+    from oracle import pyoracle
+    pyoracle.build()   # once, before the workers load it
+    cores = cores or os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    out, go, t_go = ctx.Queue(), ctx.Event(), ctx.Value("d", 0.0)
+    procs = [ctx.Process(target=_cpu_batch_worker, args=(w, cores, instances, budget, out, go, t_go), daemon=True)
+             for w in range(cores)]
+    for pr in procs:
+        pr.start()
+    for _ in range(cores):   # every worker has imported the port before the clock starts
+        out.get(timeout=120)
+    t0 = time.time()
+    t_go.value = t0
+    go.set()
+    deadline = t0 + budget
+    recs, ended = [], 0
+    hard = deadline + 0.25 * budget
+    while ended < cores and time.time() < hard:
+        try:
+            r = out.get(timeout=max(0.01, min(0.5, hard - time.time())))
+        except queue.Empty:
+            continue
+        if r is None:
+            ended += 1
+        else:
+            recs.append(r)
+    dt = time.time() - t0
+    for pr in procs:
+        if pr.is_alive():
+            pr.terminate()
+        pr.join()
+    gen = sum(r[1] for r in recs)
+    verdicts = {r[0]: r[3] for r in recs if r[2]}
+    lat = [r[4] - t0 for r in recs if r[2]]
+    return {"value": gen / dt, "unit": UNIT, "cores": cores, "kind": "port", "seconds": dt,
+            "verdicts": len(verdicts), "p50_time_to_verdict_s": percentile(lat, 50),
+            "p99_time_to_verdict_s": percentile(lat, 99), "stopped_workers": cores - ended,
+            "sample": f"config-4 instance k on worker k mod {cores}, {budget:.0f} s",
+            "_verdicts": verdicts}
+
+
+def batched_compare(instances: int, budget: float, cpu_budget: float = 0.0) -> dict:
     """Config 4: `instances` seeded networks in one batched run vs the same instances one at a time
     (the plain form), each form given the same wall-time budget (some generated instances have
     millions of zones, so neither form finishes them all). Time to verdict counts from the start of
@@ -196,6 +270,14 @@ def batched_compare(instances: int, budget: float) -> dict:
     pdt = time.perf_counter() - t0
     lat = [s["seconds"] for s in b_done]
     both = [k for k in plain_v if bv[k] >= 0]
+    cpu = {}
+    if cpu_budget > 0:
+        c = cpu_batched_sample(instances, cpu_budget)
+        cv = c.pop("_verdicts")
+        cboth = [k for k in cv if bv[k] >= 0]
+        c["verdicts_compared"] = len(cboth)
+        c["verdicts_agree"] = all(cv[k] == bv[k] for k in cboth)
+        cpu = {"cpu_port_all_cores": c}
     return {"workload": f"config4: {instances} seeded networks (clocks U[2,16], automata "
             f"U[2,10], locations U[4,12], c in [0,40], query mix 60/30/10), {budget:.0f} s budget per form",
             "batched": {"value": b_gen / bdt, "unit": UNIT, "seconds": bdt, "verdicts": len(b_done),
@@ -204,11 +286,12 @@ def batched_compare(instances: int, budget: float) -> dict:
                                     "p50_time_to_verdict_s": percentile(plain_lat, 50),
                                     "p99_time_to_verdict_s": percentile(plain_lat, 99)},
             "speedup_successors_per_s": (b_gen / bdt) / max(1e-9, plain_gen / pdt),
-            "verdicts_compared": len(both), "verdicts_agree": all(plain_v[k] == bv[k] for k in both)}
+            "verdicts_compared": len(both), "verdicts_agree": all(plain_v[k] == bv[k] for k in both), **cpu}
 
 
 def run_batched(args):
-    line = {"metric": METRIC, **batched_compare(args.instances, args.budget)}
+    line = {"metric": METRIC, **batched_compare(args.instances, args.budget,
+                                                0.0 if args.no_cpu_baseline else args.budget)}
     print(json.dumps(line), flush=True)
 
 
@@ -392,7 +475,8 @@ def main():
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(net, CPU_SAMPLE_SECONDS)
     if args.batched_budget > 0 and world == 1:
-        line["batched"] = batched_compare(args.instances, args.batched_budget)
+        line["batched"] = batched_compare(args.instances, args.batched_budget,
+                                          0.0 if args.no_cpu_baseline else args.batched_budget)
     print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()

@@ -1116,6 +1116,13 @@ static double now_s(void) {
   return ts.tv_sec + ts.tv_nsec * 1e-9;
 }
 
+/* True once a set time limit has passed since t0. Checked between BFS levels and every 256 items
+ * of the loops inside one, so a sample ends close to its limit; a run stopped this way reports
+ * HORA_E_TIMEOUT and the successors generated so far, and its verdict is not used. */
+static int over_time(double t0, int i) {
+  return g_time_limit > 0 && (i & 255) == 255 && now_s() - t0 > g_time_limit;
+}
+
 /* The engine shared by E<> and deadlock. `collapse` selects the a_M bounds of deadlock_reachable
  * (engine.cpp:2363-2405, the HORA_DL_MODE=m route). */
 static int32_t run_reach(const hora_net_desc* net, const Goal* goal, int collapse, hora_stats* st,
@@ -1183,15 +1190,19 @@ static int32_t run_reach(const hora_net_desc* net, const Goal* goal, int collaps
     B.n = 0;
     /* expand in frontier order; successor b's insertion order is its buffer position */
     for (int f = 0; f < nfr; ++f) {
+      if (over_time(t0, f)) { S0.generated += B.n; S0.levels = level; S0.status = HORA_E_TIMEOUT; goto done; }
       key_decode(&m, fr[f].key, locs, ints);
       successors(&m, locs, ints, S.zones + (size_t)fr[f].node * d2, m.L, m.U, qmask, emode, sb_emit, &B);
     }
     S0.generated += B.n;
-    for (int b = 0; b < B.n && !found; ++b)
+    for (int b = 0; b < B.n && !found; ++b) {
+      if (over_time(t0, b)) { S0.levels = level; S0.status = HORA_E_TIMEOUT; goto done; }
       if (goal_hit(&m, goal, B.locs + (size_t)b * np, B.ints + (size_t)b * ni, B.zones + (size_t)b * d2)) found = 1;
+    }
     if (found) { S0.levels = level; goto done; }
     /* insert in order */
     for (int b = 0; b < B.n; ++b) {
+      if (over_time(t0, b)) { S0.levels = level; S0.status = HORA_E_TIMEOUT; goto done; }
       const int32_t* sl = B.locs + (size_t)b * np;
       const uint64_t k = key_encode(&m, sl, B.ints + (size_t)b * ni);
       for (int c = 1; c < dim; ++c) {
@@ -1420,11 +1431,13 @@ static int32_t liveness_core(const hora_net_desc* net, const hora_pred_desc* p, 
     ++level;
     B.n = 0;
     for (int f = 0; f < nfr; ++f) {
+      if (over_time(t0, f)) { timed_out = 1; break; }
       key_decode(&m, fr[f].key, locs, ints);
       successors(&m, locs, ints, R.zones + (size_t)fr[f].node * d2, m.L, m.U, qmask, emode, sb_emit, &B);
     }
     S0.generated += B.n;
-    for (int b = 0; b < B.n; ++b) {
+    for (int b = 0; b < B.n && !timed_out; ++b) {
+      if (over_time(t0, b)) { timed_out = 1; break; }
       const int32_t* sl = B.locs + (size_t)b * np;
       const uint64_t k = key_encode(&m, sl, B.ints + (size_t)b * ni);
       for (int c = 1; c < dim; ++c) {
@@ -1436,6 +1449,7 @@ static int32_t liveness_core(const hora_net_desc* net, const hora_pred_desc* p, 
       int id = store_add(&R, k, B.zones + (size_t)b * d2, level, dim, Ls, Us, NULL);
       if (id >= 0) R.stouch[slot_of(&R, k)] = level;
     }
+    if (timed_out) break;
     nfr = collect_frontier(&R, level, &fr, &capfr);
     if (emode == 0 && R.nkeys && (double)R.nlive >= 4.0 * (double)R.nkeys) emode = 1;
   }
@@ -1493,6 +1507,7 @@ static int32_t liveness_core(const hora_net_desc* net, const hora_pred_desc* p, 
     ++level;
     FItem* nxt = NULL; int nn = 0, capn = 0;
     for (int f = 0; f < nfr; ++f) {
+      if (over_time(t0, f)) { timed_out = 1; break; }
       key_decode(&m, fr[f].key, locs, ints);
       B.n = 0;
       successors(&m, locs, ints, G.zones + (size_t)fr[f].node * d2, m.L, m.U, qmask, 1, sb_emit, &B);
@@ -1523,6 +1538,7 @@ static int32_t liveness_core(const hora_net_desc* net, const hora_pred_desc* p, 
   char* inW = (char*)malloc(G.nn ? G.nn : 1);
   const hora_pred_desc* av = m.avoid;
   for (int u = 0; u < nkcap; ++u) {
+    if (over_time(t0, u)) { timed_out = 1; break; }
     key_decode(&m, nkey[u], locs, ints);
     const int32_t* zu = G.zones + (size_t)u * d2;
     m.avoid = NULL;   /* deadlock and any-successor are judged in the unrestricted network */

@@ -22,5 +22,20 @@ def test_reference_arm_prints_one_contract_line():
     assert d["config"]["workload"].startswith("config2")
     cb = d["cpu_baseline"]
     assert cb["kind"] == "port" and cb["cores"] == 1 and cb["value"] == d["value"]
-    assert "BFS levels" in cb["sample"] or "whole query" in cb["sample"]
+    assert "BFS levels 1-" in cb["sample"] or "whole query" in cb["sample"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+
+
+def test_cpu_batched_sample_is_bounded_and_counts_verdicts():
+    """The all-core CPU sample of the batched workload (the oracle port on spawned workers) ends
+    close to its budget and reports the instances it finished."""
+    import time
+    sys.path.insert(0, ROOT)
+    import bench
+    t = time.time()
+    r = bench.cpu_batched_sample(64, 3.0, cores=2)
+    assert time.time() - t < 3.0 * 1.25 + 60   # worker start-up (imports) is outside the budget
+    assert r["cores"] == 2 and r["kind"] == "port" and r["unit"] == "successors/s"
+    assert 3.0 <= r["seconds"] <= 3.0 * 1.25 + 1
+    assert r["value"] > 0 and r["verdicts"] == len(r["_verdicts"]) >= 1
+    assert all(v in (0, 1) for v in r["_verdicts"].values())
