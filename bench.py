@@ -196,8 +196,16 @@ def cpu_batched_sample(instances: int, budget: float, cores: int = 0) -> dict:
     try:
         for pr in procs:
             pr.start()
-        for _ in range(cores):   # every worker has imported the port before the clock starts
-            out.get(timeout=120)
+        ready, t_start = 0, time.time()
+        while ready < cores:   # every worker has imported the port before the clock starts
+            try:
+                if out.get(timeout=1.0) == "ready":
+                    ready += 1
+            except queue.Empty:
+                if any(pr.exitcode is not None for pr in procs):
+                    raise RuntimeError("a CPU worker exited before starting")
+                if time.time() - t_start > 120:
+                    raise RuntimeError("CPU workers did not start within 120 s")
         t0 = time.time()
         t_go.value = t0
         go.set()
