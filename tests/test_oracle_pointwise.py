@@ -9,6 +9,7 @@ import pytest
 from oracle.pyoracle import Dbm
 
 INF = 1 << 30
+NEG_INF = -(1 << 29)   # the a_LU "-inf" bound
 
 
 def raw(v, weak):
@@ -100,3 +101,38 @@ def test_try_union_is_exactly_convexity(nclk):
             refused += 1
             assert np.array_equal(u.d, a.d)   # a failed union leaves a unchanged
     assert merged > 20 and refused > 20
+
+
+@pytest.mark.parametrize("nclk", [1, 2, 3])
+def test_delay_reset_extrapolate_and_simulation_laws(nclk):
+    """delay and Extra_LU+ only add points; reset puts the clock at 0; a_LU simulation is reflexive,
+    implied by inclusion, and transitive along chains of inclusions."""
+    rng = np.random.default_rng(47 + nclk)
+    P = grid(nclk, hi=12.0, step=0.25)
+    zones = [z for z in (random_zone(rng, nclk) for _ in range(300)) if z is not None]
+    for z in zones[:120]:
+        mz = member(z.d, P)
+        up = z.copy().delay()
+        assert up.includes(z) and np.all(member(up.d, P) | ~mz)
+        assert np.array_equal(up.copy().delay().d, up.d)
+        k = int(rng.integers(1, nclk + 1))
+        r = z.copy().reset(k)
+        mr = member(r.d, P)
+        assert mr.any() and np.all(P[mr, k] == 0)
+        bounds = np.array([NEG_INF, 0, 1, 2, 3, 4, 5], np.int64)   # NEG_INF: the clock has no bound
+        L = np.concatenate([[0], rng.choice(bounds, nclk)]).astype(np.int32)
+        U = np.concatenate([[0], rng.choice(bounds, nclk)]).astype(np.int32)
+        e = z.copy().extrapolate_lu_plus(L, U)
+        assert e.includes(z)
+        assert z.alu_le(z, L, U)
+    for a, b in zip(zones[:200:2], zones[1:200:2]):
+        L = np.concatenate([[0], rng.integers(0, 8, nclk)]).astype(np.int32)
+        U = np.concatenate([[0], rng.integers(0, 8, nclk)]).astype(np.int32)
+        if b.includes(a):
+            assert a.alu_le(b, L, U)
+        # a chain a' ⊆ a and a ≼ b gives a' ≼ b
+        if a.alu_le(b, L, U):
+            sub = a.copy()
+            i, j = (int(x) for x in rng.choice(nclk + 1, 2, replace=False))
+            if sub.constrain(i, j, raw(int(rng.integers(-3, 4)), True)):
+                assert sub.alu_le(b, L, U)
