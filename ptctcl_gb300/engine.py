@@ -101,6 +101,13 @@ def leads_to_clocks(net: Network, p: Pred, q: Pred, backend: Backend = Backend.C
     return bool(res.value)
 
 
+def leads_to_otf(net: Network, p: Pred, q: Pred, backend: Backend = Backend.Cuda,
+                 stats: Optional[ReachStats] = None) -> bool:
+    """p --> q (leads_to_otf, include/hora/liveness.hpp:123-124): the same query and route as
+    leads_to_clocks -- the reference's two entry points differ only in how they build their graph."""
+    return leads_to_clocks(net, p, q, backend, stats)
+
+
 def exists_invariant_run(net: Network, psi: Pred, backend: Backend = Backend.Cuda,
                          stats: Optional[ReachStats] = None) -> bool:
     """E[] psi (exists_invariant_run, include/hora/liveness.hpp:35-46): psi a conjunction of
