@@ -1,7 +1,8 @@
 """Whole queries at the bench's full size (config 2, A[] not deadlock, up to 1.45M stored zones and
 20M successors) against the oracle's verdict and counts, recorded by
 tests/golden/make_full_size.py because the single-threaded oracle needs minutes per query; a
-second run must reproduce every count (the merge order is canonical, not scheduling-dependent)."""
+second run must reproduce every count (the merge order is canonical, not scheduling-dependent).
+Kept in a file collected near the end so that a failure here comes after the other parity tests."""
 import json
 import os
 
