@@ -2,7 +2,7 @@
 20M successors) against the oracle's verdict and counts, recorded by
 tests/golden/make_full_size.py because the single-threaded oracle needs minutes per query; a
 second run must reproduce every count (the merge order is canonical, not scheduling-dependent).
-Kept in a file collected near the end so that a failure here comes after the other parity tests."""
+Kept in the file collected last so that a failure here comes after every other test has run."""
 import json
 import os
 
