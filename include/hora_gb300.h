@@ -236,7 +236,9 @@ HORA_GB_API int32_t hora_gb_has_deadlock(const hora_net_desc* net, int32_t n, co
  * fetched on the first call on each device, which should therefore come before any stream capture.
  * The array is shared by all calls and keeps the last call's contents (its counters are cleared on
  * every call): calls that overlap on the GPU race. Runs on the legacy default stream and returns
- * after the kernel has finished. */
+ * after the kernel has finished. The legacy default stream is not ordered against streams created
+ * with cudaStreamNonBlocking (PyTorch's side streams are): a caller that fills d_locs, d_ints or
+ * d_zones on such a stream must synchronise it (cudaStreamSynchronize) before the call. */
 HORA_GB_API int32_t hora_gb_has_deadlock_noalloc(const hora_net_desc* net, int32_t n, const int32_t* d_locs,
                                                  const int32_t* d_ints, const int32_t* d_zones, int32_t* d_out);
 

@@ -70,6 +70,7 @@ extern "C" HORA_GB_API int32_t hora_gb_has_deadlock_noalloc(const hora_net_desc*
                                                             const int32_t* d_locs, const int32_t* d_ints,
                                                             const int32_t* d_zones, int32_t* d_out) {
   std::string err;
+  set_last_error("");
   if (n < 0 || (n > 0 && (!d_locs || !d_zones || !d_out))) { set_last_error("bad arguments"); return HORA_E_INVALID; }
   HostNet H;
   int rc = compile_net(net, HORA_Q_DEADLOCK, nullptr, nullptr, H, err);

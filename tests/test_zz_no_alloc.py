@@ -14,6 +14,7 @@ import pytest
 
 from ptctcl_gb300 import capi, engine
 from ptctcl_gb300.generator import config_instance
+from oracle import pyoracle
 from ptctcl_gb300.model import NetArrays, Network, Process, Location, Edge, c_le, c_ge
 from states import sample_states
 
@@ -34,6 +35,7 @@ def test_noalloc_matches_allocating_entry_point(cfg, seed):
     locs, ints, zones, _, _ = smp
     n = locs.shape[0]
     want = engine.has_deadlock(net, locs, ints, zones)        # the allocating entry point
+    np.testing.assert_array_equal(want, pyoracle.has_deadlock(net, locs, ints, zones))   # and the oracle
     na = NetArrays(net)
     d_locs, d_zones = _dev(torch, locs), _dev(torch, zones)
     d_ints = _dev(torch, ints) if len(net.ints) else None
@@ -45,6 +47,7 @@ def test_noalloc_matches_allocating_entry_point(cfg, seed):
                                               d_ints.data_ptr() if d_ints is not None else None,
                                               d_zones.data_ptr(), d_out.data_ptr())
         assert rc == capi.OK, capi.last_error()
+        assert capi.last_error() == ""                       # a successful call leaves no message
         got = d_out.cpu().numpy()
         np.testing.assert_array_equal(got.astype(bool), want)
         assert set(np.unique(got)) <= {0, 1}
