@@ -605,8 +605,11 @@ static int build_broadcast_parts(const Model* m, const int32_t* locs, const int3
 
 /* Successor generation (successors_net, src/reachability/engine.cpp:243-368; the same emission
  * order as tagged_successors, src/liveness/operators.cpp:55-206). Calls emit() per non-empty
- * successor in order. */
-typedef void (*emit_fn)(void* ctx, const int32_t* locs, const int32_t* ints, const int32_t* zone);
+ * successor in order. `raw` numbers the transition among every candidate the enumeration visits
+ * (the combinations that pass the integer guards and the committed filter, whether or not their
+ * zone turns out empty), so find_trans() can rebuild its recipe -- the tag of tagged_successors --
+ * from the source's discrete state alone. */
+typedef void (*emit_fn)(void* ctx, const int32_t* locs, const int32_t* ints, const int32_t* zone, int raw);
 static int successors(const Model* m, const int32_t* locs, const int32_t* ints, const int32_t* zone,
                       const int32_t* L, const int32_t* U, const uint8_t* qmask, int emode,
                       emit_fn emit, void* ctx) {
@@ -614,7 +617,7 @@ static int successors(const Model* m, const int32_t* locs, const int32_t* ints, 
   const int dim = m->dim, d2 = dim * dim, np = n->nprocs, ni = n->nints;
   int32_t z1[64 * 64];
   int32_t tl[64], ti[64];
-  int src_c, src_u;
+  int src_c, src_u, raw = 0;
   frozen_flags(m, locs, ints, &src_c, &src_u);
   /* local edges */
   for (int p = 0; p < np; ++p) {
@@ -624,6 +627,7 @@ static int successors(const Model* m, const int32_t* locs, const int32_t* ints, 
       const int e = m->eloc[k];
       if (n->edge_chan[e] >= 0) continue;
       if (!int_ok(n, e, ints)) continue;
+      const int rw = raw++;
       memcpy(z1, zone, sizeof(int32_t) * d2);
       if (!apply_cons(z1, dim, n->cons, n->edge_guard_off[e], n->edge_guard_off[e + 1])) continue;
       for (int r = n->edge_reset_off[e]; r < n->edge_reset_off[e + 1]; ++r) orc_dbm_reset(z1, dim, n->resets[r]);
@@ -632,7 +636,7 @@ static int successors(const Model* m, const int32_t* locs, const int32_t* ints, 
       for (int u = n->edge_iupd_off[e]; u < n->edge_iupd_off[e + 1]; ++u) ti[n->iupds[2 * u]] = n->iupds[2 * u + 1];
       if (!close_succ_zone(m, tl, ti, z1, qmask, L, U, emode)) continue;
       if (orc_dbm_empty(z1, dim)) continue;
-      emit(ctx, tl, ti, z1);
+      emit(ctx, tl, ti, z1, rw);
     }
   }
   /* binary synchronisation */
@@ -652,6 +656,7 @@ static int successors(const Model* m, const int32_t* locs, const int32_t* ints, 
           if (n->edge_chan[re] != n->edge_chan[se] || n->edge_dir[re] != -1) continue;
           if (src_c && !(i_comm || loc_committed(m, j, locs[j]))) continue;
           if (!int_ok(n, re, ints)) continue;
+          const int rw = raw++;
           memcpy(z1, zone, sizeof(int32_t) * d2);
           if (!apply_cons(z1, dim, n->cons, n->edge_guard_off[se], n->edge_guard_off[se + 1])) continue;
           if (!apply_cons(z1, dim, n->cons, n->edge_guard_off[re], n->edge_guard_off[re + 1])) continue;
@@ -663,7 +668,7 @@ static int successors(const Model* m, const int32_t* locs, const int32_t* ints, 
           for (int u = n->edge_iupd_off[re]; u < n->edge_iupd_off[re + 1]; ++u) ti[n->iupds[2 * u]] = n->iupds[2 * u + 1];
           if (!close_succ_zone(m, tl, ti, z1, qmask, L, U, emode)) continue;
           if (orc_dbm_empty(z1, dim)) continue;
-          emit(ctx, tl, ti, z1);
+          emit(ctx, tl, ti, z1, rw);
         }
       }
     }
@@ -687,6 +692,7 @@ static int successors(const Model* m, const int32_t* locs, const int32_t* ints, 
           if (pt->edge[pick[t]] >= 0 && loc_committed(m, pt->proc, locs[pt->proc])) part_comm = 1;
         }
         if (!src_c || part_comm) {
+          const int rw = raw++;
           memcpy(z1, zone, sizeof(int32_t) * d2);
           int ok = apply_cons(z1, dim, n->cons, n->edge_guard_off[se], n->edge_guard_off[se + 1]);
           for (int t = 0; ok && t < P->nparts; ++t) {
@@ -712,7 +718,7 @@ static int successors(const Model* m, const int32_t* locs, const int32_t* ints, 
               for (int r = n->edge_reset_off[re]; r < n->edge_reset_off[re + 1]; ++r) orc_dbm_reset(z1, dim, n->resets[r]);
             }
             if (close_succ_zone(m, tl, ti, z1, qmask, L, U, emode) && !orc_dbm_empty(z1, dim))
-              emit(ctx, tl, ti, z1);
+              emit(ctx, tl, ti, z1, rw);
           }
         }
         if (P->nparts == 0) break;
@@ -763,21 +769,26 @@ static uint64_t reset_mask(const hora_net_desc* n, int e) {
   for (int q = n->edge_reset_off[e]; q < n->edge_reset_off[e + 1]; ++q) r |= 1ull << n->resets[q];
   return r;
 }
-static int state_has_deadlock(const Model* m, const int32_t* locs, const int32_t* ints, const int32_t* zone) {
+/* The escape regions of a state: every transition's guard region of the delay-closed zone `Z`
+ * (filled here), pulled back through the target invariant, then let down unless the state is
+ * frozen. Returns 0 when the state has no concrete valuation (empty zone, or invariant
+ * unsatisfiable); Eout->covered is set when one escape is all of Z. */
+static int deadlock_escapes(const Model* m, const int32_t* locs, const int32_t* ints, const int32_t* zone,
+                            Escapes* Eout, int32_t* Z, int* frozen_out) {
   const hora_net_desc* n = m->n;
-  const int dim = m->dim, d2 = dim * dim, np = n->nprocs, ni = n->nints;
+  const int dim = m->dim, d2 = dim * dim, np = n->nprocs;
   if (orc_dbm_empty(zone, dim)) return 0;
   int src_c, src_u;
   frozen_flags(m, locs, ints, &src_c, &src_u);
   const int frozen = src_c || src_u;
-  int32_t Z[64 * 64], g[64 * 64];
+  *frozen_out = frozen;
+  int32_t g[64 * 64];
   int32_t tl[64];
   memcpy(Z, zone, sizeof(int32_t) * d2);
   if (!frozen) orc_dbm_delay(Z, dim);
   if (!apply_inv(m, Z, locs)) return 0;
   Escapes E = {0};
   E.dim = dim; E.Z = Z;
-  (void)ni;
   for (int p = 0; p < np && !E.covered; ++p) {
     if (src_c && !loc_committed(m, p, locs[p])) continue;
     const int gp = m->loc_base[p] + locs[p];
@@ -856,10 +867,19 @@ static int state_has_deadlock(const Model* m, const int32_t* locs, const int32_t
       }
     }
   }
+  if (!E.covered && !frozen) for (int w = 0; w < E.nw; ++w) orc_dbm_down(E.w + (size_t)w * d2, dim);
+  *Eout = E;
+  return 1;
+}
+static int state_has_deadlock(const Model* m, const int32_t* locs, const int32_t* ints, const int32_t* zone) {
+  const int dim = m->dim, d2 = dim * dim;
+  int32_t Z[64 * 64];
+  Escapes E = {0};
+  int frozen = 0;
+  if (!deadlock_escapes(m, locs, ints, zone, &E, Z, &frozen)) { free(E.w); return 0; }
   int dead;
   if (E.covered) dead = 0;
   else {
-    if (!frozen) for (int w = 0; w < E.nw; ++w) orc_dbm_down(E.w + (size_t)w * d2, dim);
     dead = -1;
     for (int w = 0; w < E.nw; ++w)
       if (orc_dbm_includes(E.w + (size_t)w * d2, Z, dim)) { dead = 0; break; }
@@ -878,7 +898,8 @@ typedef struct {
   int np, ni, d2;
   int32_t *out_src, *out_ord, *out_locs, *out_ints, *out_zones;
 } ExpCtx;
-static void exp_emit(void* c, const int32_t* locs, const int32_t* ints, const int32_t* zone) {
+static void exp_emit(void* c, const int32_t* locs, const int32_t* ints, const int32_t* zone, int raw) {
+  (void)raw;
   ExpCtx* x = (ExpCtx*)c;
   if (x->n < x->cap) {
     const int64_t k = x->n;
@@ -1077,19 +1098,25 @@ static int collect_frontier(const Store* S, int level, FItem** frp, int* capp) {
 
 typedef struct {
   int32_t* locs; int32_t* ints; int32_t* zones;
+  int* raw; int* parent;         /* transition index and emitting node (phase-2 graph) */
   int n, cap, np, ni, d2;
+  int cur_parent;
 } SuccBuf;
-static void sb_emit(void* c, const int32_t* locs, const int32_t* ints, const int32_t* zone) {
+static void sb_emit(void* c, const int32_t* locs, const int32_t* ints, const int32_t* zone, int raw) {
   SuccBuf* b = (SuccBuf*)c;
   if (b->n == b->cap) {
     b->cap = b->cap ? b->cap * 2 : 1024;
     b->locs = (int32_t*)realloc(b->locs, sizeof(int32_t) * b->np * (size_t)b->cap);
     b->ints = (int32_t*)realloc(b->ints, sizeof(int32_t) * (b->ni ? b->ni : 1) * (size_t)b->cap);
     b->zones = (int32_t*)realloc(b->zones, sizeof(int32_t) * b->d2 * (size_t)b->cap);
+    b->raw = (int*)realloc(b->raw, sizeof(int) * (size_t)b->cap);
+    b->parent = (int*)realloc(b->parent, sizeof(int) * (size_t)b->cap);
   }
   memcpy(b->locs + (size_t)b->n * b->np, locs, sizeof(int32_t) * b->np);
   if (b->ni) memcpy(b->ints + (size_t)b->n * b->ni, ints, sizeof(int32_t) * b->ni);
   memcpy(b->zones + (size_t)b->n * b->d2, zone, sizeof(int32_t) * b->d2);
+  b->raw[b->n] = raw;
+  b->parent[b->n] = b->cur_parent;
   b->n++;
 }
 
@@ -1236,7 +1263,7 @@ done:
   S0.seconds = now_s() - t0;
   S0.probes += 0;
   if (st) *st = S0;
-  free(fr); free(B.locs); free(B.ints); free(B.zones);
+  free(fr); free(B.locs); free(B.ints); free(B.zones); free(B.raw); free(B.parent);
   store_free(&S);
   model_free(&m);
   return HORA_OK;
@@ -1275,13 +1302,13 @@ int32_t orc_initial_state(const hora_net_desc* net, const uint8_t* qmask, int32_
  *
  *  1. the reachable states, explored with the deadlock-sound a_M bisimulation bounds (every query
  *     constant folded in), give the roots: their p-part, cut to !q;
- *  2. from the roots, the exact zone graph of the network restricted to !q (q's clock atom is a
- *     single constraint, so its complement is convex and is adjoined to the invariant exactly
- *     where q's discrete part holds) is built with Extra_M+ for finiteness and exact-zone
- *     deduplication, so the graph is post-stable: every valuation of a node has a predecessor in
- *     each of its source nodes;
- *  3. on that graph, node-level emptiness of W is exact: W starts as every node and repeatedly
- *     loses the nodes with no stop valuation and no successor left in W.
+ *  2. from the roots, the zone graph of the network restricted to !q (q's clock atom is a single
+ *     constraint, so its complement is convex and is adjoined to the invariant exactly where q's
+ *     discrete part holds) is built with Extra_M+ for finiteness and inclusion covers, and W is
+ *     swept on federations with the exact predecessor (leadsto_subsumed below).
+ * E[] psi keeps the exact-zone variant of step 2: exact-zone deduplication makes the graph
+ * post-stable (every valuation of a node has a predecessor in each of its source nodes), so
+ * node-level emptiness of W is exact there, and a witness is a path of nodes.
  * ============================================================================================ */
 /* A location requirement (p, l) with l >= 0 asks for location l; l < 0 for any location but -l-1. */
 static int disc_match(const hora_pred_desc* t, const int32_t* locs, const int32_t* ints) {
@@ -1367,11 +1394,13 @@ static void iv_push(IVec* v, int x) {
 }
 
 typedef struct { IVec* succ_keys_unused; int count; } CountCtx;
-static void count_emit(void* c, const int32_t* l, const int32_t* i, const int32_t* z) {
-  (void)l; (void)i; (void)z;
+static void count_emit(void* c, const int32_t* l, const int32_t* i, const int32_t* z, int raw) {
+  (void)l; (void)i; (void)z; (void)raw;
   ((CountCtx*)c)->count++;
 }
 
+static int32_t leadsto_subsumed(Model* m, Store* R, const hora_pred_desc* p, const hora_pred_desc* q,
+                                const uint8_t* qmask, hora_stats* S0, double t0, int* violated_out);
 /* p --> q (psi NULL), or E[] psi (p, q NULL): the two share the restricted exact zone graph, its
  * stop sets and the greatest fixpoint. E[] psi roots the graph at the initial state of the
  * psi-restricted network instead of at the p-states of a reachability pass. */
@@ -1458,6 +1487,19 @@ static int32_t liveness_core(const hora_net_desc* net, const hora_pred_desc* p, 
   m.avoid_psi = psi != NULL;
   if (!psi && q->nclk == 1) {
     m.avoid_neg[0] = q->clk_cond[1]; m.avoid_neg[1] = q->clk_cond[0]; m.avoid_neg[2] = r_negate(q->clk_cond[2]);
+  }
+  if (!psi) {   /* p --> q: the subsumed graph and the federation sweep */
+    int viol = 0;
+    if (timed_out) S0.status = HORA_E_TIMEOUT;
+    else leadsto_subsumed(&m, &R, p, q, qmask, &S0, t0, &viol);
+    store_free(&R);
+    S0.expanded = S0.explored;
+    S0.seconds = now_s() - t0;
+    if (st) *st = S0;
+    *result = !viol;
+    free(fr); free(B.locs); free(B.ints); free(B.zones); free(B.raw); free(B.parent);
+    model_free(&m);
+    return HORA_OK;
   }
   Store G;
   store_init(&G, d2);
@@ -1587,9 +1629,501 @@ static int32_t liveness_core(const hora_net_desc* net, const hora_pred_desc* p, 
   *result = psi ? violated : !violated;   /* E[] psi holds iff its root keeps a maximal psi-run */
   free(off); free(dst); free(stop); free(inW); free(nkey);
   free(roots.a); free(efrom.a); free(eto.a); free(fr);
-  free(B.locs); free(B.ints); free(B.zones);
+  free(B.locs); free(B.ints); free(B.zones); free(B.raw); free(B.parent);
   store_free(&G);
   model_free(&m);
+  return HORA_OK;
+}
+
+/* ============================================================================================
+ * Leads-to on the subsumed graph: inclusion covers and a federation-valued backward sweep
+ * (online_intern / online_covers, src/liveness/construction.cpp:194-215,480-684;
+ *  solve_greatest_fixpoint / relax, src/liveness/fixpoint.cpp:48-977,750-864;
+ *  exact_predecessor, src/liveness/operators.cpp:257-306; stop_set, construction.cpp:1200-1239)
+ *
+ * Phase 2 of p --> q. From the roots (phase 1's p-zones cut to p's clock atoms and to !q), the
+ * !q-restricted network is explored level by level with Extra_M+, and a successor is covered by a
+ * stored zone of its discrete key only when that zone CONTAINS it. A level stores, per key, the
+ * successors not contained in an earlier-level zone that are maximal among the level's own (a
+ * successor strictly inside another, or equal to an earlier one, is covered by the first stored one
+ * containing it). The stored set of a level is therefore a function of the set of successor zones
+ * alone, independent of processing order. Every edge points at a zone containing the exact
+ * successor, so the backward operator
+ *     W[v] := W[v] /\ (Stop(v) \/ U_e Pre_e(W[tgt e]))
+ * computed on federations with the exact predecessor is exact at the level of valuations: W[v] is
+ * the set of valuations of Z_v that start a maximal !q-run. p --> q is violated iff a root keeps a
+ * non-empty W. Early witness (leadsto_witness, construction.cpp:786-826): a root whose stop set is
+ * non-empty already starts such a run, and the graph is not built.
+ * ============================================================================================ */
+typedef struct { int32_t* z; int n, cap, d2; } Fed;
+static void fed_init(Fed* f, int d2) { f->z = NULL; f->n = f->cap = 0; f->d2 = d2; }
+static void fed_free(Fed* f) { free(f->z); f->z = NULL; f->n = f->cap = 0; }
+static void fed_push(Fed* f, const int32_t* z) {
+  if (f->n == f->cap) {
+    f->cap = f->cap ? f->cap * 2 : 4;
+    f->z = (int32_t*)realloc(f->z, sizeof(int32_t) * f->d2 * (size_t)f->cap);
+  }
+  memcpy(f->z + (size_t)f->n * f->d2, z, sizeof(int32_t) * f->d2);
+  f->n++;
+}
+static void fed_remove(Fed* f, int i) {   /* order is not kept */
+  if (i != f->n - 1) memcpy(f->z + (size_t)i * f->d2, f->z + (size_t)(f->n - 1) * f->d2, sizeof(int32_t) * f->d2);
+  f->n--;
+}
+/* out := a /\ b; 0 when empty */
+static int dbm_intersect(int32_t* out, const int32_t* a, const int32_t* b, int dim) {
+  const int d2 = dim * dim;
+  for (int k = 0; k < d2; ++k) out[k] = a[k] < b[k] ? a[k] : b[k];
+  orc_dbm_close(out, dim);
+  return !orc_dbm_empty(out, dim);
+}
+/* Add z (non-empty) to f: dropped if a member contains it; members it contains are dropped; exact
+ * convex unions with members are taken (fed_compact, src/liveness/operators.cpp:428). */
+static void fed_add_compact(Fed* f, int32_t* z, int dim) {
+  const int d2 = dim * dim;
+  for (int i = 0; i < f->n; ++i) if (orc_dbm_includes(f->z + (size_t)i * d2, z, dim)) return;
+  for (int merged = 1; merged;) {
+    merged = 0;
+    for (int i = 0; i < f->n;) {
+      if (orc_dbm_includes(z, f->z + (size_t)i * d2, dim)) { fed_remove(f, i); continue; }
+      ++i;
+    }
+    for (int i = 0; i < f->n; ++i)
+      if (orc_dbm_try_union(z, f->z + (size_t)i * d2, dim)) { fed_remove(f, i); merged = 1; break; }
+  }
+  fed_push(f, z);
+}
+/* The pieces of z \ (w[0] U .. U w[k-1]) appended to out (disjoint pieces; fed_subtract). */
+static void fed_subtract_rec(const int32_t* z, const int32_t* w, int k, int dim, Fed* out) {
+  const int d2 = dim * dim;
+  int32_t t[64 * 64];
+  int i = 0;
+  for (; i < k; ++i) if (dbm_intersect(t, z, w + (size_t)i * d2, dim)) break;
+  if (i == k) { fed_push(out, z); return; }
+  const int32_t* wi = w + (size_t)i * d2;
+  if (orc_dbm_includes(wi, z, dim)) return;
+  int32_t* r = (int32_t*)malloc(sizeof(int32_t) * d2 * 2);
+  int32_t* p = r + d2;
+  memcpy(r, z, sizeof(int32_t) * d2);
+  int alive = 1;
+  for (int a = 0; a < dim && alive; ++a)
+    for (int b = 0; b < dim && alive; ++b) {
+      if (a == b || wi[a * dim + b] >= r[a * dim + b]) continue;
+      memcpy(p, r, sizeof(int32_t) * d2);
+      if (orc_dbm_constrain(p, dim, b, a, r_negate(wi[a * dim + b])))
+        fed_subtract_rec(p, w + (size_t)(i + 1) * d2, k - i - 1, dim, out);
+      if (!orc_dbm_constrain(r, dim, a, b, wi[a * dim + b])) alive = 0;
+    }
+  free(r);
+}
+
+/* The recipe of one transition (GfpTag, src/liveness/operators.cpp:55-206): the participating
+ * local edges, sender first, and the abstaining broadcast receivers' guard complements. */
+#define TR_MAXAB 1024
+typedef struct { int ne; int edge[64]; int nab; int32_t ab[3 * TR_MAXAB]; } Trans;
+/* Rebuild the recipe of transition `want` (the raw index successors() gave it) of the discrete
+ * state (locs, ints): the same enumeration with no zone work. Returns 0 if there is none. */
+static int find_trans(const Model* m, const int32_t* locs, const int32_t* ints, int want, Trans* T) {
+  const hora_net_desc* n = m->n;
+  const int np = n->nprocs;
+  int src_c, src_u, raw = 0;
+  frozen_flags(m, locs, ints, &src_c, &src_u);
+  T->ne = 0; T->nab = 0;
+  for (int p = 0; p < np; ++p) {
+    if (src_c && !loc_committed(m, p, locs[p])) continue;
+    const int gp = m->loc_base[p] + locs[p];
+    for (int k = m->eloc_off[gp]; k < m->eloc_off[gp + 1]; ++k) {
+      const int e = m->eloc[k];
+      if (n->edge_chan[e] >= 0 || !int_ok(n, e, ints)) continue;
+      if (raw++ == want) { T->edge[T->ne++] = e; return 1; }
+    }
+  }
+  for (int i = 0; i < np; ++i) {
+    const int gi = m->loc_base[i] + locs[i];
+    for (int k = m->eloc_off[gi]; k < m->eloc_off[gi + 1]; ++k) {
+      const int se = m->eloc[k];
+      if (n->edge_chan[se] < 0 || n->edge_dir[se] != 1) continue;
+      if (n->chan_flags[n->edge_chan[se]] & HORA_CHAN_BROADCAST) continue;
+      if (!int_ok(n, se, ints)) continue;
+      const int i_comm = loc_committed(m, i, locs[i]);
+      for (int j = 0; j < np; ++j) {
+        if (j == i) continue;
+        const int gj = m->loc_base[j] + locs[j];
+        for (int q = m->eloc_off[gj]; q < m->eloc_off[gj + 1]; ++q) {
+          const int re = m->eloc[q];
+          if (n->edge_chan[re] != n->edge_chan[se] || n->edge_dir[re] != -1) continue;
+          if (src_c && !(i_comm || loc_committed(m, j, locs[j]))) continue;
+          if (!int_ok(n, re, ints)) continue;
+          if (raw++ == want) { T->edge[0] = se; T->edge[1] = re; T->ne = 2; return 1; }
+        }
+      }
+    }
+  }
+  Parts* P = parts_scratch();
+  for (int i = 0; i < np; ++i) {
+    const int gi = m->loc_base[i] + locs[i];
+    for (int k = m->eloc_off[gi]; k < m->eloc_off[gi + 1]; ++k) {
+      const int se = m->eloc[k];
+      if (n->edge_chan[se] < 0 || n->edge_dir[se] != 1 || !(n->chan_flags[n->edge_chan[se]] & HORA_CHAN_BROADCAST)) continue;
+      if (!int_ok(n, se, ints)) continue;
+      if (!build_broadcast_parts(m, locs, ints, se, i, P)) return 0;
+      int pick[MAXPART];
+      memset(pick, 0, sizeof pick);
+      for (;;) {
+        int part_comm = loc_committed(m, i, locs[i]);
+        for (int t = 0; t < P->nparts; ++t) {
+          const Part* pt = &P->parts[t];
+          if (pt->edge[pick[t]] >= 0 && loc_committed(m, pt->proc, locs[pt->proc])) part_comm = 1;
+        }
+        if (!src_c || part_comm) {
+          if (raw++ == want) {
+            T->edge[T->ne++] = se;
+            for (int t = 0; t < P->nparts; ++t) {
+              const Part* pt = &P->parts[t];
+              const int o = pick[t];
+              if (pt->edge[o] >= 0) { T->edge[T->ne++] = pt->edge[o]; continue; }
+              for (int c = 0; c < pt->xn[o]; ++c) {
+                if (T->nab == TR_MAXAB) return 0;
+                memcpy(T->ab + 3 * T->nab, P->xcons + 3 * (pt->xoff[o] + c), sizeof(int32_t) * 3);
+                T->nab++;
+              }
+            }
+            return 1;
+          }
+        }
+        if (P->nparts == 0) break;
+        int t = 0;
+        for (; t < P->nparts; ++t) { if (++pick[t] < P->parts[t].nopt) break; pick[t] = 0; }
+        if (t == P->nparts) break;
+      }
+    }
+  }
+  return 0;
+}
+/* Exact predecessor of the target valuations Y through T, from (sl, si) to (tl, ti), in place
+ * (exact_predecessor, src/liveness/operators.cpp:257-306): undo the active-clock reduction at the
+ * target, the target invariant and delay, the resets, the guards and abstain constraints, then the
+ * delay before the action. The !q restriction is adjoined to both invariants exactly as the
+ * successor pipeline adjoins it, and the source invariant also holds at the action point itself, so
+ * the result is the exact set of source valuations with a step into Y. Returns 0 when empty. */
+static int pre_trans(const Model* m, const Trans* T, const int32_t* sl, const int32_t* si, const int32_t* tl,
+                     const int32_t* ti, const uint8_t* qmask, int32_t* Y) {
+  const hora_net_desc* n = m->n;
+  const int dim = m->dim;
+  uint64_t act = 0;
+  for (int c = 1; c < dim; ++c) if (qmask[c]) act |= 1ull << c;
+  for (int p = 0; p < n->nprocs; ++p) act |= m->act[m->loc_base[p] + tl[p]];
+  for (int c = 1; c < dim; ++c) if (!((act >> c) & 1)) orc_dbm_free(Y, dim, c);
+  if (!apply_inv(m, Y, tl) || !avoid_cut(m, Y, tl, ti) || orc_dbm_empty(Y, dim)) return 0;
+  int fc, fu;
+  frozen_flags(m, tl, ti, &fc, &fu);
+  if (!fc && !fu) {
+    orc_dbm_down(Y, dim);
+    if (!apply_inv(m, Y, tl) || !avoid_cut(m, Y, tl, ti) || orc_dbm_empty(Y, dim)) return 0;
+  }
+  for (int k = 0; k < T->ne; ++k) {
+    const int e = T->edge[k];
+    for (int r = n->edge_reset_off[e]; r < n->edge_reset_off[e + 1]; ++r) {
+      const int x = n->resets[r];
+      if (!orc_dbm_constrain(Y, dim, x, 0, ORC_ZERO_LE) || !orc_dbm_constrain(Y, dim, 0, x, ORC_ZERO_LE)) return 0;
+    }
+  }
+  for (int k = 0; k < T->ne; ++k) {
+    const int e = T->edge[k];
+    for (int r = n->edge_reset_off[e]; r < n->edge_reset_off[e + 1]; ++r) orc_dbm_free(Y, dim, n->resets[r]);
+  }
+  for (int k = 0; k < T->ne; ++k) {
+    const int e = T->edge[k];
+    if (!apply_cons(Y, dim, n->cons, n->edge_guard_off[e], n->edge_guard_off[e + 1])) return 0;
+  }
+  if (T->nab && !apply_cons(Y, dim, T->ab, 0, T->nab)) return 0;
+  if (!apply_inv(m, Y, sl) || !avoid_cut(m, Y, sl, si) || orc_dbm_empty(Y, dim)) return 0;
+  frozen_flags(m, sl, si, &fc, &fu);
+  if (!fc && !fu) {
+    orc_dbm_down(Y, dim);
+    if (!apply_inv(m, Y, sl) || !avoid_cut(m, Y, sl, si) || orc_dbm_empty(Y, dim)) return 0;
+  }
+  return 1;
+}
+/* Stop(v) as a federation (stop_set, construction.cpp:1200-1239): the whole zone when time
+ * diverges inside !q (or, for a purely discrete q, when the state has no successor at all);
+ * nothing when q has a clock atom and the unrestricted location lets time run away; otherwise the
+ * deadlocked valuations of the zone in the unrestricted network (state_has_deadlock's residue,
+ * src/reachability/deadlock.cpp:262-267), as disjoint pieces. Returns 1 when it is the whole zone. */
+static int stop_fed(Model* m, const hora_pred_desc* q, const int32_t* locs, const int32_t* ints,
+                    const int32_t* zu, const uint8_t* qmask, Fed* out) {
+  const hora_pred_desc* av = m->avoid;
+  int whole = 0;
+  out->n = 0;
+  if (q->nclk == 0) {
+    m->avoid = NULL;
+    CountCtx cc = {NULL, 0};
+    successors(m, locs, ints, zu, m->L, m->U, qmask, 1, count_emit, &cc);
+    whole = cc.count == 0 || time_diverges(m, locs, ints, zu, 0);
+  } else {
+    whole = time_diverges(m, locs, ints, zu, 1);
+    if (!whole && orig_time_open(m, locs, ints)) { m->avoid = av; return 0; }
+    m->avoid = NULL;
+  }
+  if (whole) fed_push(out, zu);
+  else {
+    int32_t Z[64 * 64];
+    Escapes E = {0};
+    int frozen = 0;
+    if (deadlock_escapes(m, locs, ints, zu, &E, Z, &frozen) && !E.covered)
+      fed_subtract_rec(zu, E.w, E.nw, m->dim, out);
+    free(E.w);
+  }
+  m->avoid = av;
+  return whole;
+}
+
+typedef struct { uint64_t key; int idx; } KIdx;
+static int kidx_cmp(const void* a, const void* b) {
+  const KIdx* x = (const KIdx*)a; const KIdx* y = (const KIdx*)b;
+  if (x->key != y->key) return x->key < y->key ? -1 : 1;
+  return x->idx < y->idx ? -1 : (x->idx > y->idx);
+}
+/* One level of the inclusion graph. Candidates c = 0..n-1 (key, zone); cov[c] receives the node
+ * that covers c (an earlier-level node containing it, else the first stored candidate of the level
+ * containing it, or its own new node). New nodes are appended to G (level `level`) in candidate
+ * order; their ids are listed in *newids. */
+static void incl_level(Store* G, uint64_t** nkey, int* nkcap, int nc, const uint64_t* ckey, const int32_t* cz,
+                       int level, int dim, int* cov, IVec* newids, uint64_t* probes) {
+  const int d2 = dim * dim;
+  KIdx* sv = (KIdx*)malloc(sizeof(KIdx) * (nc ? nc : 1));
+  int ns = 0;
+  for (int c = 0; c < nc; ++c) {
+    cov[c] = -1;
+    const uint64_t si = slot_of(G, ckey[c]);
+    if (G->shead[si] != -2)
+      for (int nd = G->shead[si]; nd >= 0; nd = G->next[nd]) {
+        if (probes) (*probes)++;
+        if (orc_dbm_includes(G->zones + (size_t)nd * d2, cz + (size_t)c * d2, dim)) { cov[c] = nd; break; }
+      }
+    if (cov[c] < 0) { sv[ns].key = ckey[c]; sv[ns].idx = c; ns++; }
+  }
+  qsort(sv, ns, sizeof(KIdx), kidx_cmp);
+  char* keep = (char*)calloc(nc ? nc : 1, 1);
+  for (int a = 0; a < ns;) {
+    int b = a;
+    while (b < ns && sv[b].key == sv[a].key) ++b;
+    for (int i = a; i < b; ++i) {
+      const int32_t* zi = cz + (size_t)sv[i].idx * d2;
+      int kept = 1;
+      for (int j = a; j < b && kept; ++j) {
+        if (j == i) continue;
+        const int32_t* zj = cz + (size_t)sv[j].idx * d2;
+        if (!orc_dbm_includes(zj, zi, dim)) continue;
+        if (j < i || memcmp(zi, zj, sizeof(int32_t) * d2) != 0) kept = 0;
+      }
+      keep[sv[i].idx] = (char)kept;
+    }
+    a = b;
+  }
+  for (int c = 0; c < nc; ++c) {
+    if (!keep[c]) continue;
+    if ((uint64_t)(G->nkeys + 1) * 10 >= (G->smask + 1) * 7) store_grow(G);
+    const uint64_t si = slot_of(G, ckey[c]);
+    if (G->shead[si] == -2) { G->skey[si] = ckey[c]; G->shead[si] = -1; G->nkeys++; }
+    const int id = store_node(G, cz + (size_t)c * d2, level, G->shead[si]);
+    G->shead[si] = id;
+    if (id >= *nkcap) { *nkcap = *nkcap ? *nkcap * 2 : 1024; *nkey = (uint64_t*)realloc(*nkey, sizeof(uint64_t) * *nkcap); }
+    (*nkey)[id] = ckey[c];
+    cov[c] = id;
+    iv_push(newids, id);
+  }
+  /* a survivor not stored: the first stored survivor of its key (candidate order) containing it */
+  for (int a = 0; a < ns;) {
+    int b = a;
+    while (b < ns && sv[b].key == sv[a].key) ++b;
+    for (int i = a; i < b; ++i) {
+      const int c = sv[i].idx;
+      if (keep[c]) continue;
+      for (int j = a; j < b; ++j)
+        if (keep[sv[j].idx] && orc_dbm_includes(cz + (size_t)sv[j].idx * d2, cz + (size_t)c * d2, dim)) {
+          cov[c] = cov[sv[j].idx];
+          break;
+        }
+    }
+    a = b;
+  }
+  free(keep); free(sv);
+}
+
+/* Phase 2 of p --> q on the subsumed graph, from phase 1's store R. */
+static int32_t leadsto_subsumed(Model* m, Store* R, const hora_pred_desc* p, const hora_pred_desc* q,
+                                const uint8_t* qmask, hora_stats* S0, double t0, int* violated_out) {
+  const hora_net_desc* net = m->n;
+  const int dim = m->dim, d2 = dim * dim, np = net->nprocs, ni = net->nints;
+  int32_t locs[64], ints[64], z2[64 * 64];
+  Store G;
+  store_init(&G, d2);
+  uint64_t* nkey = NULL; int nkcap = 0;
+  IVec efrom = {0}, eto = {0}, eraw = {0}, roots = {0}, front = {0};
+  int timed_out = 0, violated = 0;
+  /* ---- roots ---- */
+  {
+    uint64_t* ck = NULL; int32_t* cz = NULL; int nc = 0, cc = 0;
+    for (uint64_t i = 0; i <= R->smask; ++i) {
+      if (R->shead[i] == -2) continue;
+      key_decode(m, R->skey[i], locs, ints);
+      if (!disc_match(p, locs, ints)) continue;
+      for (int nd = R->shead[i]; nd >= 0; nd = R->next[nd]) {
+        if (R->dead[nd]) continue;
+        memcpy(z2, R->zones + (size_t)nd * d2, sizeof(int32_t) * d2);
+        if (!apply_cons(z2, dim, p->clk_cond, 0, p->nclk)) continue;
+        if (!avoid_cut(m, z2, locs, ints) || orc_dbm_empty(z2, dim)) continue;
+        if (nc == cc) { cc = cc ? cc * 2 : 64; ck = (uint64_t*)realloc(ck, 8 * (size_t)cc); cz = (int32_t*)realloc(cz, sizeof(int32_t) * d2 * (size_t)cc); }
+        ck[nc] = R->skey[i];
+        memcpy(cz + (size_t)nc * d2, z2, sizeof(int32_t) * d2);
+        nc++;
+      }
+    }
+    int* cov = (int*)malloc(sizeof(int) * (nc ? nc : 1));
+    incl_level(&G, &nkey, &nkcap, nc, ck, cz, 0, dim, cov, &roots, NULL);
+    free(cov); free(ck); free(cz);
+  }
+  /* early witness: a root holding a stop valuation starts a maximal !q-run */
+  Fed sf;
+  fed_init(&sf, d2);
+  for (int r = 0; r < roots.n && !violated; ++r) {
+    key_decode(m, nkey[roots.a[r]], locs, ints);
+    stop_fed(m, q, locs, ints, G.zones + (size_t)roots.a[r] * d2, qmask, &sf);
+    if (sf.n) violated = 1;
+  }
+  int level = 0;
+  if (!violated) {
+    for (int r = 0; r < roots.n; ++r) iv_push(&front, roots.a[r]);
+    SuccBuf B = {0};
+    B.np = np; B.ni = ni; B.d2 = d2;
+    uint64_t* ck = NULL; int ckcap = 0;
+    int* cov = NULL;
+    while (front.n > 0 && !timed_out) {
+      if (g_time_limit > 0 && now_s() - t0 > g_time_limit) { timed_out = 1; break; }
+      S0->explored += front.n;
+      ++level;
+      B.n = 0;
+      for (int f = 0; f < front.n; ++f) {
+        if (over_time(t0, f)) { timed_out = 1; break; }
+        key_decode(m, nkey[front.a[f]], locs, ints);
+        B.cur_parent = front.a[f];
+        successors(m, locs, ints, G.zones + (size_t)front.a[f] * d2, m->L, m->U, qmask, 1, sb_emit, &B);
+      }
+      if (timed_out) break;
+      S0->generated += B.n;
+      if (B.n > ckcap) { ckcap = B.n; ck = (uint64_t*)realloc(ck, 8 * (size_t)ckcap); cov = (int*)realloc(cov, sizeof(int) * ckcap); }
+      for (int b = 0; b < B.n; ++b) ck[b] = key_encode(m, B.locs + (size_t)b * np, B.ints + (size_t)b * ni);
+      IVec nxt = {0};
+      incl_level(&G, &nkey, &nkcap, B.n, ck, B.zones, level, dim, cov, &nxt, &S0->probes);
+      for (int b = 0; b < B.n; ++b) { iv_push(&efrom, B.parent[b]); iv_push(&eto, cov[b]); iv_push(&eraw, B.raw[b]); }
+      free(front.a);
+      front = nxt;
+    }
+    free(B.locs); free(B.ints); free(B.zones); free(B.raw); free(B.parent);
+    free(ck); free(cov);
+  }
+  S0->stored = (uint64_t)G.nn;
+  S0->keys = (uint64_t)G.nkeys;
+  S0->levels = (uint64_t)level;
+  /* ---- the backward sweep: a worklist of nodes whose successors' W changed ---- */
+  if (!violated && !timed_out && G.nn > 0) {
+    const int N = G.nn, E = efrom.n;
+    int* off = (int*)calloc(N + 1, sizeof(int));        /* out-edges by source */
+    int* eidx = (int*)malloc(sizeof(int) * (E ? E : 1));
+    int* roff = (int*)calloc(N + 1, sizeof(int));       /* sources by target */
+    int* rsrc = (int*)malloc(sizeof(int) * (E ? E : 1));
+    for (int e = 0; e < E; ++e) { off[efrom.a[e] + 1]++; roff[eto.a[e] + 1]++; }
+    for (int u = 0; u < N; ++u) { off[u + 1] += off[u]; roff[u + 1] += roff[u]; }
+    {
+      int* f1 = (int*)calloc(N + 1, sizeof(int));
+      int* f2 = (int*)calloc(N + 1, sizeof(int));
+      for (int e = 0; e < E; ++e) {
+        eidx[off[efrom.a[e]] + f1[efrom.a[e]]++] = e;
+        rsrc[roff[eto.a[e]] + f2[eto.a[e]]++] = efrom.a[e];
+      }
+      free(f1); free(f2);
+    }
+    Fed* W = (Fed*)malloc(sizeof(Fed) * N);
+    Fed* ST = (Fed*)malloc(sizeof(Fed) * N);
+    char* whole = (char*)calloc(N, 1);
+    char* isroot = (char*)calloc(N, 1);
+    for (int r = 0; r < roots.n; ++r) isroot[roots.a[r]] = 1;
+    for (int u = 0; u < N; ++u) {
+      fed_init(&W[u], d2); fed_init(&ST[u], d2);
+      fed_push(&W[u], G.zones + (size_t)u * d2);
+      if (timed_out || over_time(t0, u)) { timed_out = 1; continue; }
+      key_decode(m, nkey[u], locs, ints);
+      whole[u] = (char)stop_fed(m, q, locs, ints, G.zones + (size_t)u * d2, qmask, &ST[u]);
+    }
+    int* queue = (int*)malloc(sizeof(int) * N);
+    char* inq = (char*)malloc(N);
+    int qh = 0, qn = N;
+    for (int u = 0; u < N; ++u) { queue[u] = N - 1 - u; inq[u] = 1; }   /* deepest first */
+    int live_roots = roots.n;
+    Fed nw;
+    fed_init(&nw, d2);
+    int32_t Y[64 * 64], X[64 * 64], tl[64], tlI[64];
+    char* cov = NULL;
+    int covcap = 0;
+    Trans* Tp = (Trans*)malloc(sizeof(Trans));
+    while (qn > 0 && !timed_out && live_roots > 0) {
+      const int v = queue[qh];
+      qh = (qh + 1) % N; qn--; inq[v] = 0;
+      S0->gfp_iters++;
+      if (over_time(t0, (int)S0->gfp_iters)) { timed_out = 1; break; }
+      if (W[v].n == 0 || whole[v]) continue;
+      key_decode(m, nkey[v], locs, ints);
+      nw.n = 0;
+      const int nwv = W[v].n;
+      if (nwv > covcap) { covcap = nwv * 2; cov = (char*)realloc(cov, covcap); }
+      memset(cov, 0, nwv);
+      int ncov = 0;
+      #define ORC_OFFER(CAND) do { \
+          for (int i_ = 0; i_ < nwv; ++i_) { \
+            const int32_t* w_ = W[v].z + (size_t)i_ * d2; \
+            if (!dbm_intersect(X, w_, (CAND), dim)) continue; \
+            if (!cov[i_] && orc_dbm_includes((CAND), w_, dim)) { cov[i_] = 1; ncov++; } \
+            fed_add_compact(&nw, X, dim); \
+          } } while (0)
+      for (int c = 0; c < ST[v].n && ncov < nwv; ++c) ORC_OFFER(ST[v].z + (size_t)c * d2);
+      for (int k = off[v]; k < off[v + 1] && ncov < nwv; ++k) {
+        const int e = eidx[k], j = eto.a[e];
+        if (W[j].n == 0) continue;
+        if (!find_trans(m, locs, ints, eraw.a[e], Tp)) continue;
+        key_decode(m, nkey[j], tl, tlI);
+        for (int y = 0; y < W[j].n && ncov < nwv; ++y) {
+          memcpy(Y, W[j].z + (size_t)y * d2, sizeof(int32_t) * d2);
+          S0->pre_calls++;
+          if (!pre_trans(m, Tp, locs, ints, tl, tlI, qmask, Y)) continue;
+          ORC_OFFER(Y);
+        }
+      }
+      #undef ORC_OFFER
+      if (ncov == nwv) continue;                       /* every piece survives whole: unchanged */
+      int changed = 0;
+      for (int i = 0; i < nwv && !changed; ++i)
+        if (!cov[i] && !orc_fed_covers(W[v].z + (size_t)i * d2, nw.z, nw.n, dim)) changed = 1;
+      if (!changed) continue;
+      Fed tmp = W[v]; W[v] = nw; nw = tmp;
+      if (isroot[v] && W[v].n == 0) live_roots--;
+      for (int k = roff[v]; k < roff[v + 1]; ++k) {
+        const int u = rsrc[k];
+        if (!inq[u]) { inq[u] = 1; queue[(qh + qn) % N] = u; qn++; }
+      }
+    }
+    for (int r = 0; r < roots.n && !violated && !timed_out; ++r) violated = W[roots.a[r]].n > 0;
+    fed_free(&nw);
+    free(cov); free(Tp);
+    for (int u = 0; u < N; ++u) { fed_free(&W[u]); fed_free(&ST[u]); }
+    free(W); free(ST); free(whole); free(isroot); free(queue); free(inq);
+    free(off); free(eidx); free(roff); free(rsrc);
+  }
+  fed_free(&sf);
+  free(nkey); free(efrom.a); free(eto.a); free(eraw.a); free(roots.a); free(front.a);
+  store_free(&G);
+  if (timed_out) S0->status = HORA_E_TIMEOUT;
+  *violated_out = violated;
   return HORA_OK;
 }
 
@@ -1659,7 +2193,7 @@ int32_t orc_eg_successors(const hora_net_desc* net, const hora_pred_desc* psi, c
     if (B.ni) memcpy(out_ints + (size_t)k * B.ni, B.ints + (size_t)k * B.ni, sizeof(int32_t) * B.ni);
     memcpy(out_zones + (size_t)k * B.d2, B.zones + (size_t)k * B.d2, sizeof(int32_t) * B.d2);
   }
-  free(B.locs); free(B.ints); free(B.zones);
+  free(B.locs); free(B.ints); free(B.zones); free(B.raw); free(B.parent);
   model_free(&m);
   return HORA_OK;
 }
