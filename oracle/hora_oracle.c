@@ -1401,6 +1401,8 @@ static void count_emit(void* c, const int32_t* l, const int32_t* i, const int32_
 
 static int32_t leadsto_subsumed(Model* m, Store* R, const hora_pred_desc* p, const hora_pred_desc* q,
                                 const uint8_t* qmask, hora_stats* S0, double t0, int* violated_out);
+static int leadsto_witness_at(Model* m, const hora_pred_desc* p, const hora_pred_desc* q, const int32_t* locs,
+                              const int32_t* ints, const int32_t* zone, const uint8_t* qmask);
 /* p --> q (psi NULL), or E[] psi (p, q NULL): the two share the restricted exact zone graph, its
  * stop sets and the greatest fixpoint. E[] psi roots the graph at the initial state of the
  * psi-restricted network instead of at the p-states of a reachability pass. */
@@ -1451,6 +1453,7 @@ static int32_t liveness_core(const hora_net_desc* net, const hora_pred_desc* p, 
     int id = store_add(&R, k0, zone, 0, dim, m.L, m.U, NULL);
     capfr = 16; fr = (FItem*)malloc(sizeof(FItem) * capfr);
     fr[0].key = k0; fr[0].node = id; nfr = 1;
+    if (leadsto_witness_at(&m, p, q, locs, ints, zone, qmask)) { violated = 1; nfr = 0; }
   }
   int level = 0;
   int timed_out = 0;
@@ -1481,6 +1484,13 @@ static int32_t liveness_core(const hora_net_desc* net, const hora_pred_desc* p, 
     if (timed_out) break;
     nfr = collect_frontier(&R, level, &fr, &capfr);
     if (emode == 0 && R.nkeys && (double)R.nlive >= 4.0 * (double)R.nkeys) emode = 1;
+    /* p --> q: the early witness on every zone this level stored (leadsto_witness,
+       construction.cpp:786-826); the search stops at the level that finds one */
+    for (int f = 0; f < nfr && !psi && !violated; ++f) {
+      key_decode(&m, fr[f].key, locs, ints);
+      violated = leadsto_witness_at(&m, p, q, locs, ints, R.zones + (size_t)fr[f].node * d2, qmask);
+    }
+    if (violated) break;
   }
   /* ---- roots: the p-part of every stored zone, cut to !q; for E[] psi, the initial state ---- */
   m.avoid = psi ? psi : q;
@@ -1489,9 +1499,10 @@ static int32_t liveness_core(const hora_net_desc* net, const hora_pred_desc* p, 
     m.avoid_neg[0] = q->clk_cond[1]; m.avoid_neg[1] = q->clk_cond[0]; m.avoid_neg[2] = r_negate(q->clk_cond[2]);
   }
   if (!psi) {   /* p --> q: the subsumed graph and the federation sweep */
-    int viol = 0;
+    int viol = violated;
     if (timed_out) S0.status = HORA_E_TIMEOUT;
-    else leadsto_subsumed(&m, &R, p, q, qmask, &S0, t0, &viol);
+    else if (!viol) leadsto_subsumed(&m, &R, p, q, qmask, &S0, t0, &viol);
+    else S0.levels = (uint64_t)level;
     store_free(&R);
     S0.expanded = S0.explored;
     S0.seconds = now_s() - t0;
@@ -1878,6 +1889,35 @@ static int stop_fed(Model* m, const hora_pred_desc* q, const int32_t* locs, cons
   return whole;
 }
 
+/* The early witness of p --> q at a reachable zone (leadsto_witness, construction.cpp:786-826): its
+ * p-part, cut to !q, holds a valuation where a maximal !q-run may stop (Stop above) -- that run
+ * never meets q, so the property is violated. m->avoid is set for the test only (phase 1 explores
+ * the unrestricted network). */
+static int leadsto_witness_at(Model* m, const hora_pred_desc* p, const hora_pred_desc* q, const int32_t* locs,
+                              const int32_t* ints, const int32_t* zone, const uint8_t* qmask) {
+  if (!disc_match(p, locs, ints)) return 0;
+  const int dim = m->dim;
+  int32_t z[64 * 64];
+  memcpy(z, zone, sizeof(int32_t) * dim * dim);
+  if (!apply_cons(z, dim, p->clk_cond, 0, p->nclk)) return 0;
+  const hora_pred_desc* av = m->avoid;
+  const int ap = m->avoid_psi;
+  int32_t an[3] = {m->avoid_neg[0], m->avoid_neg[1], m->avoid_neg[2]};
+  m->avoid = q; m->avoid_psi = 0;
+  if (q->nclk == 1) { m->avoid_neg[0] = q->clk_cond[1]; m->avoid_neg[1] = q->clk_cond[0]; m->avoid_neg[2] = r_negate(q->clk_cond[2]); }
+  int hit = 0;
+  if (avoid_cut(m, z, locs, ints) && !orc_dbm_empty(z, dim)) {
+    Fed f;
+    fed_init(&f, dim * dim);
+    stop_fed(m, q, locs, ints, z, qmask, &f);
+    hit = f.n > 0;
+    fed_free(&f);
+  }
+  m->avoid = av; m->avoid_psi = ap;
+  memcpy(m->avoid_neg, an, sizeof an);
+  return hit;
+}
+
 typedef struct { uint64_t key; int idx; } KIdx;
 static int kidx_cmp(const void* a, const void* b) {
   const KIdx* x = (const KIdx*)a; const KIdx* y = (const KIdx*)b;
@@ -1983,14 +2023,6 @@ static int32_t leadsto_subsumed(Model* m, Store* R, const hora_pred_desc* p, con
     int* cov = (int*)malloc(sizeof(int) * (nc ? nc : 1));
     incl_level(&G, &nkey, &nkcap, nc, ck, cz, 0, dim, cov, &roots, NULL);
     free(cov); free(ck); free(cz);
-  }
-  /* early witness: a root holding a stop valuation starts a maximal !q-run */
-  Fed sf;
-  fed_init(&sf, d2);
-  for (int r = 0; r < roots.n && !violated; ++r) {
-    key_decode(m, nkey[roots.a[r]], locs, ints);
-    stop_fed(m, q, locs, ints, G.zones + (size_t)roots.a[r] * d2, qmask, &sf);
-    if (sf.n) violated = 1;
   }
   int level = 0;
   if (!violated) {
@@ -2119,7 +2151,6 @@ static int32_t leadsto_subsumed(Model* m, Store* R, const hora_pred_desc* p, con
     free(W); free(ST); free(whole); free(isroot); free(queue); free(inq);
     free(off); free(eidx); free(roff); free(rsrc);
   }
-  fed_free(&sf);
   free(nkey); free(efrom.a); free(eto.a); free(eraw.a); free(roots.a); free(front.a);
   store_free(&G);
   if (timed_out) S0->status = HORA_E_TIMEOUT;

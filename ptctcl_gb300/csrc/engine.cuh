@@ -95,6 +95,15 @@ struct Ctl {
   long long nlive;               // live passed-store zones
   unsigned int err;              // HORA_E_* raised on the device (table full, escape overflow)
   unsigned int flag;             // set by a fixpoint pass that changed something
+  // federation sweep of the subsumed leads-to graph
+  unsigned long long spieces;    // stop-set pieces allocated
+  unsigned long long walloc;     // W-arena zones allocated
+  unsigned long long ndirty;     // nodes to relax in the next round
+  unsigned long long nchanged;   // nodes whose W shrank this round
+  unsigned long long npre;       // exact predecessors computed
+  unsigned long long nroots_live; // roots whose W is not yet empty
+  unsigned int fed_over;         // a federation outgrew its slots (the sweep restarts with more)
+  unsigned int stop_over;        // the stop-set arena overflowed (the pass re-runs with more)
 };
 constexpr unsigned long long kCtlChunkBytes = 10 * 8 + 2 * 4;
 

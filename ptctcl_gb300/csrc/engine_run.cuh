@@ -125,14 +125,14 @@ struct Engine {
   int blocks = 0;
   DeviceNets dn;
   StoreBufs<D> S[2];
-  DBuf skey, sparent, sord, sslot, srank, szone, ssurv, sseg, ssorted, stouched, sokh, sokl, sskh, sskl, sheavy,
-      slight;
+  DBuf skey, sparent, sord, sraw, sflag, sslot, srank, szone, ssurv, sseg, ssorted, stouched, sokh, sokl, sskh, sskl,
+      sheavy, slight;
   long long scap = 0;
   DBuf clist;
   long long ccap = 0;
   DBuf fkey[2], fnode[2], frank[2], finst[2];
   long long fcapb[2] = {0, 0};
-  DBuf esrc, edst, eord;
+  DBuf esrc, edst, eord, eraw;
   long long ecap = 0;
   int merge_blocks = 0;         // resident blocks of the merge kernel (it schedules keys itself)
   DBuf hv_n, hv_a, hv_cb, hv_bm, hv_bounds, hv_pool, hv_prefix, hv_order;   // keys merged block-wide
@@ -178,6 +178,7 @@ struct Engine {
     Succ sc;
     sc.key = skey.template as<unsigned long long>(); sc.parent = sparent.template as<int>();
     sc.ord = sord.template as<int>(); sc.slot = sslot.template as<int>(); sc.rank = srank.template as<int>();
+    sc.raw = sraw.template as<int>(); sc.flag = sflag.template as<int>();
     sc.zone = szone.template as<int>(); sc.surv = ssurv.template as<int>(); sc.seg = sseg.template as<int>();
     sc.sorted = ssorted.template as<int>(); sc.touched = stouched.template as<int>(); sc.cap = scap;
     sc.okh = sokh.template as<unsigned long long>(); sc.okl = sokl.template as<unsigned long long>();
@@ -195,7 +196,9 @@ struct Engine {
     f.rank = frank[b].template as<int>(); f.inst = finst[b].template as<int>();
     return f;
   }
-  Edges edges() { return Edges{esrc.template as<int>(), edst.template as<int>(), eord.template as<int>(), ecap}; }
+  Edges edges() {
+    return Edges{esrc.template as<int>(), edst.template as<int>(), eord.template as<int>(), ecap, eraw.template as<int>()};
+  }
   ZTab ztab() { return ZTab{zw.template as<unsigned long long>(), zcap - 1}; }
   InstState istate() {
     InstState is;
@@ -232,6 +235,7 @@ struct Engine {
   int alloc_succ(long long cap) {
     scap = cap;
     HGB_CUDA(skey.alloc(cap * 8)); HGB_CUDA(sparent.alloc(cap * 4)); HGB_CUDA(sord.alloc(cap * 4));
+    HGB_CUDA(sraw.alloc(cap * 4)); HGB_CUDA(sflag.alloc(cap * 4));
     HGB_CUDA(sslot.alloc(cap * 4)); HGB_CUDA(srank.alloc(cap * 4)); HGB_CUDA(szone.alloc(cap * Z2 * 4));
     HGB_CUDA(ssurv.alloc(cap * 4)); HGB_CUDA(sseg.alloc(cap * 4)); HGB_CUDA(ssorted.alloc(cap * 4));
     HGB_CUDA(stouched.alloc(cap * 4));
@@ -353,6 +357,81 @@ struct Engine {
     if (hctl.err) { err = "device error in the graph store"; return (int)hctl.err; }
     return HORA_OK;
   }
+  // One level of the subsumed leads-to graph: inclusion probe against the key's stored zones, the
+  // maximal survivors of each key stored, every successor's edge to its covering node.
+  int incl_level(const NetView* V, int k, int cur, long long nsucc, int level, bool roots) {
+    int rc;
+    InstState is = istate();
+    if (nsucc > 0) {
+      kt.begin(s);
+      Level<D>::incl_probe(V, is, succ(), store(k), dctl(), nsucc, blocks, s);
+      kt.end(s, KT_PROBE);
+      ++launches;
+      HGB_CUDA(cudaGetLastError());
+    }
+    if ((rc = read_ctl())) return rc;
+    if (hctl.err) { err = "device error in the inclusion probe"; return (int)hctl.err; }
+    const long long nsurv = (long long)hctl.nsurv, ntouched = (long long)hctl.ntouched;
+    if ((rc = ensure_nodes(k, nsurv))) return rc;
+    if ((rc = ensure_arena(k, std::max<long long>(0, hctl.nlive) + nsurv))) return rc;
+    if ((rc = grow_front(cur ^ 1, (long long)hctl.nfront, nsurv))) return rc;
+    const bool record = !roots;
+    if (record && (rc = ensure_edges((long long)hctl.nedges + nsucc))) return rc;
+    if (ntouched > 0) {
+      kt.begin(s);
+      Level<D>::incl_group(succ(), store(k), dctl(), nsucc, ntouched, s);
+      kt.end(s, KT_GROUP, 2);
+      kt.begin(s);
+      Level<D>::incl_keep(succ(), store(k), dctl(), nsurv, blocks, s);
+      Level<D>::incl_store(V, is, succ(), store(k), front(cur ^ 1), dctl(), nsurv, level, blocks, s);
+      Level<D>::incl_cover(succ(), store(k), dctl(), nsurv, blocks, s);
+      Level<D>::incl_lists(V, is, succ(), store(k), dctl(), ntouched, s);
+      kt.end(s, KT_MERGE, 4);
+      launches += 6;
+      HGB_CUDA(cudaGetLastError());
+    }
+    if (record && nsucc > 0) {
+      kt.begin(s);
+      Level<D>::incl_edges(succ(), front(cur), edges(), dctl(), nsucc, s);
+      kt.end(s, KT_MERGE);
+      ++launches;
+      HGB_CUDA(cudaGetLastError());
+    }
+    if ((rc = read_ctl())) return rc;
+    if (hctl.err) { err = "device error in the inclusion store"; return (int)hctl.err; }
+    return HORA_OK;
+  }
+  // The early witness of p --> q on the n phase-1 nodes of frontier b (leadsto_witness,
+  // src/liveness/construction.cpp:786-826): an instance whose reachable p-zone, cut to !q, holds a
+  // stop valuation is violated and stops.
+  int leadsto_witness(int b, long long n) {
+    bool any = false;
+    for (int q = 0; q < ninst; ++q) any |= nets[q]->kind == HORA_Q_LEADSTO && !h_done[q];
+    if (!any || n <= 0) return HORA_OK;
+    InstState is = istate();
+    Fix fx{};
+    kt.begin(s);
+    Level<D>::stop_fed(dn.views, is, store(0), 0, n, front(b).node, fx, dctl(), 1, blocks, s);
+    kt.end(s, KT_DEADLOCK);
+    ++launches;
+    HGB_CUDA(cudaGetLastError());
+    int rc = read_ctl();
+    if (rc) return rc;
+    if (hctl.err) { err = "device error in the leads-to witness test"; return (int)hctl.err; }
+    const size_t ni4 = (size_t)ninst * 4;
+    HGB_CUDA(cudaMemcpyAsync(h_found.data(), is.found, ni4, cudaMemcpyDeviceToHost, s));
+    HGB_CUDA(cudaStreamSynchronize(s));
+    d2h += ni4;
+    bool changed = false;
+    const double now = elapsed();
+    for (int q = 0; q < ninst; ++q)
+      if (!h_done[q] && h_found[q]) { h_done[q] = 1; changed = true; if (t_fin[q] < 0) t_fin[q] = now; }
+    if (changed) {
+      HGB_CUDA(cudaMemcpyAsync(is.done, h_done.data(), ni4, cudaMemcpyHostToDevice, s));
+      h2d += ni4;
+    }
+    return HORA_OK;
+  }
   // Bytes one stored node takes (zone, its column 0, level, dead flag, instance, key).
   static constexpr long long kNodeBytes = Z2 * 4 + D * 4 + 20;
   // Nodes the store budget allows (unbounded without a budget).
@@ -384,6 +463,7 @@ struct Engine {
     HGB_CUDA(esrc.grow(c * 4, used * 4, s));
     HGB_CUDA(edst.grow(c * 4, used * 4, s));
     HGB_CUDA(eord.grow(c * 4, used * 4, s));
+    HGB_CUDA(eraw.grow(c * 4, used * 4, s));
     ecap = c;
     return HORA_OK;
   }
@@ -495,6 +575,7 @@ struct Engine {
       for (size_t c = 0; c + 1 < cuts.size(); ++c)
         if ((rc = run_chunk(k, mode, cur, nf, level, roots, roots_src, V, cuts[c], cuts[c + 1]))) return rc;
       // ---- end of level: goals and the adaptive extrapolation (store 0 only)
+      if (mode == 0 && (rc = leadsto_witness(cur ^ 1, (long long)hctl.nfront))) return rc;
       if (mode == 0) {
         HGB_CUDA(cudaMemcpyAsync(h_found.data(), is.found, ni4, cudaMemcpyDeviceToHost, s));
         HGB_CUDA(cudaMemcpyAsync(h_nlive.data(), is.nlive, ni8, cudaMemcpyDeviceToHost, s));
@@ -536,7 +617,7 @@ struct Engine {
   int enforce_budget(int mode) {
     const size_t ni4 = (size_t)ninst * 4, ni8 = (size_t)ninst * 8;
     InstState is = istate();
-    if (mode == 1) {
+    if (mode >= 1) {
       HGB_CUDA(cudaMemcpyAsync(h_nlive.data(), is.nlive, ni8, cudaMemcpyDeviceToHost, s));
       HGB_CUDA(cudaStreamSynchronize(s));
     }
@@ -668,6 +749,7 @@ struct Engine {
     }
     if ((rc = ensure_hash(k, (unsigned long long)nsucc))) return rc;
     if (mode == 1) return graph_level(V, k, cur, nsucc, level, roots);   // exact-zone graph
+    if (mode == 2) return incl_level(V, k, cur, nsucc, level, roots);    // subsumed leads-to graph
     // ---- deadlock goal, on every successor before the probe: a successor the probe would drop lies
     // in a_M of a stored zone, whose valuations were all tested, and a_M is a bisimulation, so the
     // verdict and its level are those of testing the survivors only; an instance found here skips
@@ -754,16 +836,19 @@ struct Engine {
     return HORA_OK;
   }
 
-  // Leads-to after phase 1: roots, the exact !q graph, stop flags and the greatest fixpoint.
+  // Leads-to after phase 1: roots, the !q graph, stop sets and the greatest fixpoint -- the subsumed
+  // graph with the federation sweep for p --> q, the exact-zone graph with node flags for E[] psi.
   int leadsto_phase2(int& cur) {
     int rc;
     InstState is = istate();
+    const bool eg = nets[0]->kind == HORA_Q_EG;
     const long long n1 = (long long)hctl.nnodes;
     // counters of store 1 start from zero; phase 1's stay in the per-instance totals
     HGB_CUDA(cudaMemsetAsync(&dctl()->nnodes, 0, 8, s));
     HGB_CUDA(cudaMemsetAsync(&dctl()->nkeys, 0, 8, s));
     HGB_CUDA(cudaMemsetAsync(&dctl()->nslots, 0, 8, s));
     HGB_CUDA(cudaMemsetAsync(&dctl()->nlive, 0, 8, s));
+    HGB_CUDA(cudaMemsetAsync(&dctl()->arena_alloc, 0, 8, s));
     HGB_CUDA(cudaMemsetAsync(is.nlive, 0, (size_t)ninst * 8, s));
     HGB_CUDA(cudaMemsetAsync(is.nkeys, 0, (size_t)ninst * 8, s));
     HGB_CUDA(cudaMemsetAsync(is.nfront, 0, (size_t)ninst * 8, s));
@@ -786,7 +871,8 @@ struct Engine {
     int level = 0;
     // the reported level count is the graph's: per instance, its last level with a frontier
     for (int q = 0; q < ninst; ++q) levels[q] = 0;
-    if ((rc = run_levels(1, 1, cur, nf, level, S[0].nzone.template as<int>()))) return rc;
+    if ((rc = run_levels(1, eg ? 1 : 2, cur, nf, level, S[0].nzone.template as<int>()))) return rc;
+    if (!eg) return fed_sweep();
     // stop flags and the sweep
     const long long n2 = (long long)hctl.nnodes, ne = (long long)hctl.nedges;
     DBuf stop, W, F;
@@ -829,6 +915,137 @@ struct Engine {
     pre_calls = (unsigned long long)ne;
     if (o.trace && ninst == 1 && nets[0]->kind == HORA_Q_EG)
       return extract_trace(n2, ne, W.template as<int>(), stop.template as<int>());
+    return HORA_OK;
+  }
+
+  // The federation sweep of p --> q over the subsumed graph: stop sets, the edges by source, then
+  // Jacobi rounds of W = W /\ (Stop \/ Pre(W)) over the nodes whose successors changed, until nothing
+  // changes or every root is empty. A federation that outgrows its K zones restarts the sweep with
+  // twice the room (up to kFedMax; past it the query reports HORA_E_OVERFLOW, the reference's
+  // capped fixpoint).
+  int fed_sweep() {
+    int rc;
+    InstState is = istate();
+    const long long n2 = (long long)hctl.nnodes, ne = (long long)hctl.nedges;
+    const Store st = store(1);
+    const Edges ed = edges();
+    // stop sets, re-run with a larger piece arena if they overflow it
+    DBuf swhole, shead, snext, spiece, eoff, eidx, tmp, woff, wcnt, woff2, wcnt2, warena, dirty, dlist, chg, clst, scratch;
+    const long long nn = std::max<long long>(n2, 1);
+    HGB_CUDA(swhole.alloc(nn * 4)); HGB_CUDA(shead.alloc(nn * 4));
+    Fix fx{};
+    fx.swhole = swhole.template as<int>(); fx.shead = shead.template as<int>();
+    long long scap = std::max<long long>(1 << 14, n2 / 4);
+    for (;;) {
+      HGB_CUDA(snext.alloc(scap * 4)); HGB_CUDA(spiece.alloc(scap * Z2 * 4));
+      fx.snext = snext.template as<int>(); fx.spiece = spiece.template as<int>(); fx.scap = scap;
+      HGB_CUDA(cudaMemsetAsync(&dctl()->spieces, 0, 8, s));
+      HGB_CUDA(cudaMemsetAsync(&dctl()->stop_over, 0, 4, s));
+      kt.begin(s);
+      Level<D>::stop_fed(dn.views, is, st, 0, n2, nullptr, fx, dctl(), 0, blocks, s);
+      kt.end(s, KT_DEADLOCK);
+      ++launches;
+      HGB_CUDA(cudaGetLastError());
+      if ((rc = read_ctl())) return rc;
+      if (hctl.err) { err = "stop-set test exceeded its escape table"; return (int)hctl.err; }
+      if (!hctl.stop_over) break;
+      scap = 2 * (long long)hctl.spieces + 1024;
+    }
+    // edges by source
+    const long long nb = (n2 + 1 + 1023) / 1024;
+    HGB_CUDA(eoff.alloc((size_t)(n2 + 1) * 4)); HGB_CUDA(eidx.alloc((size_t)std::max<long long>(ne, 1) * 4));
+    HGB_CUDA(tmp.alloc((size_t)std::max(nn, nb) * 4));
+    HGB_CUDA(cudaMemsetAsync(eoff.p, 0, (size_t)(n2 + 1) * 4, s));
+    kt.begin(s);
+    Level<D>::edge_csr(ed, ne, n2, eoff.template as<int>(), eidx.template as<int>(), tmp.template as<int>(), s);
+    kt.end(s, KT_OTHER, 5);
+    launches += 5;
+    HGB_CUDA(cudaGetLastError());
+    fx.eoff = eoff.template as<int>(); fx.eidx = eidx.template as<int>();
+    HGB_CUDA(woff.alloc(nn * 8)); HGB_CUDA(wcnt.alloc(nn * 4)); HGB_CUDA(woff2.alloc(nn * 8)); HGB_CUDA(wcnt2.alloc(nn * 4));
+    HGB_CUDA(dirty.alloc(nn * 4)); HGB_CUDA(dlist.alloc(nn * 4)); HGB_CUDA(chg.alloc(nn * 4)); HGB_CUDA(clst.alloc(nn * 4));
+    fx.woff = woff.template as<long long>(); fx.wcnt = wcnt.template as<int>();
+    fx.woff2 = woff2.template as<long long>(); fx.wcnt2 = wcnt2.template as<int>();
+    fx.dirty = dirty.template as<int>(); fx.dlist = dlist.template as<int>();
+    fx.changed = chg.template as<int>(); fx.clist = clst.template as<int>();
+    fx.ntiles = Level<D>::relax_tiles(blocks);
+    unsigned long long rounds = 0, npre = 0;
+    for (int K = 16;; K *= 2) {
+      fx.K = K;
+      HGB_CUDA(scratch.alloc((size_t)fx.ntiles * K * Z2 * 4));
+      fx.scratch = scratch.template as<int>();
+      long long wcap = std::max<long long>(1 << 16, 4 * n2);
+      HGB_CUDA(warena.alloc((size_t)wcap * Z2 * 4));
+      fx.warena = warena.template as<int>(); fx.wcap = wcap;
+      kt.begin(s);
+      Level<D>::gfp_init(fx, n2, dctl(), s);
+      kt.end(s, KT_OTHER);
+      ++launches;
+      HGB_CUDA(cudaMemsetAsync(&dctl()->walloc, 0, 8, s));
+      HGB_CUDA(cudaMemsetAsync(&dctl()->fed_over, 0, 4, s));
+      long long ndirty = n2, live_roots = 1;
+      while (ndirty > 0 && live_roots > 0) {
+        if (o.cancel && *o.cancel) return HORA_E_CANCELLED;
+        // room in the arena for this round's new values; otherwise copy the live values into a
+        // fresh arena sized for them and the round
+        if ((long long)hctl.walloc + ndirty * K > wcap) {
+          const long long cap2 = std::max<long long>(wcap, 4 * ndirty * (long long)K);
+          DBuf a2, na;
+          HGB_CUDA(a2.alloc((size_t)cap2 * Z2 * 4)); HGB_CUDA(na.alloc(8));
+          HGB_CUDA(cudaMemsetAsync(na.p, 0, 8, s));
+          kt.begin(s);
+          Level<D>::gfp_compact(fx, n2, a2.template as<int>(), na.template as<unsigned long long>(), s);
+          kt.end(s, KT_OTHER);
+          ++launches;
+          HGB_CUDA(cudaMemcpyAsync(&dctl()->walloc, na.p, 8, cudaMemcpyDeviceToDevice, s));
+          std::swap(warena.p, a2.p); std::swap(warena.bytes, a2.bytes);
+          wcap = cap2;
+          fx.warena = warena.template as<int>(); fx.wcap = wcap;
+          if ((rc = read_ctl())) return rc;
+          if ((long long)hctl.walloc + ndirty * K > wcap) {   // still short: grow once more
+            const long long cap3 = 2 * ((long long)hctl.walloc + ndirty * K);
+            DBuf a3, nb3;
+            HGB_CUDA(a3.alloc((size_t)cap3 * Z2 * 4)); HGB_CUDA(nb3.alloc(8));
+            HGB_CUDA(cudaMemsetAsync(nb3.p, 0, 8, s));
+            Level<D>::gfp_compact(fx, n2, a3.template as<int>(), nb3.template as<unsigned long long>(), s);
+            ++launches;
+            HGB_CUDA(cudaMemcpyAsync(&dctl()->walloc, nb3.p, 8, cudaMemcpyDeviceToDevice, s));
+            std::swap(warena.p, a3.p); std::swap(warena.bytes, a3.bytes);
+            wcap = cap3;
+            fx.warena = warena.template as<int>(); fx.wcap = wcap;
+          }
+        }
+        HGB_CUDA(cudaMemsetAsync(&dctl()->nchanged, 0, 8, s));
+        kt.begin(s);
+        Level<D>::gfp_relax(dn.views, st, ed, fx, dctl(), ndirty, blocks, s);
+        kt.end(s, KT_MERGE);
+        kt.begin(s);
+        Level<D>::gfp_round_end(ed, ne, n2, fx, S[1].nlevel.template as<int>(), dctl(), s);
+        kt.end(s, KT_OTHER, 3);
+        launches += 4;
+        ++rounds;
+        HGB_CUDA(cudaGetLastError());
+        if ((rc = read_ctl())) return rc;
+        if (hctl.err) { err = "device error in the federation sweep"; return (int)hctl.err; }
+        if (hctl.fed_over) break;
+        ndirty = (long long)hctl.ndirty;
+        live_roots = (long long)hctl.nroots_live;
+        if (rounds > 10000000ull) { err = "federation sweep did not settle"; return HORA_E_OVERFLOW; }
+      }
+      npre += hctl.npre;
+      if (!hctl.fed_over) break;
+      if (2 * K > kFedMax) { err = "a federation of the sweep outgrew its capacity"; return HORA_E_OVERFLOW; }
+      HGB_CUDA(cudaMemsetAsync(&dctl()->npre, 0, 8, s));
+    }
+    // instances found by the phase-1 witness keep their flag: they have no roots here
+    kt.begin(s);
+    Level<D>::gfp_verdict_fed(dn.views, st, n2, fx, is, s);
+    kt.end(s, KT_OTHER);
+    ++launches;
+    HGB_CUDA(cudaGetLastError());
+    if ((rc = read_ctl())) return rc;
+    gfp_iters = rounds;
+    pre_calls = npre;
     return HORA_OK;
   }
 
@@ -963,7 +1180,8 @@ int run_group(const std::vector<const HostNet*>& nets, std::vector<InstResult>& 
   const bool eg = !nets.empty() && nets[0]->kind == HORA_Q_EG;
   const bool leadsto = !nets.empty() && (nets[0]->kind == HORA_Q_LEADSTO || eg);
   // E[] psi has no reachability pass: its graph is rooted at the (restricted) initial state
-  int status = eg ? HORA_OK : E.run_levels(0, 0, cur, nf, level, nullptr);
+  int status = eg ? HORA_OK : E.leadsto_witness(cur, nf);
+  if (status == HORA_OK && !eg) status = E.run_levels(0, 0, cur, nf, level, nullptr);
   if (status == HORA_OK && leadsto) status = E.leadsto_phase2(cur);
   if (status != HORA_OK && status != HORA_E_CANCELLED) {
     E.finish(res, status, leadsto);

@@ -255,8 +255,11 @@ __device__ bool apply_abstain(const NetView& N, const Tile<D>& t, int (&r)[D], c
   return true;
 }
 
-// Enumerate the successors of (locs, ints, src). `emit(tl, ti, z)` is called for each non-empty
-// successor zone, in emission order. Returns false if a broadcast exceeded the device tables.
+// Enumerate the successors of (locs, ints, src). `emit(tl, ti, z, raw)` is called for each non-empty
+// successor zone, in emission order; `raw` numbers the transition among every candidate the
+// enumeration visits (integer guards and committed filter passed, zone not yet tested), so
+// find_trans() rebuilds its recipe from the discrete state alone. Returns false if a broadcast
+// exceeded the device tables.
 template <int D, class Emit>
 __device__ bool for_each_successor(const NetView& N, const Tile<D>& t, const int* locs, const int* ints,
                                    const int (&src)[D], int emode, Emit&& emit) {
@@ -264,6 +267,7 @@ __device__ bool for_each_successor(const NetView& N, const Tile<D>& t, const int
   int z[D];
   bool src_c, src_u;
   frozen_flags(N, locs, ints, src_c, src_u);
+  int raw = 0;
   // ---- local edges ----
   for (int p = 0; p < N.nprocs; ++p) {
     if (src_c && !committed_at(N, p, locs[p])) continue;
@@ -272,6 +276,7 @@ __device__ bool for_each_successor(const NetView& N, const Tile<D>& t, const int
       const int e = N.eloc[k];
       if (N.edge_chan[e] >= 0) continue;
       if (!int_ok(N, e, ints)) continue;
+      const int rw = raw++;
 #pragma unroll
       for (int j = 0; j < D; ++j) z[j] = src[j];
       if (!apply_cons(t, z, N.cons, N.edge_guard_off[e], N.edge_guard_off[e + 1])) continue;
@@ -282,7 +287,7 @@ __device__ bool for_each_successor(const NetView& N, const Tile<D>& t, const int
       apply_iupd(N, e, ti);
       if (!close_succ(N, t, z, tl, ti, emode)) continue;
       if (is_empty(t, z)) continue;
-      emit(tl, ti, z);
+      emit(tl, ti, z, rw);
     }
   }
   // ---- binary synchronisation ----
@@ -302,6 +307,7 @@ __device__ bool for_each_successor(const NetView& N, const Tile<D>& t, const int
           if (N.edge_chan[re] != ch || N.edge_dir[re] != -1) continue;
           if (src_c && !(i_comm || committed_at(N, j, locs[j]))) continue;
           if (!int_ok(N, re, ints)) continue;
+          const int rw = raw++;
 #pragma unroll
           for (int jj = 0; jj < D; ++jj) z[jj] = src[jj];
           if (!apply_cons(t, z, N.cons, N.edge_guard_off[se], N.edge_guard_off[se + 1])) continue;
@@ -316,7 +322,7 @@ __device__ bool for_each_successor(const NetView& N, const Tile<D>& t, const int
           apply_iupd(N, re, ti);
           if (!close_succ(N, t, z, tl, ti, emode)) continue;
           if (is_empty(t, z)) continue;
-          emit(tl, ti, z);
+          emit(tl, ti, z, rw);
         }
       }
     }
@@ -338,6 +344,7 @@ __device__ bool for_each_successor(const NetView& N, const Tile<D>& t, const int
         for (int q = 0; q < P.n; ++q)
           if (pick[q] < P.ne[q] && committed_at(N, P.proc[q], locs[P.proc[q]])) part_comm = true;
         if (!src_c || part_comm) {
+          const int rw = raw++;
 #pragma unroll
           for (int jj = 0; jj < D; ++jj) z[jj] = src[jj];
           bool ok = apply_cons(t, z, N.cons, N.edge_guard_off[se], N.edge_guard_off[se + 1]);
@@ -362,7 +369,7 @@ __device__ bool for_each_successor(const NetView& N, const Tile<D>& t, const int
               apply_iupd(N, re, ti);
               apply_resets(N, t, z, re);
             }
-            if (close_succ(N, t, z, tl, ti, emode) && !is_empty(t, z)) emit(tl, ti, z);
+            if (close_succ(N, t, z, tl, ti, emode) && !is_empty(t, z)) emit(tl, ti, z, rw);
           }
         }
         if (P.n == 0) break;
@@ -395,13 +402,18 @@ struct DlScratch {
   int spos[kMaxEscapes + 1];    // next constraint position of the split
 };
 
+// Collect the escape regions of (locs, ints, zone): every enabled transition's guard region of
+// the delay-closed zone Z (returned), pulled back through the target invariant (add_src,
+// deadlock.cpp:106-149), then let down unless the state is frozen, into S.w[0..nw). Returns 0 when
+// no valuation can deadlock (no concrete state, or one escape is all of Z), 1 when the escapes are
+// collected, -1 when there are more than kMaxEscapes.
 template <int D>
-__device__ int state_has_deadlock(const NetView& N, const Tile<D>& t, const int* locs, const int* ints,
-                                  const int (&zone)[D], DlScratch<D>& S) {
+__device__ int collect_escapes(const NetView& N, const Tile<D>& t, const int* locs, const int* ints,
+                               const int (&zone)[D], DlScratch<D>& S, int (&Z)[D], int& nw_out) {
   bool src_c, src_u;
   frozen_flags(N, locs, ints, src_c, src_u);
   const bool frozen = src_c || src_u;
-  int Z[D], g[D];
+  int g[D];
 #pragma unroll
   for (int j = 0; j < D; ++j) Z[j] = zone[j];
   if (!frozen) delay(t, Z);
@@ -532,11 +544,22 @@ __device__ int state_has_deadlock(const NetView& N, const Tile<D>& t, const int*
     }
     if (includes(t, a, Z)) return 0;
   }
-  if (nw == 0) return 1;
-  // depth-first subtraction: is Z ⊆ ∪ w ?
+  nw_out = nw;
+  return 1;
+}
+
+// Depth-first subtraction of zones W_0..W_{nw-1} (row i of W_k loaded by getw(k, rows)) from Z0:
+// Z0 \ W_i splits into the disjoint pieces Z0 ∧ c_1 ∧ .. ∧ c_{m-1} ∧ ¬c_m over W_i's tightening
+// constraints, each then taken against the later zones. `piece(R)` is called for every piece no W
+// reaches; the walk stops early when it returns false. S provides a stack of nw + 1 rows (stack,
+// sidx, spos). Returns the number of pieces reported (0: Z0 ⊆ ∪ W).
+template <int D, class Stk, class GetW, class Piece>
+__device__ int dfs_subtract(const Tile<D>& t, const int (&Z0)[D], Stk& S, int nw, GetW&& getw, Piece&& piece) {
+  int npieces = 0;
+  if (nw == 0) { ++npieces; piece(Z0); return npieces; }
   int sp = 0;
 #pragma unroll
-  for (int j = 0; j < D; ++j) S.stack[0][j] = Z[j];
+  for (int j = 0; j < D; ++j) S.stack[0][j] = Z0[j];
   S.sidx[0] = 0;
   S.spos[0] = -1;   // -1: escape index not yet settled for this piece
   while (sp >= 0) {
@@ -548,18 +571,21 @@ __device__ int state_has_deadlock(const NetView& N, const Tile<D>& t, const int*
       // first escape from wi on that meets the piece
       int W[D];
       for (; wi < nw; ++wi) {
-#pragma unroll
-        for (int j = 0; j < D; ++j) W[j] = S.w[wi][j];
+        getw(wi, W);
         if (intersects(t, R, W)) break;
       }
-      if (wi == nw) return 1;                   // a piece no escape reaches: deadlock
+      if (wi == nw) {                            // a piece no escape reaches
+        ++npieces;
+        if (!piece(R)) return npieces;
+        --sp;
+        continue;
+      }
       if (includes(t, W, R)) { --sp; continue; }  // piece covered
       S.sidx[sp] = wi;
       S.spos[sp] = 0;
     }
     int W[D];
-#pragma unroll
-    for (int j = 0; j < D; ++j) W[j] = S.w[wi][j];
+    getw(wi, W);
     // next tightening constraint (a, b) of W at linear position >= spos
     const int pos0 = S.spos[sp];
     unsigned long long m = 0;   // bit j of this lane's row: W[i][j] < R[i][j]
@@ -580,7 +606,7 @@ __device__ int state_has_deadlock(const NetView& N, const Tile<D>& t, const int*
     int Pc[D];
 #pragma unroll
     for (int j = 0; j < D; ++j) Pc[j] = R[j];
-    const bool piece = constrain(t, Pc, b, a, r_negate(wab));
+    const bool cut = constrain(t, Pc, b, a, r_negate(wab));
     const bool rest = constrain(t, R, a, b, wab);
     if (rest) {
 #pragma unroll
@@ -588,8 +614,12 @@ __device__ int state_has_deadlock(const NetView& N, const Tile<D>& t, const int*
     } else {
       S.spos[sp] = D * D;                        // nothing left of this piece after the child
     }
-    if (piece) {
-      if (wi + 1 >= nw) return 1;                // the piece escapes every region
+    if (cut) {
+      if (wi + 1 >= nw) {                        // the piece escapes every region
+        ++npieces;
+        if (!piece(Pc)) return npieces;
+        continue;
+      }
       ++sp;
 #pragma unroll
       for (int j = 0; j < D; ++j) S.stack[sp][j] = Pc[j];
@@ -597,7 +627,27 @@ __device__ int state_has_deadlock(const NetView& N, const Tile<D>& t, const int*
       S.spos[sp] = -1;
     }
   }
-  return 0;
+  return npieces;
+}
+
+// The escapes S.w[0..nw) subtracted from Z0 (dfs_subtract over the deadlock scratch).
+template <int D, class Piece>
+__device__ int subtract_escapes(const Tile<D>& t, const int (&Z0)[D], DlScratch<D>& S, int nw, Piece&& piece) {
+  return dfs_subtract(t, Z0, S, nw,
+                      [&](int k, int (&W)[D]) {
+#pragma unroll
+                        for (int j = 0; j < D; ++j) W[j] = S.w[k][j];
+                      },
+                      piece);
+}
+
+template <int D>
+__device__ int state_has_deadlock(const NetView& N, const Tile<D>& t, const int* locs, const int* ints,
+                                  const int (&zone)[D], DlScratch<D>& S) {
+  int Z[D], nw = 0;
+  const int r = collect_escapes(N, t, locs, ints, zone, S, Z, nw);
+  if (r <= 0) return r;
+  return subtract_escapes(t, Z, S, nw, [](const int (&)[D]) { return false; }) > 0 ? 1 : 0;
 }
 
 // ---------------------------------------------------------------------------------------------

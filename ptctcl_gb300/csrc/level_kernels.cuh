@@ -30,6 +30,33 @@ struct Edges {                // zone-graph edges (leads-to graph mode)
   int* dst;
   int* ord;                   // emission ordinal of the successor the edge came from
   long long cap;
+  int* raw;                   // its transition index (for_each_successor's raw), for the predecessor
+};
+// The federation-valued greatest fixpoint of the subsumed leads-to graph. W[v] (a union of zones
+// inside node v's zone) lives in an append-only arena: wcnt[v] zones from warena + woff[v] * D*D,
+// or the node's own zone when woff[v] < 0 (the seed is not copied). A round reads the current values
+// and writes changed ones to woff2/wcnt2, committed after the round (Jacobi order).
+struct Fix {
+  const int* eoff;            // [nnodes+1] out-edges of each node (CSR over eidx)
+  const int* eidx;            // edge ids grouped by source
+  int* swhole;                // [nnodes] 1: every valuation of the zone may end a run
+  int* shead;                 // [nnodes] first piece of the node's stop set, -1 when none
+  int* snext;                 // [scap] next piece of the same node
+  int* spiece;                // [scap * D*D] stop-set pieces
+  long long scap;
+  long long* woff;
+  int* wcnt;
+  long long* woff2;
+  int* wcnt2;
+  int* warena;                // [wcap * D*D]
+  long long wcap;
+  int* dirty;                 // [nnodes] flag: relax in the next round
+  int* dlist;                 // [nnodes] nodes to relax this round
+  int* changed;               // [nnodes] flag: W changed this round
+  int* clist;                 // [nnodes] nodes whose W changed this round
+  int* scratch;               // [ntiles * K * D*D] one federation under construction per tile
+  int K;                      // zones a federation may hold
+  long long ntiles;
 };
 struct HeavyKeys {            // per key merged block-wide (index j of Succ::heavy)
   int* n;                     // survivors
@@ -43,6 +70,8 @@ struct Succ {                 // successors of the current level
   unsigned long long* key;    // hash key
   int* parent;                // frontier index of the source
   int* ord;                   // emission ordinal within the source
+  int* raw;                   // transition index within the source (for_each_successor's raw)
+  int* flag;                  // inclusion store: 1 when the survivor is stored
   int* slot;                  // hash slot after the probe, -1 when dropped
   int* rank;                  // position among the slot's pending survivors (arrival order)
   int* zone;                  // [cap * D*D]
@@ -122,6 +151,34 @@ struct Level {
                        cudaStream_t s);
   static void gfp_verdict(const NetView* nets, Store st, long long nnodes, const int* W, InstState is, Ctl* ctl,
                           cudaStream_t s);
+  // Subsumed leads-to graph (store 1): a successor is covered by a stored zone of its key that
+  // contains it; per level the maximal survivors of each key are stored (incl_*), and every
+  // successor records one edge to its covering node.
+  static void incl_probe(const NetView* nets, InstState is, Succ sc, Store st, Ctl* ctl, long long nsucc, int blocks,
+                         cudaStream_t s);
+  static void incl_group(Succ sc, Store st, Ctl* ctl, long long nsucc, long long ntouched, cudaStream_t s);
+  static void incl_keep(Succ sc, Store st, Ctl* ctl, long long nsurv, int blocks, cudaStream_t s);
+  static void incl_store(const NetView* nets, InstState is, Succ sc, Store st, Front out, Ctl* ctl, long long nsurv,
+                         int level, int blocks, cudaStream_t s);
+  static void incl_lists(const NetView* nets, InstState is, Succ sc, Store st, Ctl* ctl, long long ntouched,
+                         cudaStream_t s);
+  static void incl_cover(Succ sc, Store st, Ctl* ctl, long long nsurv, int blocks, cudaStream_t s);
+  static void incl_edges(Succ sc, Front fr, Edges ed, Ctl* ctl, long long nsucc, cudaStream_t s);
+  // Stop sets of nodes [n0, n1) as federations; with `witness`, an instance whose node holds a stop
+  // valuation of its p-part cut to !q is found (the early witness on phase-1 nodes, whose zones
+  // are read from st; fx.swhole/shead are then not written).
+  static void stop_fed(const NetView* nets, InstState is, Store st, long long n0, long long n1, const int* nodes,
+                       Fix fx, Ctl* ctl, int witness, int blocks, cudaStream_t s);
+  // CSR of the edges by source: eoff (nnodes+1, zeroed by the caller) and eidx; tmp holds nnodes ints.
+  static void edge_csr(Edges ed, long long nedges, long long nnodes, int* eoff, int* eidx, int* tmp, cudaStream_t s);
+  static void gfp_init(Fix fx, long long nnodes, Ctl* ctl, cudaStream_t s);
+  static void gfp_relax(const NetView* nets, Store st, Edges ed, Fix fx, Ctl* ctl, long long ndirty, int blocks,
+                        cudaStream_t s);
+  static void gfp_round_end(Edges ed, long long nedges, long long nnodes, Fix fx, const int* nlevel, Ctl* ctl,
+                            cudaStream_t s);
+  static void gfp_compact(Fix fx, long long nnodes, int* narena, unsigned long long* nalloc, cudaStream_t s);
+  static void gfp_verdict_fed(const NetView* nets, Store st, long long nnodes, Fix fx, InstState is, cudaStream_t s);
+  static long long relax_tiles(int blocks);
   // Host-buffer successor pipeline (hora_gb_expand): states given as frontier + node zones.
   static void expand_plain(const NetView* nets, const int* locs, const int* ints, const int* zones, int n,
                            int emode, unsigned long long* okey, int* osrc, int* oord, int* olocs, int* oints,

@@ -120,7 +120,7 @@ __global__ void __launch_bounds__(kBlock) k_expand(const NetView* nets, InstStat
     const int emode = is.emode[inst];
     int ord = 0;
     bool hit = false;
-    auto emit = [&](const int* tl, const int* ti, const int (&z)[D]) {
+    auto emit = [&](const int* tl, const int* ti, const int (&z)[D], int raw) {
       unsigned long long idx = 0;
       if (t.i == 0) idx = atomicAdd(&ctl->nsucc, 1ull);
       idx = t.shfl64(idx, 0);
@@ -130,6 +130,7 @@ __global__ void __launch_bounds__(kBlock) k_expand(const NetView* nets, InstStat
           sc.key[idx] = key_encode(N, tl, ti) | ((unsigned long long)inst << N.inst_shift);
           sc.parent[idx] = (int)f;
           sc.ord[idx] = ord;
+          sc.raw[idx] = raw;
           sc.okh[idx] = hk;
           sc.okl[idx] = ((unsigned long long)(unsigned)fr.rank[f] << 32) | (unsigned)ord;
         }
@@ -143,7 +144,7 @@ __global__ void __launch_bounds__(kBlock) k_expand(const NetView* nets, InstStat
     if (roots) {
       // leads-to roots: the p-part of a phase-1 zone, cut to !q
       if (apply_cons(t, src, N.p_clk, 0, N.p_nclk) && avoid_cut(N, t, src, locs, ints) && !is_empty(t, src))
-        emit(locs, ints, src);
+        emit(locs, ints, src, -1);
     } else {
       ok = for_each_successor(N, t, locs, ints, src, emode, emit);
     }
@@ -1207,7 +1208,7 @@ __global__ void __launch_bounds__(kBlock) k_stop(const NetView* nets, Store st, 
       NetView U = N;
       U.av_on = 0;
       int cnt = 0;
-      const bool ok = for_each_successor(U, t, locs, ints, z, 1, [&](const int*, const int*, const int (&)[D]) { ++cnt; });
+      const bool ok = for_each_successor(U, t, locs, ints, z, 1, [&](const int*, const int*, const int (&)[D], int) { ++cnt; });
       if (!ok) { if (t.i == 0) atomicMax(&ctl->err, 4u); continue; }
       if (cnt == 0 || time_diverges(N, t, locs, ints, z, false)) r = 1;
       else {
@@ -1267,7 +1268,7 @@ __global__ void __launch_bounds__(kBlock) k_expand_plain(const NetView* nets, co
     int src[D];
     load_rows(t, src, zones + f * D * D);
     int ord = 0;
-    const bool ok = for_each_successor(N, t, locs, ints, src, emode, [&](const int* tl, const int* ti, const int (&z)[D]) {
+    const bool ok = for_each_successor(N, t, locs, ints, src, emode, [&](const int* tl, const int* ti, const int (&z)[D], int) {
       unsigned long long idx = 0;
       if (t.i == 0) idx = atomicAdd(&ctl->nsucc, 1ull);
       idx = t.shfl64(idx, 0);
@@ -1437,3 +1438,5 @@ void Level<D>::has_deadlock(const NetView* nets, const int* locs, const int* int
 }
 
 }  // namespace hgb
+
+#include "subsumed_impl.cuh"
