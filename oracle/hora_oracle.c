@@ -547,9 +547,9 @@ static void xpush(Parts* P, int i, int j, int32_t raw) {
   P->xcons[3 * P->nx] = i; P->xcons[3 * P->nx + 1] = j; P->xcons[3 * P->nx + 2] = raw;
   P->nx++;
 }
-/* One broadcast-enumeration scratch block, reused across calls (the oracle is single-threaded). */
+/* One broadcast-enumeration scratch block per thread, reused across calls. */
 static Parts* parts_scratch(void) {
-  static Parts* P = NULL;
+  static _Thread_local Parts* P = NULL;   /* one per thread: the multi-core port expands in parallel */
   if (!P) P = (Parts*)calloc(1, sizeof(Parts));
   return P;
 }
@@ -988,18 +988,26 @@ static void store_grow(Store* S) {
   free(S->skey); free(S->shead); free(S->stouch);
   S->skey = nk; S->shead = nh; S->stouch = nt; S->smask = nmask;
 }
+/* Room for `extra` more nodes without reallocation (the multi-core port reserves a level's worth
+ * before inserting in parallel). */
+static void store_reserve(Store* S, int extra) {
+  if (S->nn + extra <= S->capn) return;
+  int c = S->capn ? S->capn : 1024;
+  while (S->nn + extra > c) c *= 2;
+  S->capn = c;
+  S->zones = (int32_t*)realloc(S->zones, sizeof(int32_t) * S->d2 * (size_t)S->capn);
+  S->next = (int*)realloc(S->next, sizeof(int) * S->capn);
+  S->level = (int*)realloc(S->level, sizeof(int) * S->capn);
+  S->dead = (char*)realloc(S->dead, S->capn);
+}
+/* Node ids and the live count are updated atomically: in the multi-core port, threads insert into
+ * disjoint keys of one store (capacity reserved beforehand). */
 static int store_node(Store* S, const int32_t* z, int level, int next) {
-  if (S->nn == S->capn) {
-    S->capn = S->capn ? S->capn * 2 : 1024;
-    S->zones = (int32_t*)realloc(S->zones, sizeof(int32_t) * S->d2 * (size_t)S->capn);
-    S->next = (int*)realloc(S->next, sizeof(int) * S->capn);
-    S->level = (int*)realloc(S->level, sizeof(int) * S->capn);
-    S->dead = (char*)realloc(S->dead, S->capn);
-  }
-  const int id = S->nn++;
+  if (S->nn == S->capn) store_reserve(S, 1);
+  const int id = __atomic_fetch_add(&S->nn, 1, __ATOMIC_RELAXED);
   memcpy(S->zones + (size_t)id * S->d2, z, sizeof(int32_t) * S->d2);
   S->next[id] = next; S->level[id] = level; S->dead[id] = 0;
-  S->nlive++;
+  __atomic_fetch_add(&S->nlive, 1, __ATOMIC_RELAXED);
   return id;
 }
 #define MERGE_SCAN 32   /* kMergeScan, include/hora/detail/engine_config.hpp:52 */
@@ -1028,7 +1036,7 @@ static int store_add(Store* S, uint64_t k, int32_t* z, int level, int dim, const
   /* (3): retire stored zones simulated by z */
   int w = 0;
   for (int t = 0; t < nlv; ++t) {
-    if (orc_dbm_alu_le(S->zones + (size_t)live[t] * d2, z, dim, Ls, Us)) { S->dead[live[t]] = 1; S->nlive--; }
+    if (orc_dbm_alu_le(S->zones + (size_t)live[t] * d2, z, dim, Ls, Us)) { S->dead[live[t]] = 1; __atomic_fetch_sub(&S->nlive, 1, __ATOMIC_RELAXED); }
     else live[w++] = live[t];
   }
   nlv = w;
@@ -1037,7 +1045,7 @@ static int store_add(Store* S, uint64_t k, int32_t* z, int level, int dim, const
     merged = 0;
     for (int t = 0; t < nlv && t < MERGE_SCAN; ++t) {
       if (orc_dbm_try_union(z, S->zones + (size_t)live[t] * d2, dim)) {
-        S->dead[live[t]] = 1; S->nlive--;
+        S->dead[live[t]] = 1; __atomic_fetch_sub(&S->nlive, 1, __ATOMIC_RELAXED);
         memmove(live + t, live + t + 1, sizeof(int) * (nlv - t - 1));
         nlv--;
         merged = 1;
@@ -1137,6 +1145,15 @@ static int goal_hit(const Model* m, const Goal* g, const int32_t* locs, const in
 
 static double g_time_limit = 0.0;   /* seconds; 0 = none. Bounds a CPU-baseline sample. */
 void orc_set_time_limit(double seconds) { g_time_limit = seconds; }
+static int g_threads = 1;           /* host threads of the reachability route (orc_set_threads) */
+int32_t orc_set_threads(int32_t n) {
+#ifdef _OPENMP
+  g_threads = n < 1 ? 1 : n;
+#else
+  g_threads = 1;
+#endif
+  return g_threads;
+}
 
 static double now_s(void) {
   struct timespec ts; clock_gettime(CLOCK_MONOTONIC, &ts);
@@ -1149,6 +1166,98 @@ static double now_s(void) {
 static int over_time(double t0, int i) {
   return g_time_limit > 0 && (i & 255) == 255 && now_s() - t0 > g_time_limit;
 }
+
+#ifdef _OPENMP
+#include <omp.h>
+/* One BFS level of run_reach on g_threads host threads, with the sequential level's results: the
+ * frontier is expanded in contiguous chunks (a thread's successors keep frontier order), the goal is
+ * tested on every successor, new keys are entered in successor order, and each thread then inserts
+ * the successors of its own share of the keys in successor order -- the passed-store folds of one
+ * key never interleave with another's, so every key sees the same insertion sequence as in the
+ * sequential loop (the reference's omp backend likewise inserts under per-stripe locks,
+ * src/reachability/engine.cpp:2045-2201). Node ids differ; the stored sets and the next frontier
+ * (ordered by key, then chain order) do not. Returns 1 when the goal is found or the time limit
+ * passed, else 0. */
+static int reach_level_par(Model* m, const Goal* goal, Store* S, const FItem* fr, int nfr, int level, int emode,
+                           const uint8_t* qmask, const int32_t* Lq, const int32_t* Uq, double t0, hora_stats* S0,
+                           int* found, SuccBuf* TB) {
+  const int T = g_threads, dim = m->dim, d2 = dim * dim, np = m->n->nprocs, ni = m->n->nints;
+  for (int t = 0; t < T; ++t) TB[t].n = 0;
+  int timed = 0;
+  S0->explored += nfr;
+#pragma omp parallel num_threads(T)
+  {
+    const int t = omp_get_thread_num();
+    const int f0 = (int)((long)nfr * t / T), f1 = (int)((long)nfr * (t + 1) / T);
+    int32_t l[64], i[64];
+    for (int f = f0; f < f1; ++f) {
+      if (((f - f0) & 255) == 255 && g_time_limit > 0 && now_s() - t0 > g_time_limit) { timed = 1; break; }
+      key_decode(m, fr[f].key, l, i);
+      successors(m, l, i, S->zones + (size_t)fr[f].node * d2, m->L, m->U, qmask, emode, sb_emit, &TB[t]);
+    }
+  }
+  long total = 0;
+  for (int t = 0; t < T; ++t) total += TB[t].n;
+  S0->generated += (uint64_t)total;
+  if (timed) { S0->status = HORA_E_TIMEOUT; return 1; }
+  int hit = 0;
+#pragma omp parallel num_threads(T) reduction(|:hit)
+  {
+    const SuccBuf* b = &TB[omp_get_thread_num()];
+    for (int j = 0; j < b->n && !hit; ++j)
+      if (goal_hit(m, goal, b->locs + (size_t)j * np, b->ints + (size_t)j * ni, b->zones + (size_t)j * d2)) hit = 1;
+  }
+  if (hit) { *found = 1; return 1; }
+  /* successor g -> (buffer, position); keys; new keys entered in successor order */
+  uint64_t* K = (uint64_t*)malloc(sizeof(uint64_t) * (total ? total : 1));
+  const int32_t** Z = (const int32_t**)malloc(sizeof(int32_t*) * (total ? total : 1));
+  const int32_t** Lp = (const int32_t**)malloc(sizeof(int32_t*) * (total ? total : 1));
+  {
+    long g = 0;
+    for (int t = 0; t < T; ++t)
+      for (int j = 0; j < TB[t].n; ++j, ++g) {
+        Z[g] = TB[t].zones + (size_t)j * d2;
+        Lp[g] = TB[t].locs + (size_t)j * np;
+        K[g] = key_encode(m, Lp[g], TB[t].ints + (size_t)j * ni);
+      }
+  }
+  for (long g = 0; g < total; ++g) {
+    if ((uint64_t)(S->nkeys + 1) * 10 >= (S->smask + 1) * 7) store_grow(S);
+    const uint64_t si = slot_of(S, K[g]);
+    if (S->shead[si] == -2) { S->skey[si] = K[g]; S->shead[si] = -1; S->nkeys++; }
+  }
+  if ((uint64_t)(S->nkeys + 1) * 10 >= (S->smask + 1) * 7) store_grow(S);
+  store_reserve(S, (int)total);
+  uint64_t probes = 0;
+#pragma omp parallel num_threads(T) reduction(+:probes)
+  {
+    const int t = omp_get_thread_num();
+    int32_t Ls[64], Us[64];
+    int64_t pr = 0;
+    for (long g = 0; g < total; ++g) {
+      if ((int)((mix64(K[g]) >> 33) % (uint64_t)T) != t) continue;
+      const int32_t* sl = Lp[g];
+      for (int c = 1; c < dim; ++c) {
+        int32_t lv = ORC_ALU_NEG_INF, uv = ORC_ALU_NEG_INF;
+        for (int p = 0; p < np; ++p) {
+          const int gl = m->loc_base[p] + sl[p];
+          lv = imax(lv, m->Lloc[gl * dim + c]); uv = imax(uv, m->Uloc[gl * dim + c]);
+        }
+        Ls[c] = imax(lv, Lq[c]); Us[c] = imax(uv, Uq[c]);
+      }
+      Ls[0] = Us[0] = 0;
+      int32_t zc[64 * 64];
+      memcpy(zc, Z[g], sizeof(int32_t) * d2);
+      const int id = store_add(S, K[g], zc, level, dim, Ls, Us, &pr);
+      if (id >= 0) S->stouch[slot_of(S, K[g])] = level;
+    }
+    probes += (uint64_t)pr;
+  }
+  S0->probes += probes;
+  free(K); free(Z); free(Lp);
+  return 0;
+}
+#endif
 
 /* The engine shared by E<> and deadlock. `collapse` selects the a_M bounds of deadlock_reachable
  * (engine.cpp:2363-2405, the HORA_DL_MODE=m route). */
@@ -1197,6 +1306,7 @@ static int32_t run_reach(const hora_net_desc* net, const Goal* goal, int collaps
   store_init(&S, d2);
   SuccBuf B = {0};
   B.np = np; B.ni = ni; B.d2 = d2;
+  SuccBuf* TB = NULL;   /* per-thread successor buffers of the multi-core port */
   FItem* fr = NULL; int nfr = 0, capfr = 0;
   int32_t Ls[64], Us[64];
   if (!close_succ_zone(&m, locs, ints, zone, qmask, m.L, m.U, emode) || orc_dbm_empty(zone, dim)) {
@@ -1212,6 +1322,21 @@ static int32_t run_reach(const hora_net_desc* net, const Goal* goal, int collaps
   }
   int level = 0;
   while (nfr > 0) {
+#ifdef _OPENMP
+    if (g_threads > 1) {
+      if (!TB) {   /* one successor buffer per thread, for this network's shapes */
+        TB = (SuccBuf*)calloc((size_t)g_threads, sizeof(SuccBuf));
+        for (int t = 0; t < g_threads; ++t) { TB[t].np = np; TB[t].ni = ni; TB[t].d2 = d2; }
+      }
+      const int lr = reach_level_par(&m, goal, &S, fr, nfr, ++level, emode, qmask, Lq, Uq, t0, &S0, &found, TB);
+      if (lr) { S0.levels = level; goto done; }     /* goal found or time limit */
+      nfr = collect_frontier(&S, level, &fr, &capfr);
+      if (g_time_limit > 0 && now_s() - t0 > g_time_limit) { S0.levels = level; S0.status = HORA_E_TIMEOUT; goto done; }
+      if (emode == 0 && S.nkeys && (double)S.nlive >= 4.0 * (double)S.nkeys) { emode = 1; S0.extrapolating = 1; }
+      S0.levels = level;
+      continue;
+    }
+#endif
     S0.explored += nfr;
     ++level;
     B.n = 0;
@@ -1264,6 +1389,10 @@ done:
   S0.probes += 0;
   if (st) *st = S0;
   free(fr); free(B.locs); free(B.ints); free(B.zones); free(B.raw); free(B.parent);
+  for (int t = 0; TB && t < g_threads; ++t) {
+    free(TB[t].locs); free(TB[t].ints); free(TB[t].zones); free(TB[t].raw); free(TB[t].parent);
+  }
+  free(TB);
   store_free(&S);
   model_free(&m);
   return HORA_OK;

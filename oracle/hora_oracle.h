@@ -80,6 +80,9 @@ int32_t orc_eg_successors(const hora_net_desc* net, const hora_pred_desc* psi, c
  * then reports status HORA_E_TIMEOUT with the counters reached so far. Used to bound the CPU
  * baseline sample. */
 void orc_set_time_limit(double seconds);
+/* Host threads of the E<> / deadlock reachability route (1: the sequential loop). Returns the count
+ * in effect (1 when the oracle was built without OpenMP). Results do not depend on it. */
+int32_t orc_set_threads(int32_t n);
 
 /* Initial symbolic state of the reach route (initial_symbolic_state,
  * src/reachability/engine.cpp:1322-1335): fills locs[nprocs], ints[nints], zone[dim*dim]. Returns 0

@@ -62,11 +62,18 @@ def lib():
         L.orc_initial_state.restype = I32
         L.orc_set_time_limit.argtypes = [ctypes.c_double]
         L.orc_set_time_limit.restype = None
+        L.orc_set_threads.argtypes = [I32]
+        L.orc_set_threads.restype = I32
     return _lib
 
 
 def set_time_limit(seconds: float):
     lib().orc_set_time_limit(float(seconds))
+
+
+def set_threads(n: int) -> int:
+    """Host threads of the E<> / deadlock reachability route; returns the count in effect."""
+    return int(lib().orc_set_threads(int(n)))
 
 
 def _p(a: np.ndarray):

@@ -870,7 +870,8 @@ struct Engine {
     long long nf = (long long)hctl.nfront;
     int level = 0;
     // the reported level count is the graph's: per instance, its last level with a frontier
-    for (int q = 0; q < ninst; ++q) levels[q] = 0;
+    for (int q = 0; q < ninst; ++q)
+      if (!h_done[q]) levels[q] = 0;   // an instance decided in phase 1 keeps its level count
     if ((rc = run_levels(1, eg ? 1 : 2, cur, nf, level, S[0].nzone.template as<int>()))) return rc;
     if (!eg) return fed_sweep();
     // stop flags and the sweep
@@ -1030,7 +1031,7 @@ struct Engine {
         if (hctl.fed_over) break;
         ndirty = (long long)hctl.ndirty;
         live_roots = (long long)hctl.nroots_live;
-        if (rounds > 10000000ull) { err = "federation sweep did not settle"; return HORA_E_OVERFLOW; }
+        if (rounds > 1000000ull) { err = "federation sweep did not settle"; return HORA_E_OVERFLOW; }
       }
       npre += hctl.npre;
       if (!hctl.fed_over) break;
