@@ -13,9 +13,11 @@ The passed store of one query (hundreds of MB at this size) exceeds L2; L2 is al
 256 MB write between steps. Under torchrun each rank runs an independent replica on its own GPU
 (the single-query path does not shard) and value sums successors over ranks / max time.
 
---impl reference times the CPU restatement of the reference's algorithm (oracle/, single
-threaded: the reference's deadlock route is sequential code) on a bounded sample of the same
-workload, on this machine's host cores.
+--impl reference times the CPU restatement of the reference's algorithm (oracle/) on the same
+workload on every host core: the route it restates (deadlock_reachable's a_M route) runs in the
+reference through reach_engine with the OpenMP backend (src/reachability/engine.cpp:2367,2408-2409),
+so the port expands each BFS level on all host threads and inserts per key in the sequential order.
+Each step is one whole query, bounded in time (a step that hits the bound reports its partial rate).
 """
 from __future__ import annotations
 
@@ -34,7 +36,7 @@ sys.path.insert(0, ROOT)
 WORKLOAD_CONFIG = 2
 WORKLOAD_SEED = int(os.environ.get("HORA_BENCH_SEED", "2483"))
 # The port stops within a few hundred items of this limit (it checks its clock inside BFS levels).
-CPU_SAMPLE_SECONDS = 15.0
+CPU_SAMPLE_SECONDS = 90.0
 METRIC = "zone successors/s"
 UNIT = "successors/s"
 
@@ -93,8 +95,12 @@ def measured_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
-def cpu_baseline(net, seconds: float):
+def cpu_baseline(net, seconds: float, threads: int = 0):
+    """The oracle port of the query on `threads` host threads (default: every core), bounded by
+    `seconds`; the successors/s of the whole query, or of the levels reached when the bound hits."""
     from oracle import pyoracle
+    threads = threads or os.cpu_count() or 1
+    used = pyoracle.set_threads(threads)
     pyoracle.set_time_limit(seconds)
     try:
         t = time.perf_counter()
@@ -102,30 +108,67 @@ def cpu_baseline(net, seconds: float):
         dt = time.perf_counter() - t
     finally:
         pyoracle.set_time_limit(0)
-    return {"value": st["generated"] / dt if dt > 0 else 0.0, "unit": UNIT, "cores": 1, "kind": "port",
+        pyoracle.set_threads(1)
+    return {"value": st["generated"] / dt if dt > 0 else 0.0, "unit": UNIT, "cores": used, "kind": "port",
+            "whole_query": not st["status"], "seconds": dt,
             "sample": f"{'BFS levels 1-' + str(st['levels']) + ' (the last in part)' if st['status'] else 'whole query'}"
-                      f" of the workload, {st['generated']} successors in {dt:.1f} s"}
+                      f" of the workload on {used} host threads, {st['generated']} successors in {dt:.1f} s"}
+
+
+def family_bytes(st, dim: int) -> dict:
+    """Algorithmic bytes each kernel family of one query must move at least (int32 zones): expand
+    reads every frontier zone and writes every successor; the deadlock goal reads every successor;
+    the probe reads every successor, the column 0 of every stored zone it tests and the whole of
+    those column 0 does not decide; the merge reads its survivors and the live zones of the keys it
+    folds them into, and writes the zones it stores."""
+    z, c0 = 4 * dim * dim, 4 * dim
+    return {"expand": z * (st.explored + st.generated), "deadlock": z * st.generated,
+            "probe": z * st.generated + c0 * st.probes + z * st.probe_full,
+            "merge": z * (st.merge_surv + st.merge_live + st.nodes)}
+
+
+def roofline(st, dim: int, peaks: dict, peak_kind: str) -> dict:
+    """HBM roofline of the dominant kernel family (CUDA-event time on the engine's stream): its
+    algorithmic bytes per launch over its mean launch time, against the measured copy bandwidth;
+    every family's figure beside it."""
+    kern = st.kernels
+    tot = sum(x["seconds"] for x in kern.values())
+    fb = family_bytes(st, dim)
+    per = {}
+    for k, b in fb.items():
+        sec, calls = kern[k]["seconds"], max(1, kern[k]["calls"])
+        ach = (b / calls) / (sec / calls) / 1e9 if sec > 0 else 0.0
+        per[k] = {"gbs": round(ach, 2), "bytes": int(b), "seconds": round(sec, 6), "launches": kern[k]["calls"]}
+    dom = max(fb, key=lambda k: kern[k]["seconds"])
+    peak = peaks.get("hbm_gbs", 1.0)
+    return {"bound": "hbm", "kernel": dom, "achieved": per[dom]["gbs"], "peak": peak, "unit": "GB/s",
+            "frac": per[dom]["gbs"] / peak, "traffic": None, "peak_source": peak_kind,
+            "bytes_per_launch": per[dom]["bytes"] / max(1, kern[dom]["calls"]),
+            "path_gbs": round(sum(fb.values()) / max(1e-12, st.device_seconds) / 1e9, 2),
+            "families": per,
+            "kernel_time_share": {k: round(v["seconds"] / max(1e-12, tot), 4) for k, v in kern.items()}}
 
 
 def run_reference(args, rank, world):
     if rank != 0:
         return
     net, kind, p, q = workload(args.seed)
-    vals, samples = [], []
-    per_step = max(2.0, min(CPU_SAMPLE_SECONDS, 150.0 / max(1, args.steps)))   # whole run within minutes
+    vals, samples, cores, whole = [], [], 1, True
+    per_step = max(5.0, min(CPU_SAMPLE_SECONDS, 240.0 / max(1, args.steps)))   # whole run within minutes
     for _ in range(args.warmup):
         cpu_baseline(net, min(2.0, per_step))
     t_all = time.perf_counter()
     for _ in range(args.steps):
         b = cpu_baseline(net, per_step)
         vals.append(b["value"]); samples.append(b["sample"])
+        cores, whole = b["cores"], whole and b["whole_query"]
     dt = time.perf_counter() - t_all
     v = statistics.mean(vals) if vals else 0.0
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * dt / max(1, args.steps), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-            "config": {"workload": workload_name(args.seed), "sample": samples[-1] if samples else ""},
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
+            "config": {"workload": workload_name(args.seed)},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "whole_query": whole,
                              "sample": samples[-1] if samples else ""},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -450,38 +493,20 @@ def main():
         return
     s0 = stats[-1]
     peaks, peak_kind = measured_peaks()
-    # dominant kernel family and its algorithmic bytes per launch (9x9 int32 zones)
-    d2 = net.dim * net.dim * 4
     line = {
         "metric": METRIC, "value": gen_all / dev_max if dev_max > 0 else 0.0, "unit": UNIT,
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * total_max / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-        "config": {"workload": workload_name(args.seed),
-                   "stored_zones": s0.stored, "successors_per_query": s0.generated, "levels": s0.levels,
-                   "verdict_deadlock_reachable": bool(verdict), "l2": "flushed (256 MB write) between steps; "
-                   "passed store exceeds L2", "parallelism": f"replicas x{world}"},
+        "config": {"workload": workload_name(args.seed)},
+        "query": {"stored_zones": s0.stored, "successors_per_query": s0.generated, "levels": s0.levels,
+                  "verdict_deadlock_reachable": bool(verdict), "l2": "flushed (256 MB write) between steps; "
+                  "passed store exceeds L2", "parallelism": f"replicas x{world}"},
         "e2e": {"value": gen_all / wall_max if wall_max > 0 else 0.0, "unit": UNIT,
                 "h2d_bytes_per_step": int(s0.h2d_bytes), "d2h_bytes_per_step": int(s0.d2h_bytes)},
         "gpu_launches": int(sum(s.kernel_launches for s in stats)),
     }
-    kern = s0.kernels
-    dom = max(kern, key=lambda k: kern[k]["seconds"])
-    kd = kern[dom]
-    calls = max(1, kd["calls"])
-    per_launch_s = kd["seconds"] / calls
-    if dom == "expand":
-        algo = d2 * (s0.explored + s0.generated) / calls
-    elif dom in ("probe", "merge"):
-        algo = d2 * (s0.generated + s0.probes) / calls
-    else:
-        algo = d2 * s0.generated / calls
-    ach = algo / per_launch_s / 1e9 if per_launch_s > 0 else 0.0
-    line["roofline"] = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peaks.get("hbm_gbs"),
-                        "unit": "GB/s", "frac": ach / peaks.get("hbm_gbs", 1.0), "traffic": None,
-                        "peak_source": peak_kind,
-                        "kernel_time_share": {k: round(v["seconds"] / max(1e-12, sum(x["seconds"] for x in kern.values())), 4)
-                                              for k, v in kern.items()}}
+    line["roofline"] = roofline(s0, net.dim, peaks, peak_kind)
     cs = clock_summary(clk, local)
     if cs:
         line["clocks"] = cs

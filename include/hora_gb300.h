@@ -41,7 +41,7 @@
 extern "C" {
 #endif
 
-#define HORA_GB_ABI_VERSION 1
+#define HORA_GB_ABI_VERSION 2
 
 #if defined(__GNUC__)
 #define HORA_GB_API __attribute__((visibility("default")))
@@ -148,7 +148,7 @@ typedef struct hora_stats {
   uint64_t stored;       /* live zones in the passed store at the end */
   uint64_t keys;         /* distinct discrete states in the passed store */
   uint64_t levels;       /* BFS levels run */
-  uint64_t probes;       /* stored zones read by the subsumption probe (algorithmic bytes) */
+  uint64_t probes;       /* stored zones the subsumption probe tested (their column 0 read) */
   uint64_t pre_calls;    /* exact_predecessor evaluations in the backward sweep */
   uint64_t gfp_iters;    /* sweeps of the backward fixpoint */
   uint64_t kernel_launches;
@@ -162,6 +162,14 @@ typedef struct hora_stats {
   uint64_t kernel_calls[6];
   uint64_t h2d_bytes;    /* host-to-device bytes moved by the call (descriptor, counters) */
   uint64_t d2h_bytes;    /* device-to-host bytes moved by the call (counters, verdict) */
+  /* work of the passed store, for the per-kernel algorithmic bytes (single-query calls):
+   * probes (above) counts the stored zones whose column 0 the probe read; of those, probe_full were
+   * read whole; merge_surv survivors were folded against merge_live live zones of their keys; nodes
+   * zones were written to the store */
+  uint64_t probe_full;
+  uint64_t merge_surv;
+  uint64_t merge_live;
+  uint64_t nodes;
 } hora_stats;
 
 /* ---- errors and device ---------------------------------------------------------------------- */

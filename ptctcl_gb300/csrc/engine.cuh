@@ -90,7 +90,7 @@ struct Ctl {
   unsigned long long nkeys;      // distinct keys holding at least one stored zone
   unsigned long long nslots;     // occupied hash slots
   unsigned long long nedges;     // graph edges recorded (leads-to graph mode)
-  unsigned long long probes;     // stored zones read by the probe and the merge
+  unsigned long long probes;     // stored zones the probe tested (their column 0 read)
   unsigned long long arena_alloc;  // key-list arena in use
   long long nlive;               // live passed-store zones
   unsigned int err;              // HORA_E_* raised on the device (table full, escape overflow)
@@ -104,6 +104,8 @@ struct Ctl {
   unsigned long long nroots_live; // roots whose W is not yet empty
   unsigned int fed_over;         // a federation outgrew its slots (the sweep restarts with more)
   unsigned int stop_over;        // the stop-set arena overflowed (the pass re-runs with more)
+  unsigned long long probe_full; // stored zones the probe read whole (column 0 did not decide)
+  unsigned long long merge_live; // live zones of the keys the merge folded into, before each merge
 };
 constexpr unsigned long long kCtlChunkBytes = 10 * 8 + 2 * 4;
 

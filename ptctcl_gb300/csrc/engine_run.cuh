@@ -609,6 +609,7 @@ struct Engine {
     return HORA_OK;
   }
   unsigned long long gen_total = 0, exp_total = 0;   // successors / expanded states so far (fan-out)
+  unsigned long long merge_surv = 0;                 // survivors handed to the merge (store 0)
   double last_fan = 0;                               // successors per frontier state, recent levels
 
   // The group's store may hold about store_budget_bytes: an instance past a quarter of it stops,
@@ -776,6 +777,7 @@ struct Engine {
     if ((rc = read_ctl())) return rc;
     if (hctl.err) { err = "device error in probe"; return (int)hctl.err; }
     const long long nsurv = (long long)hctl.nsurv, ntouched = (long long)hctl.ntouched;
+    merge_surv += (unsigned long long)nsurv;
     if (ntouched > hv_cap) {   // per-key arrays of the grouping pass
       long long c = std::max<long long>(hv_cap, 1 << 12);
       while (c < ntouched) c *= 2;
@@ -1154,6 +1156,10 @@ struct Engine {
       r.st.keys = h_nkeys[k];
       r.st.levels = levels[k];
       r.st.probes = ninst == 1 ? hctl.probes : 0;
+      r.st.probe_full = ninst == 1 ? hctl.probe_full : 0;
+      r.st.merge_surv = ninst == 1 ? merge_surv : 0;
+      r.st.merge_live = ninst == 1 ? hctl.merge_live : 0;
+      r.st.nodes = ninst == 1 ? hctl.nnodes : 0;
       r.st.pre_calls = pre_calls;
       r.st.gfp_iters = gfp_iters;
       r.st.kernel_launches = launches;

@@ -192,7 +192,7 @@ __global__ void __launch_bounds__(kBlock, 8) k_probe(const NetView* nets, InstSt
     inserted = t.shfl(inserted, 0);
     if (slot < 0) { if (t.i == 0) { atomicMax(&ctl->err, 4u); sc.slot[s] = -1; } continue; }
     bool killed = false;
-    unsigned long long nprobe = 0;
+    unsigned long long nprobe = 0, nfull = 0;
     if (!inserted) {
       // the lanes take the key's live zones in turn, newest first, each deciding a whole a_LU test
       int Lall[D];
@@ -211,13 +211,15 @@ __global__ void __launch_bounds__(kBlock, 8) k_probe(const NetView* nets, InstSt
           ++nprobe;
           const int m = __ldg(lst + k);
           // most failing tests fail on column 0: decide those from the stored zone's column copy
-          mine = !alu_col0_witness<D>(zc0, st.ncol0 + (long long)m * D, Lall) &&
-                 alu_le_lane<D>(zs, st.nzone + (long long)m * D * D, Lall, U);
+          const bool col0_pass = !alu_col0_witness<D>(zc0, st.ncol0 + (long long)m * D, Lall);
+          nfull += col0_pass;
+          mine = col0_pass && alu_le_lane<D>(zs, st.nzone + (long long)m * D * D, Lall, U);
         }
         killed = t.any(mine);
       }
     }
     if (nprobe) atomicAdd(&ctl->probes, nprobe);
+    if (nfull) atomicAdd(&ctl->probe_full, nfull);
     if (t.i == 0) {
       if (killed) {
         sc.slot[s] = -1;
@@ -279,6 +281,7 @@ static __global__ void k_seg_alloc(Succ sc, Store st, Ctl* ctl, long long ntouch
     const unsigned n = st.pend[s];
     st.pend_base[s] = (unsigned)atomicAdd(&ctl->seg_alloc, (unsigned long long)n);
     const int a = st.klive[s];
+    atomicAdd(&ctl->merge_live, (unsigned long long)a);
     if (n >= 2 && (long long)n * ((long long)a + n) >= kHeavyMerge) {
       const unsigned long long j = atomicAdd(&ctl->nheavy, 1ull);
       sc.heavy[j] = s;

@@ -44,11 +44,18 @@ class ReachStats:
     status: int = 0
     h2d_bytes: int = 0
     d2h_bytes: int = 0
+    probe_full: int = 0     # stored zones the probe read whole
+    merge_surv: int = 0     # survivors folded by the merge
+    merge_live: int = 0     # live zones of the merged keys before each merge
+    nodes: int = 0          # zones written to the passed store
+    pre_calls: int = 0      # exact predecessors of the backward sweep
+    gfp_iters: int = 0      # rounds of the backward sweep
     kernels: dict = field(default_factory=dict)   # family -> {"seconds", "calls"}
 
     def fill(self, st: Stats):
         for k in ("explored", "generated", "expanded", "stored", "keys", "levels", "probes",
-                  "kernel_launches", "seconds", "device_seconds", "status", "h2d_bytes", "d2h_bytes"):
+                  "kernel_launches", "seconds", "device_seconds", "status", "h2d_bytes", "d2h_bytes",
+                  "probe_full", "merge_surv", "merge_live", "nodes", "pre_calls", "gfp_iters"):
             setattr(self, k, getattr(st, k))
         self.extrapolating = bool(st.extrapolating)
         self.kernels = {n: {"seconds": st.kernel_seconds[i], "calls": int(st.kernel_calls[i])}

@@ -220,7 +220,8 @@ class Stats(ctypes.Structure):
                 ("device_seconds", ctypes.c_double), ("extrapolating", ctypes.c_int32),
                 ("status", ctypes.c_int32), ("kernel_seconds", ctypes.c_double * 6),
                 ("kernel_calls", ctypes.c_uint64 * 6), ("h2d_bytes", ctypes.c_uint64),
-                ("d2h_bytes", ctypes.c_uint64)]
+                ("d2h_bytes", ctypes.c_uint64), ("probe_full", ctypes.c_uint64),
+                ("merge_surv", ctypes.c_uint64), ("merge_live", ctypes.c_uint64), ("nodes", ctypes.c_uint64)]
     KERNELS = ("expand", "probe", "deadlock", "group", "merge", "other")
 
     def as_dict(self):

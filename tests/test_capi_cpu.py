@@ -27,7 +27,7 @@ def test_library_exports_every_declared_symbol():
     assert syms >= set(capi.EXPORTS)
     for s in syms:
         assert hasattr(lib, s), s
-    assert lib.hora_gb_abi_version() == 1
+    assert lib.hora_gb_abi_version() == 2
 
 
 def test_invalid_and_unsupported_inputs_are_rejected_without_a_device():
