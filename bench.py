@@ -195,6 +195,19 @@ def percentile(xs, q):
     return xs[k]
 
 
+def percentiles_all(finished_times, total: int, budget: float) -> dict:
+    """p50/p99 time to verdict over ALL `total` instances, the unfinished ones counted as taking
+    longer than the budget: a percentile that falls among them is reported as None with its flag."""
+    xs = sorted(finished_times) + [float("inf")] * max(0, total - len(finished_times))
+    out = {}
+    for q in (50, 99):
+        v = percentile(xs, q)
+        out[f"p{q}_time_to_verdict_s"] = None if v is None or v == float("inf") else v
+        out[f"p{q}_beyond_budget"] = v == float("inf")
+    out["budget_s"] = budget
+    return out
+
+
 def _cpu_batch_worker(wid, nworkers, instances, budget, out, go, t_go):
     """One process of the CPU sample: once `go` is set, instances wid, wid + n, ... of config 4
     through the oracle port until t_go + budget (time.time() based; the port checks its clock
@@ -337,12 +350,60 @@ def batched_compare(instances: int, budget: float, cpu_budget: float = 0.0) -> d
     return {"workload": f"config4: {instances} seeded networks (clocks U[2,16], automata "
             f"U[2,10], locations U[4,12], c in [0,40], query mix 60/30/10), {budget:.0f} s budget per form",
             "batched": {"value": b_gen / bdt, "unit": UNIT, "seconds": bdt, "verdicts": len(b_done),
-                        "p50_time_to_verdict_s": percentile(lat, 50), "p99_time_to_verdict_s": percentile(lat, 99)},
+                        **percentiles_all(lat, instances, budget)},
             "plain_one_at_a_time": {"value": plain_gen / pdt, "unit": UNIT, "seconds": pdt, "verdicts": plain_done,
-                                    "p50_time_to_verdict_s": percentile(plain_lat, 50),
-                                    "p99_time_to_verdict_s": percentile(plain_lat, 99)},
+                                    **percentiles_all(plain_lat, instances, budget)},
             "speedup_successors_per_s": (b_gen / bdt) / max(1e-9, plain_gen / pdt),
             "verdicts_compared": len(both), "verdicts_agree": all(plain_v[k] == bv[k] for k in both), **cpu}
+
+
+def like_for_like(config: int, seeds, cap: float, plain_budget: float) -> dict:
+    """Batched vs plain on the same instances, both to completion. The plain form runs the seeded
+    instances one at a time (each cancelled after `cap` seconds, the whole pass after `plain_budget`);
+    the instances it finished form the set S. The batched form then runs exactly S in one call. Both
+    forms did the same work, so the ratio of their successors/s is the ratio of their times; time to
+    verdict is over all of S (nothing censored), and every verdict is compared."""
+    import ctypes
+    from ptctcl_gb300 import engine
+    from ptctcl_gb300.generator import config_instance
+    done_items, plain_lat, plain_v, plain_gen = [], [], [], 0
+    tried, t0 = 0, time.perf_counter()
+    plain_busy = 0.0
+    for sd in seeds:
+        if time.perf_counter() - t0 > plain_budget:
+            break
+        it = config_instance(config, sd)
+        cancel = ctypes.c_int32(0)
+        tm = threading.Timer(cap, lambda c=cancel: setattr(c, "value", 1))
+        tm.start()
+        t = time.perf_counter()
+        v, st = engine.batch_run([it], cancel=cancel)
+        dt = time.perf_counter() - t
+        tm.cancel()
+        tried += 1
+        if v[0] >= 0 and st[0]["status"] == 0:
+            done_items.append(it)
+            plain_v.append(v[0])
+            plain_gen += st[0]["generated"]
+            plain_busy += dt
+            plain_lat.append(plain_busy)   # time to verdict when S alone runs one after another
+    if not done_items:
+        return {"instances": 0}
+    batch = engine.BatchInput(done_items)
+    t = time.perf_counter()
+    bv, bst = engine.batch_run(batch)
+    bdt = time.perf_counter() - t
+    b_gen = sum(s_["generated"] for s_ in bst)
+    lat = [s_["seconds"] for s_ in bst]
+    return {"instances": len(done_items), "tried": tried, "per_instance_cap_s": cap,
+            "plain_one_at_a_time": {"value": plain_gen / plain_busy, "unit": UNIT, "seconds": plain_busy,
+                                    "p50_time_to_verdict_s": percentile(plain_lat, 50),
+                                    "p99_time_to_verdict_s": percentile(plain_lat, 99)},
+            "batched": {"value": b_gen / bdt, "unit": UNIT, "seconds": bdt,
+                        "p50_time_to_verdict_s": percentile(lat, 50), "p99_time_to_verdict_s": percentile(lat, 99)},
+            "speedup": (b_gen / bdt) / max(1e-12, plain_gen / plain_busy),
+            "same_successors": b_gen == plain_gen,
+            "verdicts_compared": len(bv), "verdicts_agree": list(bv) == plain_v}
 
 
 def run_batched(args):
@@ -351,9 +412,13 @@ def run_batched(args):
     print(json.dumps(line), flush=True)
 
 
-def run_serving(args):
-    """Config 5: Poisson arrivals of config-3-distribution requests, continuous admission by a
-    device-memory budget; p50/p99 time-to-verdict and sustained successors/s."""
+def serving_run(rate: float, duration: float, drain: float, budget_gb: float, inflight: int,
+                serve_config: int = 3) -> dict:
+    """Config 5: Poisson arrivals of requests drawn from the config-3 distribution at `rate` per
+    second for `duration` seconds, admitted continuously by the server's device-memory pool; after
+    `drain` more seconds the server is destroyed (cancelling what still runs). Time to verdict runs
+    from submission to result; percentiles are over every offered request, those without a verdict
+    counted as beyond the run."""
     import ctypes
     import random
     from ptctcl_gb300 import capi
@@ -361,51 +426,62 @@ def run_serving(args):
     from ptctcl_gb300.generator import config_instance
     lib = capi.load()
     srv = ctypes.c_void_p()
-    capi.check(lib.hora_gb_server_create(int(args.budget_gb * (1 << 30)), args.inflight, ctypes.byref(srv)), "server")
+    capi.check(lib.hora_gb_server_create(int(budget_gb * (1 << 30)), inflight, ctypes.byref(srv)), "server")
     rng = random.Random(5)
+    # up to 2000 distinct requests, offered in turn (descriptors built before the clock)
+    reqs = [config_instance(serve_config, 100000 + k) for k in range(min(2000, int(rate * duration * 1.5) + 16))]
+    descs = [(NetArrays(n), QueryArrays(kd, p, q)) for n, kd, p, q in reqs]
     t0 = time.perf_counter()
-    tickets, keep, k = [], [], 0
-    next_t = 0.0
+    tickets, k, next_t = [], 0, 0.0
     while True:
         now = time.perf_counter() - t0
-        if now >= args.duration:
+        if now >= duration:
             break
         if now >= next_t:
-            net, kind, p, q = config_instance(args.serve_config, 100000 + k)
-            na, qa = NetArrays(net), QueryArrays(kind, p, q)
-            keep.append((na, qa))
+            na, qa = descs[k % len(descs)]
             tk = ctypes.c_int64(0)
-            rc = lib.hora_gb_server_submit(srv, ctypes.addressof(na.desc), ctypes.addressof(qa.desc), ctypes.byref(tk))
-            if rc == capi.OK:
+            if lib.hora_gb_server_submit(srv, ctypes.addressof(na.desc), ctypes.addressof(qa.desc),
+                                         ctypes.byref(tk)) == capi.OK:
                 tickets.append(tk.value)
             k += 1
-            next_t += rng.expovariate(args.rate)
+            next_t += rng.expovariate(rate)
         else:
             time.sleep(min(0.002, next_t - now))
     submitted = time.perf_counter() - t0
-    # drain
-    lat, gen, done, stopped = [], 0, 0, 0
+    pending, lat, gen, done, stopped = set(tickets), [], 0, 0, 0
     active = ctypes.c_int32(1)
-    while active.value > 0 and time.perf_counter() - t0 < args.duration + args.drain:
+    while pending and time.perf_counter() - t0 < duration + drain:
         lib.hora_gb_server_step(srv, ctypes.byref(active))
+        for tk in list(pending):
+            d, v, st = ctypes.c_int32(0), ctypes.c_int32(0), Stats()
+            if lib.hora_gb_server_poll(srv, tk, ctypes.byref(d), ctypes.byref(v), ctypes.byref(st)) != capi.OK:
+                pending.discard(tk)
+                continue
+            if d.value:
+                pending.discard(tk)
+                gen += st.generated
+                if st.status == capi.OK:
+                    done += 1
+                    lat.append(st.seconds)
+                else:
+                    stopped += 1   # needed more than the pool had left (HORA_E_BUDGET) or failed
     total = time.perf_counter() - t0
-    for tk in tickets:
-        d, v, st = ctypes.c_int32(0), ctypes.c_int32(0), Stats()
-        lib.hora_gb_server_poll(srv, tk, ctypes.byref(d), ctypes.byref(v), ctypes.byref(st))
-        if d.value:
-            gen += st.generated
-            if st.status == capi.OK:
-                done += 1
-                lat.append(st.seconds)
-            else:
-                stopped += 1   # outgrew its memory share (HORA_E_BUDGET) or failed
     lib.hora_gb_server_destroy(srv)
-    line = {"metric": METRIC, "workload": f"config{args.serve_config} requests, Poisson {args.rate}/s for "
-            f"{args.duration:.0f} s, budget {args.budget_gb} GB, {args.inflight} in flight",
-            "offered": len(tickets), "verdicts": done, "stopped_over_budget": stopped, "value": gen / total,
-            "unit": UNIT,
-            "p50_time_to_verdict_s": percentile(lat, 50), "p99_time_to_verdict_s": percentile(lat, 99),
-            "seconds": total, "submit_seconds": submitted}
+    xs = sorted(lat) + [float("inf")] * (len(tickets) - len(lat))
+    p50, p99 = percentile(xs, 50), percentile(xs, 99)
+    return {"workload": f"config{serve_config} requests, Poisson {rate:g}/s for {duration:.0f} s, "
+            f"pool {budget_gb:g} GB, {inflight} in flight, {drain:.0f} s drain",
+            "offered": len(tickets), "verdicts": done, "stopped_over_budget": stopped,
+            "unfinished": len(pending), "value": gen / total, "unit": UNIT,
+            "p50_time_to_verdict_s": None if p50 in (None, float("inf")) else p50,
+            "p99_time_to_verdict_s": None if p99 in (None, float("inf")) else p99,
+            "p99_beyond_run": p99 == float("inf"), "seconds": total, "submit_seconds": submitted}
+
+
+def run_serving(args):
+    rates = [float(r) for r in args.rates.split(",")] if args.rates else [args.rate]
+    line = {"metric": METRIC, "serving": [serving_run(r, args.duration, args.drain, args.budget_gb, args.inflight,
+                                                      args.serve_config) for r in rates]}
     print(json.dumps(line), flush=True)
 
 
@@ -421,6 +497,9 @@ def main():
     ap.add_argument("--instances", type=int, default=4096)
     ap.add_argument("--budget", type=float, default=60.0)
     ap.add_argument("--rate", type=float, default=100.0)
+    ap.add_argument("--rates", default="", help="serving: comma-separated offered loads (req/s)")
+    ap.add_argument("--serving-seconds", type=float, default=15.0,
+                    help="seconds of arrivals per load of the serving sweep added to the default line (0: leave it out)")
     ap.add_argument("--duration", type=float, default=60.0)
     ap.add_argument("--drain", type=float, default=120.0)
     ap.add_argument("--budget-gb", type=float, default=64.0)
@@ -515,6 +594,12 @@ def main():
     if args.batched_budget > 0 and world == 1:
         line["batched"] = batched_compare(args.instances, args.batched_budget,
                                           0.0 if args.no_cpu_baseline else args.batched_budget)
+        line["batched_like_for_like"] = {
+            "config4": like_for_like(4, range(args.instances), 2.0, args.batched_budget),
+            "config3": like_for_like(3, range(100000, 100000 + args.instances), 2.0, args.batched_budget)}
+    if args.serving_seconds > 0 and world == 1:
+        line["serving"] = [serving_run(r, args.serving_seconds, 2 * args.serving_seconds, args.budget_gb,
+                                       args.inflight) for r in (100.0, 1000.0)]
     print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()

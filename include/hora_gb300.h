@@ -287,19 +287,26 @@ HORA_GB_API int32_t hora_gb_batch_run(int32_t n, const hora_net_desc* nets, cons
 
 typedef struct hora_server hora_server;
 
-/* budget_bytes: device memory the passed/waiting stores of admitted requests may hold together;
- * max_inflight: instances interleaved on the device at once. */
+/* budget_bytes: device memory the passed/waiting stores of the admitted requests may hold together
+ * (a pool); max_inflight: requests on the device at once, each on its own worker thread and stream.
+ * A request is admitted, in arrival order, when a slot is free and the pool can hold its initial store
+ * reservation; while it runs its stores stay resident across BFS levels and grow by taking more from
+ * the pool; a request whose store needs more than the pool has left stops with status HORA_E_BUDGET. */
 HORA_GB_API int32_t hora_gb_server_create(uint64_t budget_bytes, int32_t max_inflight, hora_server** out);
-/* Queue a request; the descriptors are copied. *ticket identifies it. A request whose own store
- * estimate exceeds the whole budget is rejected with HORA_E_BUDGET. */
+/* Queue a request; the descriptors are copied. *ticket identifies it. A request whose initial
+ * reservation exceeds the whole pool is rejected with HORA_E_BUDGET. */
 HORA_GB_API int32_t hora_gb_server_submit(hora_server* s, const hora_net_desc* net, const hora_query_desc* q,
                               int64_t* ticket);
-/* Advance the device by one interleaved step over every admitted request, admitting queued ones as
- * slots and budget free up. *active receives the number still queued or running. */
+/* The worker threads admit and run requests on their own; this waits up to 1 ms for progress and sets
+ * *active to the number of requests still queued or running. */
 HORA_GB_API int32_t hora_gb_server_step(hora_server* s, int32_t* active);
-/* Fetch a finished request: *done = 1 and verdict/stats filled once it has finished. */
+/* Fetch a request's result: *done = 0 while it is queued or running; once it has finished, *done = 1
+ * with verdict and stats filled (stats.seconds = submission to result), and the result is released:
+ * a later poll of the same ticket returns HORA_E_INVALID. */
 HORA_GB_API int32_t hora_gb_server_poll(hora_server* s, int64_t ticket, int32_t* done, int32_t* verdict,
                             hora_stats* stats);
+/* Cancels the running requests at their next BFS level, waits for the workers and frees the server;
+ * results not yet polled are dropped. */
 HORA_GB_API int32_t hora_gb_server_destroy(hora_server* s);
 
 #ifdef __cplusplus

@@ -156,6 +156,7 @@ struct Engine {
 
   Engine(const std::vector<const HostNet*>& n, const RunOptions& opt, std::string& e) : nets(n), o(opt), err(e) {}
   ~Engine() {
+    if (o.pool && pool_taken) o.pool->give(pool_taken);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
     if (s) cudaStreamDestroy(s);
@@ -436,7 +437,20 @@ struct Engine {
   static constexpr long long kNodeBytes = Z2 * 4 + D * 4 + 20;
   // Nodes the store budget allows (unbounded without a budget).
   long long budget_nodes() const {
-    return o.store_budget_bytes ? (long long)(o.store_budget_bytes / 2 / kNodeBytes) : (1LL << 40);
+    return o.store_budget_bytes ? (long long)((o.store_budget_bytes + pool_taken) / 2 / kNodeBytes) : (1LL << 40);
+  }
+  uint64_t pool_taken = 0;   // bytes this run took from the server's pool beyond its admission share
+  // With a pool, room for `need` nodes is taken from it (at least doubling what the run holds); false
+  // when the pool cannot provide it.
+  bool grow_budget(long long need) {
+    if (!o.pool || !o.store_budget_bytes) return false;
+    const uint64_t want_total = (uint64_t)need * 2 * kNodeBytes * 2;
+    const uint64_t have = o.store_budget_bytes + pool_taken;
+    if (want_total <= have) return true;
+    const uint64_t more = std::max<uint64_t>(want_total - have, have);
+    if (o.pool->take(more)) { pool_taken += more; return true; }
+    if (o.pool->take(want_total - have)) { pool_taken += want_total - have; return true; }
+    return false;
   }
   int ensure_nodes(int k, long long extra) {
     StoreBufs<D>& B = S[k];
@@ -612,9 +626,10 @@ struct Engine {
   unsigned long long merge_surv = 0;                 // survivors handed to the merge (store 0)
   double last_fan = 0;                               // successors per frontier state, recent levels
 
-  // The group's store may hold about store_budget_bytes: an instance past a quarter of it stops,
-  // and once the store is past it every instance still running stops (status HORA_E_BUDGET, no
-  // verdict). The store grows by at most one level past the check.
+  // The group's store may hold about store_budget_bytes (plus what it took from a server's pool): in a
+  // group of several instances one past a quarter of it stops, and once the store is past it every
+  // instance still running stops (status HORA_E_BUDGET, no verdict). The store grows by at most one
+  // level past the check.
   int enforce_budget(int mode) {
     const size_t ni4 = (size_t)ninst * 4, ni8 = (size_t)ninst * 8;
     InstState is = istate();
@@ -622,12 +637,13 @@ struct Engine {
       HGB_CUDA(cudaMemcpyAsync(h_nlive.data(), is.nlive, ni8, cudaMemcpyDeviceToHost, s));
       HGB_CUDA(cudaStreamSynchronize(s));
     }
+    if (o.pool && (double)hctl.nnodes > (double)budget_nodes()) grow_budget((long long)hctl.nnodes);
     const double allowed = (double)budget_nodes();
     const bool all = (double)hctl.nnodes > allowed;
     bool changed = false;
     for (int q = 0; q < ninst; ++q) {
       if (h_done[q]) continue;
-      if (all || (double)h_nlive[q] > allowed / 4) { h_done[q] = 1; h_budget[q] = 1; changed = true; }
+      if (all || (ninst > 1 && (double)h_nlive[q] > allowed / 4)) { h_done[q] = 1; h_budget[q] = 1; changed = true; }
     }
     if (changed) {
       HGB_CUDA(cudaMemcpyAsync(is.done, h_done.data(), ni4, cudaMemcpyHostToDevice, s));
@@ -788,7 +804,8 @@ struct Engine {
     }
     // ---- room for the new nodes, their key lists and the next frontier; a chunk that would take
     // the store past its budget stops its instances instead (HORA_E_BUDGET)
-    if (o.store_budget_bytes && (long long)hctl.nnodes + nsurv > budget_nodes()) {
+    if (o.store_budget_bytes && (long long)hctl.nnodes + nsurv > budget_nodes() &&
+        !grow_budget((long long)hctl.nnodes + nsurv)) {
       bool changed = false;
       for (int q = i0; q < i1; ++q)
         if (!h_done[q]) { h_done[q] = 1; h_budget[q] = 1; changed = true; }

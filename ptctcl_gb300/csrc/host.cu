@@ -722,7 +722,7 @@ namespace hgb {
 // The batched form with an explicit store budget for the whole call (0: three quarters of the free
 // device memory), shared by the concurrent groups.
 int32_t run_batch(int32_t n, const hora_net_desc* nets, const hora_query_desc* queries, int32_t* verdicts,
-                  hora_stats* stats, const volatile int32_t* cancel, size_t store_budget) {
+                  hora_stats* stats, const volatile int32_t* cancel, size_t store_budget, BudgetPool* pool) {
   g_last_error.clear();
   if (n < 0 || (n > 0 && (!nets || !queries || !verdicts))) return fail(HORA_E_INVALID, "bad arguments");
   int rc = ensure_device();
@@ -782,6 +782,7 @@ int32_t run_batch(int32_t n, const hora_net_desc* nets, const hora_query_desc* q
   RunOptions o = run_options(cancel);
   o.t_call = std::chrono::steady_clock::now();
   o.has_t_call = true;
+  o.pool = pool;
   int nthreads = std::max(1, std::min(ng, 32));
   if (const char* e = std::getenv("HORA_GB_GROUP_THREADS")) nthreads = std::max(1, std::min(ng, std::atoi(e)));
   {
@@ -803,10 +804,10 @@ int32_t run_batch(int32_t n, const hora_net_desc* nets, const hora_query_desc* q
       grc[g] = dispatch_group(groups[g].first / 4, v, gres[g], o, gerr[g]);
     }
   };
-  std::vector<std::thread> pool;
-  for (int i = 1; i < nthreads; ++i) pool.emplace_back(worker);
+  std::vector<std::thread> workers;
+  for (int i = 1; i < nthreads; ++i) workers.emplace_back(worker);
   worker();
-  for (auto& t : pool) t.join();
+  for (auto& t : workers) t.join();
   int first_err = HORA_OK;
   bool cancelled = false;
   for (int g = 0; g < ng; ++g) {

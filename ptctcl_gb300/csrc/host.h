@@ -1,5 +1,6 @@
 // host.h -- host-side model compilation and the per-dimension engine entry points.
 #pragma once
+#include <atomic>
 #include <cstdint>
 #include <chrono>
 #include <string>
@@ -9,6 +10,21 @@
 #include "engine.cuh"
 
 namespace hgb {
+
+// Device memory shared by the requests of a server: each request's store starts from the reservation
+// it was admitted with and grows level by level while the pool has room (BudgetPool::take).
+struct BudgetPool {
+  std::atomic<uint64_t> used{0};
+  uint64_t cap = 0;
+  bool take(uint64_t b) {
+    uint64_t u = used.load();
+    while (u + b <= cap)
+      if (used.compare_exchange_weak(u, u + b)) return true;
+    return false;
+  }
+  void give(uint64_t b) { used.fetch_sub(b); }
+};
+
 
 // One (network, query) instance compiled for the device: the descriptor's arrays re-indexed, the
 // static analyses of src/model/network.cpp applied, and the query's constants folded in.
@@ -64,7 +80,8 @@ struct OwnedNet {
 // The batched form (hora_gb_batch_run) with an explicit store budget for the whole call, in bytes
 // (0: three quarters of the free device memory).
 int32_t run_batch(int32_t n, const hora_net_desc* nets, const hora_query_desc* queries, int32_t* verdicts,
-                  hora_stats* stats, const volatile int32_t* cancel, size_t store_budget);
+                  hora_stats* stats, const volatile int32_t* cancel, size_t store_budget,
+                  BudgetPool* pool = nullptr);
 
 // Result of one instance.
 struct InstResult {
@@ -87,6 +104,8 @@ struct RunOptions {
   size_t succ_cap0 = 1 << 16; // initial successor-buffer capacity
   size_t succ_budget_bytes = size_t(8) << 30;  // a level's successors beyond this run in instance chunks
   size_t store_budget_bytes = 0;  // 0: unbounded; else instances stop with HORA_E_BUDGET past it
+  BudgetPool* pool = nullptr;     // when set, the store may grow past store_budget_bytes by taking
+                                  // more from the pool (returned when the run ends)
   bool has_t_call = false;    // per-instance times count from t_call (the batch call) when set
   std::chrono::steady_clock::time_point t_call{};
   Trace* trace = nullptr;     // E[] psi, one instance: fill with a witness when it holds

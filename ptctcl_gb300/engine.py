@@ -315,10 +315,11 @@ def batch_run(items, cancel: Optional[ctypes.c_int32] = None):
 
 
 class Server:
-    """The serving form (hora_gb_server_*): requests are queued, admitted while their estimated
-    store footprint fits `budget_bytes` and at most `max_inflight` run at once, and run on the
-    device in batches by background workers; `poll` returns (verdict, stats dict) once a ticket is
-    done, else None."""
+    """The serving form (hora_gb_server_*): requests are queued and admitted in arrival order while
+    at most `max_inflight` run and the `budget_bytes` pool holds their initial store reservation;
+    each runs on its own worker and stream, its stores growing from the pool level by level.
+    `poll` returns (verdict, stats dict) once a ticket is done (the result is then released), else
+    None; closing cancels what still runs."""
 
     def __init__(self, budget_bytes: int, max_inflight: int):
         self._lib = capi.load()

@@ -1,7 +1,8 @@
 """The batched and serving forms on the GPU: every request's verdict and counts are the same
 whether it runs alone, in a batch, or through the request queue mixed with other requests; a
 cancelled batch reports its unfinished instances as cancelled; the queue rejects a request whose
-store estimate exceeds the whole memory budget."""
+initial reservation exceeds the whole pool, grows a running request's store from the pool, reports
+a result once, and cancels running requests when it is destroyed."""
 import ctypes
 
 import pytest
@@ -87,3 +88,48 @@ def test_batch_in_instance_chunks_matches_whole_levels():
         assert r.returncode == 0, r.stderr[-2000:]
         out[budget] = json.loads(r.stdout.strip().splitlines()[-1])
     assert out[""] == out["1"]
+
+
+def test_server_result_reported_once():
+    net, kind, p, q = config_instance(4, C4_SMALL[0])
+    with engine.Server(budget_bytes=1 << 30, max_inflight=2) as srv:
+        t = srv.submit(net, kind, p, q)
+        srv.drain(timeout=120)
+        assert srv.poll(t) is not None
+        with pytest.raises(capi.HoraError) as ei:
+            srv.poll(t)                       # released after the first report
+        assert ei.value.code == capi.E_INVALID
+
+
+def test_server_store_grows_from_the_pool():
+    """A request whose store outgrows its initial reservation takes more from the pool and gets the
+    verdict and counts of the batched form; with a pool barely larger than one reservation it stops
+    with HORA_E_BUDGET instead."""
+    net, kind, p, q = config_instance(2, 23)          # about 2e5 successors
+    (bv,), (bst,) = engine.batch_run([(net, kind, p, q)])
+    with engine.Server(budget_bytes=2 << 30, max_inflight=16) as srv:   # reservation: 2 GB / 64
+        t = srv.submit(net, kind, p, q)
+        srv.drain(timeout=300)
+        v, st = srv.poll(t)
+    assert st["status"] == capi.OK and v == bv
+    for c in COUNTS:
+        assert st[c] == bst[c], c
+    big, bk, bp, bq = config_instance(2, 2483)        # 1.45M stored zones, far past 64 Ki
+    d = big.dim
+    floor = (1 << 16) * (d * d * 4 + 32) * 2
+    with engine.Server(budget_bytes=floor + floor // 2, max_inflight=1) as srv:
+        t = srv.submit(big, bk, bp, bq)
+        srv.drain(timeout=300)
+        v, st = srv.poll(t)
+    assert st["status"] == capi.E_BUDGET and v == -1
+
+
+def test_server_destroy_cancels_running_requests():
+    import time
+    big, bk, bp, bq = config_instance(3, 0)            # phase 1 alone holds millions of zones
+    srv = engine.Server(budget_bytes=64 << 30, max_inflight=2)
+    srv.submit(big, bk, bp, bq)
+    time.sleep(0.3)
+    t = time.perf_counter()
+    srv.close()
+    assert time.perf_counter() - t < 10.0
