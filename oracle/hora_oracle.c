@@ -1586,8 +1586,28 @@ static int32_t liveness_core(const hora_net_desc* net, const hora_pred_desc* p, 
   }
   int level = 0;
   int timed_out = 0;
+#ifdef _OPENMP
+  SuccBuf* TB = NULL;   /* per-thread successor buffers of the multi-core phase 1 */
+  const hora_pred_desc never = {0, NULL, 0, NULL, 0, NULL, 1};
+  const Goal nogoal = {0, &never};
+#endif
   while (nfr > 0) {
     if (g_time_limit > 0 && now_s() - t0 > g_time_limit) { timed_out = 1; break; }
+#ifdef _OPENMP
+    if (g_threads > 1 && !psi) {   /* the same level on every host thread (reach_level_par) */
+      if (!TB) {
+        TB = (SuccBuf*)calloc((size_t)g_threads, sizeof(SuccBuf));
+        for (int t = 0; t < g_threads; ++t) { TB[t].np = np; TB[t].ni = ni; TB[t].d2 = d2; }
+      }
+      int unused = 0;
+      const uint64_t pr0 = S0.probes;   /* phase 1's probes are not reported, as in the loop below */
+      const int lr = reach_level_par(&m, &nogoal, &R, fr, nfr, ++level, emode, qmask, Lq, Uq, t0, &S0, &unused, TB);
+      S0.probes = pr0;
+      if (lr) { timed_out = 1; break; }
+      S0.status = 0;
+    } else
+#endif
+    {
     S0.explored += nfr;
     ++level;
     B.n = 0;
@@ -1611,6 +1631,7 @@ static int32_t liveness_core(const hora_net_desc* net, const hora_pred_desc* p, 
       if (id >= 0) R.stouch[slot_of(&R, k)] = level;
     }
     if (timed_out) break;
+    }
     nfr = collect_frontier(&R, level, &fr, &capfr);
     if (emode == 0 && R.nkeys && (double)R.nlive >= 4.0 * (double)R.nkeys) emode = 1;
     /* p --> q: the early witness on every zone this level stored (leadsto_witness,
@@ -1627,6 +1648,12 @@ static int32_t liveness_core(const hora_net_desc* net, const hora_pred_desc* p, 
   if (!psi && q->nclk == 1) {
     m.avoid_neg[0] = q->clk_cond[1]; m.avoid_neg[1] = q->clk_cond[0]; m.avoid_neg[2] = r_negate(q->clk_cond[2]);
   }
+#ifdef _OPENMP
+  for (int t = 0; TB && t < g_threads; ++t) {
+    free(TB[t].locs); free(TB[t].ints); free(TB[t].zones); free(TB[t].raw); free(TB[t].parent);
+  }
+  free(TB);
+#endif
   if (!psi) {   /* p --> q: the subsumed graph and the federation sweep */
     int viol = violated;
     if (timed_out) S0.status = HORA_E_TIMEOUT;

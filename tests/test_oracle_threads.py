@@ -23,3 +23,20 @@ def test_threads_match_sequential(cfg, seed):
     assert got == want
     for k in KEYS:
         assert gst[k] == wst[k], (k, gst[k], wst[k])
+
+
+@pytest.mark.parametrize("seed", [6, 20])
+def test_threads_match_sequential_leadsto(seed):
+    """Phase 1 of p --> q runs the same multi-core level; verdict and counts are unchanged."""
+    net, kind, p, q = config_instance(3, seed)
+    try:
+        pyoracle.set_threads(1)
+        want, wst = pyoracle.leads_to(net, p, q)
+        if pyoracle.set_threads(4) == 1:
+            pytest.skip("oracle built without OpenMP")
+        got, gst = pyoracle.leads_to(net, p, q)
+    finally:
+        pyoracle.set_threads(1)
+    assert got == want
+    for k in ("explored", "generated", "stored", "keys", "levels"):
+        assert gst[k] == wst[k], (k, gst[k], wst[k])
