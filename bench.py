@@ -366,7 +366,7 @@ def like_for_like(config: int, seeds, cap: float, plain_budget: float) -> dict:
     import ctypes
     from ptctcl_gb300 import engine
     from ptctcl_gb300.generator import config_instance
-    done_items, plain_lat, plain_v, plain_gen = [], [], [], 0
+    done_items, plain_lat, plain_v, plain_gen, plain_seeds, plain_st = [], [], [], 0, [], []
     tried, t0 = 0, time.perf_counter()
     plain_busy = 0.0
     for sd in seeds:
@@ -383,6 +383,8 @@ def like_for_like(config: int, seeds, cap: float, plain_budget: float) -> dict:
         tried += 1
         if v[0] >= 0 and st[0]["status"] == 0:
             done_items.append(it)
+            plain_seeds.append(sd)
+            plain_st.append(st[0])
             plain_v.append(v[0])
             plain_gen += st[0]["generated"]
             plain_busy += dt
@@ -403,7 +405,12 @@ def like_for_like(config: int, seeds, cap: float, plain_budget: float) -> dict:
                         "p50_time_to_verdict_s": percentile(lat, 50), "p99_time_to_verdict_s": percentile(lat, 99)},
             "speedup": (b_gen / bdt) / max(1e-12, plain_gen / plain_busy),
             "same_successors": b_gen == plain_gen,
-            "verdicts_compared": len(bv), "verdicts_agree": list(bv) == plain_v}
+            "verdicts_compared": len(bv), "verdicts_agree": list(bv) == plain_v,
+            "mismatches": [{"seed": plain_seeds[k], "kind": done_items[k][1], "plain": plain_v[k], "batched": bv[k],
+                            "batched_status": bst[k]["status"], "plain_generated": plain_st[k]["generated"],
+                            "batched_generated": bst[k]["generated"]}
+                           for k in range(len(bv)) if bv[k] != plain_v[k] or
+                           bst[k]["generated"] != plain_st[k]["generated"]][:8]}
 
 
 def run_batched(args):

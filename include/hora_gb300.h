@@ -258,10 +258,20 @@ HORA_GB_API int32_t hora_gb_has_deadlock_noalloc(const hora_net_desc* net, int32
  * out-of-scope input returns HORA_E_NOT_SUPPORTED or HORA_E_INVALID there, before any device is
  * touched. hora_gb_run runs the query on the CUDA backend; *verdict follows the single-query
  * convention of hora_gb_batch_run (reach: reachable; deadlock: deadlock reachable; leads-to and
- * E[]: holds). hora_gb_trace copies the witness of the last run of an E[] query, with the buffers
- * and conventions of hora_gb_exists_invariant_trace (*nsteps = 0 when psi fails); other kinds
- * return HORA_E_NOT_SUPPORTED, and a handle that has not run returns HORA_E_INVALID. A handle is
- * used by one thread at a time. */
+ * E[]: holds). hora_gb_trace copies the trace of the last run, into the buffers of
+ * hora_gb_exists_invariant_trace:
+ *   E[] psi: the witness, with that function's conventions (*nsteps = 0 when psi fails);
+ *   reach, deadlock, and a leads-to violation found by the early witness: a counterexample -- the path
+ *     of the passed store from the initial state (step 0) to the goal: a state matching the target,
+ *     a state holding a deadlocked valuation, or a reachable p-state whose part outside q holds a
+ *     valuation where a maximal run that avoids q may stop. ords[i] (i > 0) is the index of the
+ *     transition taken from step i-1 among those hora_gb_expand's enumeration visits (the candidate
+ *     transitions whose integer guards and committed rules hold, in emission order, whether or not
+ *     their zone is empty); zones[i] is the stored zone, which contains the exact successor of
+ *     zones[i-1] by that transition (it may be extrapolated, or a convex union); *loop_to = -1.
+ *     *nsteps = 0 when the goal was not reached, and for a leads-to violation found only by the
+ *     backward sweep (its witness is a cycle of the subsumed graph, not recorded).
+ * A handle that has not run returns HORA_E_INVALID. A handle is used by one thread at a time. */
 typedef struct hora_handle_s* hora_handle;
 HORA_GB_API int32_t hora_gb_open(const hora_net_desc* net, const hora_query_desc* q, hora_handle* out);
 HORA_GB_API int32_t hora_gb_run(hora_handle h, int32_t* verdict, hora_stats* stats);

@@ -929,6 +929,31 @@ int32_t orc_expand(const hora_net_desc* net, int32_t n, const int32_t* locs, con
   model_free(&m);
   return x.n > cap ? HORA_E_OVERFLOW : HORA_OK;
 }
+/* The successor of (locs, ints, zone) by transition `raw` (the index successors() gives it), exact
+ * (no extrapolation), with the active-clock reduction under qmask. Returns 1 and fills the out
+ * buffers when that transition yields a non-empty zone, 0 otherwise. Replays the traces of the
+ * forward routes step by step. */
+typedef struct { int want, hit; int np, ni, d2; int32_t *locs, *ints, *zone; } RawCtx;
+static void raw_emit(void* c, const int32_t* locs, const int32_t* ints, const int32_t* zone, int raw) {
+  RawCtx* x = (RawCtx*)c;
+  if (raw != x->want || x->hit) return;
+  x->hit = 1;
+  memcpy(x->locs, locs, sizeof(int32_t) * x->np);
+  if (x->ni) memcpy(x->ints, ints, sizeof(int32_t) * x->ni);
+  memcpy(x->zone, zone, sizeof(int32_t) * x->d2);
+}
+int32_t orc_successor_raw(const hora_net_desc* net, const uint8_t* qmask, const int32_t* locs, const int32_t* ints,
+                          const int32_t* zone, int32_t raw, int32_t* out_locs, int32_t* out_ints, int32_t* out_zone) {
+  Model m;
+  if (model_build(net, &m)) { model_free(&m); return 0; }
+  uint8_t qm[64] = {0};
+  if (qmask) memcpy(qm, qmask, (size_t)m.dim);
+  RawCtx x = {raw, 0, net->nprocs, net->nints, m.dim * m.dim, out_locs, out_ints, out_zone};
+  successors(&m, locs, ints, zone, m.L, m.U, qm, 0, raw_emit, &x);
+  model_free(&m);
+  return x.hit;
+}
+
 int32_t orc_has_deadlock(const hora_net_desc* net, int32_t n, const int32_t* locs,
                          const int32_t* ints, const int32_t* zones, int32_t* out) {
   Model m;

@@ -59,6 +59,10 @@ int32_t orc_expand(const hora_net_desc* net, int32_t n, const int32_t* locs, con
                    int32_t* out_locs, int32_t* out_ints, int32_t* out_zones, int64_t* out_n);
 int32_t orc_has_deadlock(const hora_net_desc* net, int32_t n, const int32_t* locs,
                          const int32_t* ints, const int32_t* zones, int32_t* out);
+/* The exact successor of one state by transition `raw` (its index in the enumeration): 1 and the
+ * out buffers filled when it is non-empty, else 0. The step check of the forward routes' traces. */
+int32_t orc_successor_raw(const hora_net_desc* net, const uint8_t* qmask, const int32_t* locs, const int32_t* ints,
+                          const int32_t* zone, int32_t raw, int32_t* out_locs, int32_t* out_ints, int32_t* out_zone);
 
 /* ---- whole queries (level-synchronous BFS in the canonical order the engine uses) ---- */
 int32_t orc_reachable_net(const hora_net_desc* net, const hora_pred_desc* target, hora_stats* st,

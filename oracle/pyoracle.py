@@ -62,6 +62,8 @@ def lib():
         L.orc_initial_state.restype = I32
         L.orc_set_time_limit.argtypes = [ctypes.c_double]
         L.orc_set_time_limit.restype = None
+        L.orc_successor_raw.argtypes = [VP, ctypes.POINTER(ctypes.c_uint8), P32, P32, P32, I32, P32, P32, P32]
+        L.orc_successor_raw.restype = I32
         L.orc_set_threads.argtypes = [I32]
         L.orc_set_threads.restype = I32
     return _lib
@@ -196,6 +198,24 @@ def has_deadlock(net: Network, locs, ints, zones):
     rc = lib().orc_has_deadlock(ctypes.addressof(na.desc), n, _p(locs), _p(ints), _p(zones), _p(out))
     assert rc == 0, rc
     return out.astype(bool)
+
+
+def successor_raw(net: Network, locs, ints, zone, raw: int, qmask=None):
+    """The exact successor by transition index `raw`, or None when that transition yields nothing."""
+    na = NetArrays(net)
+    np_, ni, d = len(net.procs), len(net.ints), net.dim
+    l = np.ascontiguousarray(locs, np.int32).reshape(-1)
+    i = np.ascontiguousarray(ints, np.int32).reshape(-1) if ni else np.zeros(1, np.int32)
+    z = np.ascontiguousarray(zone, np.int32).reshape(-1)
+    qm = np.zeros(64, np.uint8)
+    if qmask is not None:
+        qm[:len(qmask)] = np.asarray(qmask, np.uint8)
+    ol, oi, oz = np.zeros(max(np_, 1), np.int32), np.zeros(max(ni, 1), np.int32), np.zeros(d * d, np.int32)
+    ok = lib().orc_successor_raw(ctypes.addressof(na.desc), qm.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)),
+                                 _p(l), _p(i), _p(z), int(raw), _p(ol), _p(oi), _p(oz))
+    if not ok:
+        return None
+    return ol[:np_], oi[:ni], oz.reshape(d, d)
 
 
 def initial_state(net: Network, qmask=None):

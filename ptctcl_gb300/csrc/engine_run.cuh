@@ -106,7 +106,7 @@ template <int D>
 struct StoreBufs {
   DBuf hkey, pend, pend_base, klive, kloff;   // hash table
   DBuf arena;                                 // key lists
-  DBuf nzone, ncol0, nlevel, ndead, ninst, nkey;   // nodes
+  DBuf nzone, ncol0, nlevel, ndead, ninst, nkey, npar, nraw;   // nodes
   unsigned long long hcap = 0;
   long long ncap = 0, acap = 0;
 };
@@ -125,7 +125,7 @@ struct Engine {
   int blocks = 0;
   DeviceNets dn;
   StoreBufs<D> S[2];
-  DBuf skey, sparent, sord, sraw, sflag, sslot, srank, szone, ssurv, sseg, ssorted, stouched, sokh, sokl, sskh, sskl,
+  DBuf skey, sparent, sord, sraw, sflag, spnode, sslot, srank, szone, ssurv, sseg, ssorted, stouched, sokh, sokl, sskh, sskl,
       sheavy, slight;
   long long scap = 0;
   DBuf clist;
@@ -141,7 +141,8 @@ struct Engine {
   std::vector<long long> h_hbm, h_prefix;
   DBuf zw;                      // exact-zone table of the graph store
   unsigned long long zcap = 0;
-  DBuf ctl, emode, done, found, generated, gen_backup, nlive, nkeys, nfront, probes;
+  DBuf ctl, emode, done, found, generated, gen_backup, nlive, nkeys, nfront, probes, hit_node, hit_raw, hit_key,
+      hit_zone;
   Ctl hctl{};
   KTimer kt;
   unsigned long long launches = 0, h2d = 0, d2h = 0;
@@ -173,13 +174,14 @@ struct Engine {
     st.nzone = B.nzone.template as<int>(); st.ncol0 = B.ncol0.template as<int>();
     st.nlevel = B.nlevel.template as<int>(); st.ndead = B.ndead.template as<int>(); st.ninst = B.ninst.template as<int>();
     st.nkey = B.nkey.template as<unsigned long long>();
+    st.npar = B.npar.template as<int>(); st.nraw = B.nraw.template as<int>();
     return st;
   }
   Succ succ() {
     Succ sc;
     sc.key = skey.template as<unsigned long long>(); sc.parent = sparent.template as<int>();
     sc.ord = sord.template as<int>(); sc.slot = sslot.template as<int>(); sc.rank = srank.template as<int>();
-    sc.raw = sraw.template as<int>(); sc.flag = sflag.template as<int>();
+    sc.raw = sraw.template as<int>(); sc.flag = sflag.template as<int>(); sc.pnode = spnode.template as<int>();
     sc.zone = szone.template as<int>(); sc.surv = ssurv.template as<int>(); sc.seg = sseg.template as<int>();
     sc.sorted = ssorted.template as<int>(); sc.touched = stouched.template as<int>(); sc.cap = scap;
     sc.okh = sokh.template as<unsigned long long>(); sc.okl = sokl.template as<unsigned long long>();
@@ -207,6 +209,8 @@ struct Engine {
     is.generated = generated.template as<unsigned long long>(); is.nlive = nlive.template as<long long>();
     is.nkeys = nkeys.template as<unsigned long long>(); is.nfront = nfront.template as<unsigned long long>();
     is.probes = probes.template as<unsigned long long>();
+    is.hit_node = hit_node.template as<int>(); is.hit_raw = hit_raw.template as<int>();
+    is.hit_key = hit_key.template as<unsigned long long>(); is.hit_zone = hit_zone.template as<int>();
     return is;
   }
   Ctl* dctl() { return ctl.template as<Ctl>(); }
@@ -231,12 +235,13 @@ struct Engine {
     HGB_CUDA(B.arena.alloc((size_t)B.acap * 4));
     HGB_CUDA(B.nzone.alloc(ncap * Z2 * 4)); HGB_CUDA(B.ncol0.alloc(ncap * D * 4)); HGB_CUDA(B.nlevel.alloc(ncap * 4));
     HGB_CUDA(B.ndead.alloc(ncap * 4)); HGB_CUDA(B.ninst.alloc(ncap * 4)); HGB_CUDA(B.nkey.alloc(ncap * 8));
+    HGB_CUDA(B.npar.alloc(ncap * 4)); HGB_CUDA(B.nraw.alloc(ncap * 4));
     return HORA_OK;
   }
   int alloc_succ(long long cap) {
     scap = cap;
     HGB_CUDA(skey.alloc(cap * 8)); HGB_CUDA(sparent.alloc(cap * 4)); HGB_CUDA(sord.alloc(cap * 4));
-    HGB_CUDA(sraw.alloc(cap * 4)); HGB_CUDA(sflag.alloc(cap * 4));
+    HGB_CUDA(sraw.alloc(cap * 4)); HGB_CUDA(sflag.alloc(cap * 4)); HGB_CUDA(spnode.alloc(cap * 4));
     HGB_CUDA(sslot.alloc(cap * 4)); HGB_CUDA(srank.alloc(cap * 4)); HGB_CUDA(szone.alloc(cap * Z2 * 4));
     HGB_CUDA(ssurv.alloc(cap * 4)); HGB_CUDA(sseg.alloc(cap * 4)); HGB_CUDA(ssorted.alloc(cap * 4));
     HGB_CUDA(stouched.alloc(cap * 4));
@@ -466,6 +471,8 @@ struct Engine {
     HGB_CUDA(B.ndead.grow(nc * 4, used * 4, s));
     HGB_CUDA(B.ninst.grow(nc * 4, used * 4, s));
     HGB_CUDA(B.nkey.grow(nc * 8, used * 8, s));
+    HGB_CUDA(B.npar.grow(nc * 4, used * 4, s));
+    HGB_CUDA(B.nraw.grow(nc * 4, used * 4, s));
     B.ncap = nc;
     return HORA_OK;
   }
@@ -514,6 +521,9 @@ struct Engine {
     HGB_CUDA(nkeys.alloc(ni8)); HGB_CUDA(nfront.alloc(ni8)); HGB_CUDA(probes.alloc(ni8));
     for (DBuf* b : {&emode, &done, &found, &generated, &nlive, &nkeys, &nfront, &probes})
       HGB_CUDA(cudaMemsetAsync(b->p, 0, b->bytes, s));
+    HGB_CUDA(hit_node.alloc(ni4)); HGB_CUDA(hit_raw.alloc(ni4)); HGB_CUDA(hit_key.alloc(ni8));
+    HGB_CUDA(hit_zone.alloc((size_t)ninst * Z2 * 4));
+    HGB_CUDA(cudaMemsetAsync(hit_node.p, 0xff, ni4, s));   // -1: no goal state yet
     h_done.assign(ninst, 0); h_emode.assign(ninst, 0); h_found.assign(ninst, 0);
     h_nfront.assign(ninst, 0); h_nkeys.assign(ninst, 0); h_gen.assign(ninst, 0);
     h_nlive.assign(ninst, 0); explored.assign(ninst, 0); levels.assign(ninst, 0);
@@ -1136,6 +1146,74 @@ struct Engine {
   }
   unsigned long long gfp_iters = 0, pre_calls = 0;
 
+  // Trace of a forward search that reached its goal (E<> target, a deadlocked state, or the leads-to
+  // early witness): the creation path of the passed store from the initial state to the node whose
+  // successor is the goal state, then that state. Step i > 0 is labelled with its transition index
+  // (ords[i]); its zone is the stored zone, which contains the exact successor of step i-1's zone by
+  // that transition (the stored zone may be extrapolated or a convex hull). Empty when the goal was
+  // not reached, or when a leads-to violation was found only by the backward sweep.
+  int hit_trace() {
+    Trace& T = *o.trace;
+    T = Trace{};
+    int hn = -1, hr = -1;
+    unsigned long long hk = 0;
+    HGB_CUDA(cudaMemcpyAsync(&hn, hit_node.p, 4, cudaMemcpyDeviceToHost, s));
+    HGB_CUDA(cudaMemcpyAsync(&hr, hit_raw.p, 4, cudaMemcpyDeviceToHost, s));
+    HGB_CUDA(cudaMemcpyAsync(&hk, hit_key.p, 8, cudaMemcpyDeviceToHost, s));
+    HGB_CUDA(cudaStreamSynchronize(s));
+    if (hn == -1) return HORA_OK;
+    std::vector<int> path;                       // nodes, the initial one first
+    std::vector<int> raws;
+    std::vector<unsigned long long> keys;
+    for (int u = hn; u >= 0;) {
+      int par = -1, raw = -1;
+      unsigned long long k = 0;
+      HGB_CUDA(cudaMemcpyAsync(&par, S[0].npar.template as<int>() + u, 4, cudaMemcpyDeviceToHost, s));
+      HGB_CUDA(cudaMemcpyAsync(&raw, S[0].nraw.template as<int>() + u, 4, cudaMemcpyDeviceToHost, s));
+      HGB_CUDA(cudaMemcpyAsync(&k, S[0].nkey.template as<unsigned long long>() + u, 8, cudaMemcpyDeviceToHost, s));
+      HGB_CUDA(cudaStreamSynchronize(s));
+      path.push_back(u); raws.push_back(raw); keys.push_back(k);
+      if ((long long)path.size() > (long long)hctl.nnodes + 1) { err = "trace walk did not reach the initial state"; return HORA_E_CUDA; }
+      u = par;
+    }
+    std::reverse(path.begin(), path.end());
+    std::reverse(raws.begin(), raws.end());
+    std::reverse(keys.begin(), keys.end());
+    const bool extra = hn >= 0 && hr >= 0;         // the goal is a successor of the last node
+    const HostNet& H = *nets[0];
+    const int np = H.nprocs, ni = H.nints;
+    const int nsteps = hn == -2 ? 1 : (int)path.size() + (extra ? 1 : 0);
+    T.nsteps = nsteps;
+    T.ords.assign(nsteps, -1);
+    T.locs.resize((size_t)nsteps * np);
+    T.ints.resize((size_t)nsteps * std::max(ni, 0));
+    T.zones.resize((size_t)nsteps * Z2);
+    auto fill = [&](int i, unsigned long long key, const int* dz) -> int {
+      HGB_CUDA(cudaMemcpyAsync(T.zones.data() + (size_t)i * Z2, dz, Z2 * 4, cudaMemcpyDeviceToHost, s));
+      const unsigned long long kk = key & ((1ull << inst_shift) - 1);
+      for (int p = 0; p < np; ++p) T.locs[(size_t)i * np + p] = (int)((kk >> H.kshift[p]) & ((1ull << H.kwidth[p]) - 1));
+      for (int v = 0; v < ni; ++v)
+        T.ints[(size_t)i * ni + v] = (int)((kk >> H.kshift[np + v]) & ((1ull << H.kwidth[np + v]) - 1)) + H.int_lo[v];
+      return HORA_OK;
+    };
+    int rc;
+    if (hn == -2) {
+      if ((rc = fill(0, hk, hit_zone.template as<int>()))) return rc;
+    } else {
+      for (size_t i = 0; i < path.size(); ++i) {
+        T.ords[i] = i == 0 ? -1 : raws[i];
+        if ((rc = fill((int)i, keys[i], S[0].nzone.template as<int>() + (long long)path[i] * Z2))) return rc;
+      }
+      if (extra) {
+        T.ords[path.size()] = hr;
+        if ((rc = fill((int)path.size(), hk, hit_zone.template as<int>()))) return rc;
+      }
+    }
+    HGB_CUDA(cudaStreamSynchronize(s));
+    d2h += (size_t)nsteps * (Z2 * 4 + 16);
+    return HORA_OK;
+  }
+
   double elapsed() const {
     return std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
   }
@@ -1208,6 +1286,10 @@ int run_group(const std::vector<const HostNet*>& nets, std::vector<InstResult>& 
   if (status == HORA_OK && !eg) status = E.run_levels(0, 0, cur, nf, level, nullptr);
   if (status == HORA_OK && leadsto) status = E.leadsto_phase2(cur);
   if (status != HORA_OK && status != HORA_E_CANCELLED) {
+    E.finish(res, status, leadsto);
+    return status;
+  }
+  if (status == HORA_OK && o.trace && nets.size() == 1 && nets[0]->kind != HORA_Q_EG && (status = E.hit_trace())) {
     E.finish(res, status, leadsto);
     return status;
   }

@@ -635,7 +635,7 @@ int32_t hora_gb_run(hora_handle h, int32_t* verdict, hora_stats* stats) {
   h->st = hora_stats{};
   int32_t r = -1;
   const int32_t rc = run_single(&h->req.d, q.kind, query_p(q), query_q(q), HORA_BACKEND_CUDA, &h->st, nullptr, &r,
-                                q.kind == HORA_Q_EG ? &h->trace : nullptr);
+                                &h->trace);
   stats_out(stats, h->st);
   if (rc) return rc;
   h->ran = true;
@@ -647,10 +647,6 @@ int32_t hora_gb_trace(hora_handle h, int32_t cap, int32_t* nsteps, int32_t* ords
                       int32_t* zones, int32_t* loop_to, int32_t* loop_ord) {
   g_last_error.clear();
   if (!h || !nsteps || !loop_to || !loop_ord || cap < 0) return fail(HORA_E_INVALID, "bad arguments");
-  if (h->req.q.kind != HORA_Q_EG)
-    return fail(HORA_E_NOT_SUPPORTED,
-                "traces are kept for E[] queries only: the other routes store convex hulls of zones reached "
-                "along different paths");
   if (!h->ran) return fail(HORA_E_INVALID, "the handle has not run");
   return copy_trace(h->trace, cap, nsteps, ords, locs, ints, zones, loop_to, loop_ord);
 }

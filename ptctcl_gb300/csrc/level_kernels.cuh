@@ -6,6 +6,8 @@
 
 namespace hgb {
 
+constexpr int kFedMax = 64;   // zones a federation of the leads-to sweep may hold (the sweep doubles K up to it)
+
 // Device buffers the level kernels share. Plain pointers; sizes are the host's business.
 struct Store {
   // hash table of discrete keys
@@ -24,6 +26,8 @@ struct Store {
   int* ndead;                 // [ncap]
   int* ninst;                 // [ncap]
   unsigned long long* nkey;   // [ncap] hash key of the node's discrete state
+  int* npar;                  // [ncap] node whose successor created this one (-1: initial state)
+  int* nraw;                  // [ncap] the creating transition's index (for_each_successor's raw)
 };
 struct Edges {                // zone-graph edges (leads-to graph mode)
   int* src;
@@ -71,6 +75,7 @@ struct Succ {                 // successors of the current level
   int* parent;                // frontier index of the source
   int* ord;                   // emission ordinal within the source
   int* raw;                   // transition index within the source (for_each_successor's raw)
+  int* pnode;                 // passed-store node of the source
   int* flag;                  // inclusion store: 1 when the survivor is stored
   int* slot;                  // hash slot after the probe, -1 when dropped
   int* rank;                  // position among the slot's pending survivors (arrival order)
@@ -110,6 +115,13 @@ struct InstState {            // per-instance device state (one entry per instan
   unsigned long long* nkeys;
   unsigned long long* nfront;
   unsigned long long* probes;
+  // the goal state of a finished forward search, for its trace: the node whose successor reached
+  // the goal (-1 none yet; -2 the initial state itself; with hit_raw -1 the node itself is the goal,
+  // the leads-to early witness), the transition index, and the goal state's key and zone
+  int* hit_node;
+  int* hit_raw;
+  unsigned long long* hit_key;
+  int* hit_zone;              // [ninst * D*D]
 };
 
 template <int D>

@@ -39,6 +39,20 @@ inline __device__ long long slot_find_insert(const Store& st, unsigned long long
   return -1;
 }
 
+// The first goal state of an instance, kept for its trace: the node whose successor it is (or -2 for
+// the initial state, or the node itself with raw -1), the transition index, its key and zone.
+template <int D>
+__device__ __forceinline__ void record_hit(const Tile<D>& t, const InstState& is, int inst, int node, int raw,
+                                           unsigned long long hk, const int (&z)[D]) {
+  if (!is.hit_node) return;
+  int won = 0;
+  if (t.i == 0) won = atomicCAS(&is.hit_node[inst], -1, node) == -1;
+  won = t.shfl(won, 0);
+  if (!won) return;
+  store_rows(t, z, is.hit_zone + (long long)inst * D * D);
+  if (t.i == 0) { is.hit_raw[inst] = raw; is.hit_key[inst] = hk; }
+}
+
 // ---------------------------------------------------------------------------------------------
 // init: the initial symbolic state of every instance (initial_symbolic_state,
 // src/reachability/engine.cpp:1322-1335), its goal test, and its insertion at level 0.
@@ -70,6 +84,7 @@ __global__ void __launch_bounds__(kBlock) k_init(const NetView* nets, int ninst,
       hit = r == 1;
     }
     if (hit) {
+      record_hit(t, is, inst, -2, -1, key_encode(N, locs, ints) | ((unsigned long long)inst << N.inst_shift), z);
       if (t.i == 0) { is.found[inst] = 1; is.done[inst] = 1; atomicOr(&ctl->found, 1u); }
       continue;
     }
@@ -87,6 +102,7 @@ __global__ void __launch_bounds__(kBlock) k_init(const NetView* nets, int ninst,
     st.ncol0[node * D + t.i] = z[0];
     if (t.i == 0) {
       st.nlevel[node] = 0; st.ndead[node] = 0; st.ninst[node] = inst; st.nkey[node] = hk;
+      st.npar[node] = -1; st.nraw[node] = -1;
       const long long off = (long long)atomicAdd(&ctl->arena_alloc, 1ull);
       if (off < st.acap) { st.arena[off] = (int)node; st.kloff[slot] = off; st.klive[slot] = 1; }
       else atomicMax(&ctl->err, 4u);
@@ -131,6 +147,7 @@ __global__ void __launch_bounds__(kBlock) k_expand(const NetView* nets, InstStat
           sc.parent[idx] = (int)f;
           sc.ord[idx] = ord;
           sc.raw[idx] = raw;
+          sc.pnode[idx] = fr.node[f];
           sc.okh[idx] = hk;
           sc.okl[idx] = ((unsigned long long)(unsigned)fr.rank[f] << 32) | (unsigned)ord;
         }
@@ -138,7 +155,11 @@ __global__ void __launch_bounds__(kBlock) k_expand(const NetView* nets, InstStat
         ctl->overflow = 1;
       }
       ++ord;
-      if (N.kind == 0 && !hit) hit = target_hit(N, t, z, tl, ti);
+      if (N.kind == 0 && !hit) {
+        hit = target_hit(N, t, z, tl, ti);
+        if (hit) record_hit(t, is, inst, fr.node[f], raw,
+                            key_encode(N, tl, ti) | ((unsigned long long)inst << N.inst_shift), z);
+      }
     };
     bool ok = true;
     if (roots) {
@@ -256,6 +277,7 @@ __global__ void __launch_bounds__(kBlock) k_deadlock(const NetView* nets, InstSt
     int z[D];
     load_rows(t, z, sc.zone + (long long)s * D * D);
     const int r = state_has_deadlock(N, t, locs, ints, z, S);
+    if (r == 1) record_hit(t, is, inst, sc.pnode[s], sc.raw[s], hk, z);
     if (t.i == 0) {
       if (r < 0) atomicMax(&ctl->err, 4u);
       else if (r == 1) { is.found[inst] = 1; atomicOr(&ctl->found, 1u); }
@@ -403,11 +425,14 @@ __device__ __forceinline__ void finish_key(const Succ& sc, const Store& st, cons
 }
 
 // New node for zone rows `z` of key hk (metadata only; the caller writes the zone).
-__device__ __forceinline__ void node_meta(const Store& st, long long node, int level, int inst, unsigned long long hk) {
+__device__ __forceinline__ void node_meta(const Store& st, long long node, int level, int inst, unsigned long long hk,
+                                          int par, int raw) {
   st.nlevel[node] = level;
   st.ndead[node] = 0;
   st.ninst[node] = inst;
   st.nkey[node] = hk;
+  st.npar[node] = par;
+  st.nraw[node] = raw;
 }
 
 template <int D>
@@ -863,7 +888,7 @@ __device__ void merge_key_block(const NetView* nets, const InstState& is, const 
     const long long node = node_base + used;
     ++used;
     if (tid == 0) {
-      node_meta(st, node, level, inst, hk);
+      node_meta(st, node, level, inst, hk, sc.pnode[a_s], sc.raw[a_s]);
       cl[clen] = (int)node;
       if (rel) {
         if (sh.unioned) hull[sh.nhull++] = clen - clen0;
@@ -967,7 +992,7 @@ __device__ void merge_key_tile(const NetView* nets, const InstState& is, const S
     store_rows(t, z, st.nzone + node * D * D);
     st.ncol0[node * D + t.i] = z[0];
     if (t.i == 0) {
-      node_meta(st, node, level, inst, hk);
+      node_meta(st, node, level, inst, hk, sc.pnode[a], sc.raw[a]);
       cl[clen] = (int)node;
     }
     ++clen;
@@ -1441,5 +1466,3 @@ void Level<D>::has_deadlock(const NetView* nets, const int* locs, const int* int
 }
 
 }  // namespace hgb
-
-#include "subsumed_impl.cuh"

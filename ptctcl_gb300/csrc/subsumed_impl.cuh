@@ -16,8 +16,6 @@
 
 namespace hgb {
 
-constexpr int kFedMax = 64;   // zones a federation of the sweep may hold (the sweep doubles K up to it)
-
 // ---------------------------------------------------------------------------------------------
 // inclusion probe, grouping, maximal survivors, store, key lists, covers, edges
 // ---------------------------------------------------------------------------------------------
@@ -279,6 +277,9 @@ __global__ void __launch_bounds__(kBlock) k_stop_fed(const NetView* nets, InstSt
     key_decode(N, key_part(hk, ishift), locs, ints);
     int z[D];
     load_rows(t, z, st.nzone + n * D * D);
+    int zn[D];   // the node's zone, recorded as the witness state
+#pragma unroll
+    for (int j = 0; j < D; ++j) zn[j] = z[j];
     if (witness) {
       if (!pred_disc(N.p_loc, N.p_nloc, N.p_int, N.p_nint, locs, ints)) continue;
       if (!apply_cons(t, z, N.p_clk, 0, N.p_nclk) || !avoid_cut(N, t, z, locs, ints) || is_empty(t, z)) continue;
@@ -314,6 +315,7 @@ __global__ void __launch_bounds__(kBlock) k_stop_fed(const NetView* nets, InstSt
           return true;
         });
     }
+    if (witness && (whole || npieces > 0)) record_hit(t, is, inst, (int)n, -1, hk, zn);
     if (t.i == 0) {
       if (witness) {
         if (whole || npieces > 0) { is.found[inst] = 1; atomicOr(&ctl->found, 1u); }

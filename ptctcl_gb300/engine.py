@@ -181,7 +181,10 @@ class QueryHandle:
         return bool(v.value)
 
     def trace(self, cap: int = 1 << 16):
-        """The witness of the last run of an E[] query (as exists_invariant_trace), None when psi fails."""
+        """The trace of the last run (hora_gb_trace): the witness of an E[] query (as
+        exists_invariant_trace); for reach / deadlock / a leads-to violation found by the early
+        witness, the counterexample path from the initial state to the goal, ords[i] the transition
+        index of step i. None when there is none."""
         net = self.net
         np_, ni, d2 = len(net.procs), len(net.ints), net.dim * net.dim
         n, lt, lo = ctypes.c_int32(0), ctypes.c_int32(0), ctypes.c_int32(0)

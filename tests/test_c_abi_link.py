@@ -41,7 +41,7 @@ def test_c_program_links_and_calls_the_library(tmp_path):
                     str(exe), "-L", libdir, "-lhora_gb300", f"-Wl,-rpath,{libdir}"], check=True)
     out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.splitlines()
     got = dict(line.split(" ", 1) for line in out)
-    assert got["abi"] == "1"
+    assert got["abi"] == "2"
     assert got["count"] == "0 1"
     assert got["open"] == "1 1"       # HORA_E_INVALID, handle left null
     assert got["run"] == "1" and got["close"] == "1" and got["batch"] == "1"

@@ -84,7 +84,7 @@ def test_handle_open_validates_and_copies_without_a_device():
     assert open_(0, Pred([(0, 3)])) == capi.OK and h.value
     n, lt, lo = ctypes.c_int32(0), ctypes.c_int32(0), ctypes.c_int32(0)
     rc = lib.hora_gb_trace(h, 0, ctypes.byref(n), None, None, None, None, ctypes.byref(lt), ctypes.byref(lo))
-    assert rc == capi.E_NOT_SUPPORTED and "E[]" in capi.last_error()
+    assert rc == capi.E_INVALID and "not run" in capi.last_error()   # every kind keeps a trace once run
     assert lib.hora_gb_close(h) == capi.OK
     assert open_(3, Pred([(0, 3)])) == capi.OK
     rc = lib.hora_gb_trace(h, 0, ctypes.byref(n), None, None, None, None, ctypes.byref(lt), ctypes.byref(lo))

@@ -43,3 +43,73 @@ def test_eg_witness_replays(model, formula, kind, p, q, result):
         k, j = tr["loop_ord"], tr["loop_to"]
         assert 0 <= k < len(sz) and 0 <= j < n
         assert _same((sl[k], si[k], sz[k]), (tr["locs"][j], tr["ints"][j], tr["zones"][j]))
+
+
+# ---- counterexamples of the forward routes: reach, deadlock, the leads-to early witness ----
+from ptctcl_gb300.generator import config_instance  # noqa: E402
+from ptctcl_gb300.model import Q_REACH, Q_DEADLOCK, Q_LEADSTO  # noqa: E402
+from test_gpu_parity import small_config3  # noqa: E402
+
+
+def _qmask(net, *preds):
+    """The clocks the query reads (kept by the active-clock reduction), as the engine folds them in."""
+    m = np.zeros(net.dim, np.uint8)
+    for pr in preds:
+        for (i, j, _) in pr.clk_cond:
+            m[i] = m[j] = 1
+    m[0] = 0
+    return m
+
+
+def _disc_ok(pred, locs, ints):
+    for (pp, l) in pred.loc_req:
+        if (locs[pp] != l) if l >= 0 else (locs[pp] == -l - 1):
+            return False
+    ops = {0: np.equal, 1: np.not_equal, 2: np.less, 3: np.less_equal, 4: np.greater, 5: np.greater_equal}
+    return all(ops[op](ints[v], c) for (v, op, c) in pred.int_cond)
+
+
+CASES = ([("c1", 1, s) for s in range(12)] + [("c2", 2, s) for s in (0, 3, 10, 23)] +
+         [("c4", 4, s) for s in (0, 1, 2, 3, 4, 5, 8, 9, 12, 13, 14, 18, 19, 22, 23, 25, 26, 75)] +
+         [("c3", 3, s) for s in (0, 1, 13, 19, 20, 33)])
+
+
+@pytest.mark.parametrize("name,cfg,seed", CASES, ids=[f"{n}-{s}" for n, _, s in CASES])
+def test_counterexample_replays(name, cfg, seed):
+    """When the goal is reached, the trace is a path of the passed store: step 0 is the initial state,
+    the oracle's exact successor of step i-1 by transition ords[i] exists, has step i's discrete state
+    and lies inside step i's stored zone, and the last step is a goal state (a target state, a state
+    holding a deadlocked valuation, or a p-state for the leads-to witness)."""
+    net, kind, p, q = small_config3(seed) if cfg == 3 else config_instance(cfg, seed)
+    with engine.QueryHandle(net, kind, p, q) as h:
+        verdict = h.run()
+        tr = h.trace()
+    goal = verdict if kind in (Q_REACH, Q_DEADLOCK) else not verdict
+    if not goal:
+        assert tr is None
+        return
+    if kind == Q_LEADSTO and tr is None:
+        pytest.skip("violation found by the backward sweep (no forward witness)")
+    assert tr is not None
+    qm = _qmask(net, p) if kind == Q_REACH else _qmask(net, p, q) if kind == Q_LEADSTO else _qmask(net)
+    n = len(tr["ords"])
+    assert tr["ords"][0] == -1 and tr["loop_to"] == -1
+    ok, l0, i0, z0 = pyoracle.initial_state(net, qm)
+    assert ok
+    assert np.array_equal(l0, tr["locs"][0]) and np.array_equal(i0, tr["ints"][0])
+    assert (tr["zones"][0] >= z0).all()
+    for i in range(1, n):
+        succ = pyoracle.successor_raw(net, tr["locs"][i - 1], tr["ints"][i - 1], tr["zones"][i - 1], tr["ords"][i], qm)
+        assert succ is not None, i
+        sl, si, sz = succ
+        assert np.array_equal(sl, tr["locs"][i]) and np.array_equal(si, tr["ints"][i]), i
+        assert (tr["zones"][i] >= sz).all(), i          # the stored zone contains the exact successor
+    fl, fi, fz = tr["locs"][-1], tr["ints"][-1], tr["zones"][-1]
+    if kind == Q_REACH:
+        assert _disc_ok(p, fl, fi)
+        d = pyoracle.Dbm(net.nclocks, fz)
+        assert all(d.constrain(i, j, r) for (i, j, r) in p.clk_cond)
+    elif kind == Q_DEADLOCK:
+        assert pyoracle.has_deadlock(net, fl[None, :], fi[None, :], fz[None, :])[0]
+    else:
+        assert _disc_ok(p, fl, fi) and not (q.clk_cond == [] and _disc_ok(q, fl, fi))
