@@ -413,6 +413,41 @@ def like_for_like(config: int, seeds, cap: float, plain_budget: float) -> dict:
                            bst[k]["generated"] != plain_st[k]["generated"]][:8]}
 
 
+def leadsto_record(seed: int, cpu_seconds: float = 0.0) -> dict:
+    """Config 3 at full size (6 automata x 8 locations, 6 clocks, p --> q): one warm-up and one timed
+    query through the C ABI; the oracle port of the same query on every host core beside it."""
+    from ptctcl_gb300 import engine
+    from ptctcl_gb300.engine import Backend, ReachStats
+    from ptctcl_gb300.generator import config_instance
+    net, kind, p, q = config_instance(3, seed)
+    engine.leads_to_clocks(net, p, q, Backend.Cuda, ReachStats())
+    st = ReachStats()
+    t = time.perf_counter()
+    holds = engine.leads_to_clocks(net, p, q, Backend.Cuda, st)
+    wall = time.perf_counter() - t
+    rec = {"workload": f"config3 seed {seed}: 6 automata x 8 locations, 6 clocks (7x7 DBM), p --> q",
+           "holds": holds, "successors": st.generated, "levels": st.levels, "graph_zones": st.stored,
+           "value": st.generated / max(1e-12, st.device_seconds), "e2e": st.generated / max(1e-12, wall),
+           "unit": UNIT, "time_to_verdict_s": wall,
+           "decided_by": "early witness" if (not holds and st.stored == 0) else "backward sweep" if st.stored else "no root",
+           "roofline": roofline(st, net.dim, *measured_peaks())}
+    if cpu_seconds > 0:
+        from oracle import pyoracle
+        used = pyoracle.set_threads(os.cpu_count() or 1)
+        pyoracle.set_time_limit(cpu_seconds)
+        try:
+            t = time.perf_counter()
+            ch, cst = pyoracle.leads_to(net, p, q)
+            cdt = time.perf_counter() - t
+        finally:
+            pyoracle.set_time_limit(0)
+            pyoracle.set_threads(1)
+        rec["cpu_baseline"] = {"value": cst["generated"] / cdt, "unit": UNIT, "cores": used, "kind": "port",
+                               "whole_query": not cst["status"], "seconds": cdt,
+                               "verdict_agrees": (ch == holds) if not cst["status"] else None}
+    return rec
+
+
 def run_batched(args):
     line = {"metric": METRIC, **batched_compare(args.instances, args.budget,
                                                 0.0 if args.no_cpu_baseline else args.budget)}
@@ -505,6 +540,8 @@ def main():
     ap.add_argument("--budget", type=float, default=60.0)
     ap.add_argument("--rate", type=float, default=100.0)
     ap.add_argument("--rates", default="", help="serving: comma-separated offered loads (req/s)")
+    ap.add_argument("--leadsto-seeds", default="22,2",
+                    help="full-size config-3 seeds recorded on the default line (empty: none)")
     ap.add_argument("--serving-seconds", type=float, default=15.0,
                     help="seconds of arrivals per load of the serving sweep added to the default line (0: leave it out)")
     ap.add_argument("--duration", type=float, default=60.0)
@@ -604,6 +641,9 @@ def main():
         line["batched_like_for_like"] = {
             "config4": like_for_like(4, range(args.instances), 2.0, args.batched_budget),
             "config3": like_for_like(3, range(100000, 100000 + args.instances), 2.0, args.batched_budget)}
+    seeds3 = [int(x) for x in args.leadsto_seeds.split(",") if x.strip()]
+    if seeds3 and world == 1:
+        line["config3"] = [leadsto_record(sd, 0.0 if (args.no_cpu_baseline or k) else 60.0) for k, sd in enumerate(seeds3)]
     if args.serving_seconds > 0 and world == 1:
         line["serving"] = [serving_run(r, args.serving_seconds, 2 * args.serving_seconds, args.budget_gb,
                                        args.inflight) for r in (100.0, 1000.0)]
