@@ -638,9 +638,11 @@ def main():
     if args.batched_budget > 0 and world == 1:
         line["batched"] = batched_compare(args.instances, args.batched_budget,
                                           0.0 if args.no_cpu_baseline else args.batched_budget)
+        # the same instances to completion in both forms: those the plain form finishes within 0.1 s
+        # (the many small requests of the mix) and within 2 s (a few large ones bound the batch)
         line["batched_like_for_like"] = {
-            "config4": like_for_like(4, range(args.instances), 2.0, args.batched_budget),
-            "config3": like_for_like(3, range(100000, 100000 + args.instances), 2.0, args.batched_budget)}
+            f"config{c}_cap_{cap:g}s": like_for_like(c, range(base, base + args.instances), cap, args.batched_budget / 2)
+            for c, base in ((4, 0), (3, 100000)) for cap in (0.1, 2.0)}
     seeds3 = [int(x) for x in args.leadsto_seeds.split(",") if x.strip()]
     if seeds3 and world == 1:
         line["config3"] = [leadsto_record(sd, 0.0 if (args.no_cpu_baseline or k) else 60.0) for k, sd in enumerate(seeds3)]

@@ -650,10 +650,12 @@ struct Engine {
     if (o.pool && (double)hctl.nnodes > (double)budget_nodes()) grow_budget((long long)hctl.nnodes);
     const double allowed = (double)budget_nodes();
     const bool all = (double)hctl.nnodes > allowed;
+    // with a pool the group grows while the pool has room, so no instance is held to a fixed quarter
+    const bool quarter = ninst > 1 && !o.pool;
     bool changed = false;
     for (int q = 0; q < ninst; ++q) {
       if (h_done[q]) continue;
-      if (all || (ninst > 1 && (double)h_nlive[q] > allowed / 4)) { h_done[q] = 1; h_budget[q] = 1; changed = true; }
+      if (all || (quarter && (double)h_nlive[q] > allowed / 4)) { h_done[q] = 1; h_budget[q] = 1; changed = true; }
     }
     if (changed) {
       HGB_CUDA(cudaMemcpyAsync(is.done, h_done.data(), ni4, cudaMemcpyHostToDevice, s));
@@ -1173,7 +1175,7 @@ struct Engine {
       HGB_CUDA(cudaMemcpyAsync(&k, S[0].nkey.template as<unsigned long long>() + u, 8, cudaMemcpyDeviceToHost, s));
       HGB_CUDA(cudaStreamSynchronize(s));
       path.push_back(u); raws.push_back(raw); keys.push_back(k);
-      if ((long long)path.size() > (long long)hctl.nnodes + 1) { err = "trace walk did not reach the initial state"; return HORA_E_CUDA; }
+      if ((long long)path.size() > S[0].ncap + 1) { err = "trace walk did not reach the initial state"; return HORA_E_CUDA; }
       u = par;
     }
     std::reverse(path.begin(), path.end());

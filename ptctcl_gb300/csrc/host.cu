@@ -778,17 +778,30 @@ int32_t run_batch(int32_t n, const hora_net_desc* nets, const hora_query_desc* q
   RunOptions o = run_options(cancel);
   o.t_call = std::chrono::steady_clock::now();
   o.has_t_call = true;
-  o.pool = pool;
+  o.pool = pool;   // replaced by the call's own pool below when the caller gives none
   int nthreads = std::max(1, std::min(ng, 32));
   if (const char* e = std::getenv("HORA_GB_GROUP_THREADS")) nthreads = std::max(1, std::min(ng, std::atoi(e)));
+  BudgetPool local;
   {
-    // the concurrent groups share three quarters of the free device memory
+    // The concurrent groups share three quarters of the free device memory as a pool: each group
+    // starts from a small reservation and its store grows from the pool level by level, so a large
+    // instance is not held to a fixed share while small groups leave memory unused. A caller's pool
+    // (the serving form) is used instead when given, with the request's reservation already taken.
     size_t fr = 0, tot = 0;
-    if (!store_budget && cudaMemGetInfo(&fr, &tot) == cudaSuccess && fr > 0) store_budget = (size_t)((double)fr * 0.75);
-    if (store_budget) {
-      o.store_budget_bytes = store_budget / nthreads;
-      o.succ_budget_bytes = std::min(o.succ_budget_bytes, std::max<size_t>(o.store_budget_bytes / 4, 64 << 20));
+    if (!pool) {
+      if (!store_budget && cudaMemGetInfo(&fr, &tot) == cudaSuccess && fr > 0) store_budget = (size_t)((double)fr * 0.75);
+      if (store_budget) {
+        const size_t floor = std::min<size_t>(store_budget / (4 * (size_t)nthreads), size_t(256) << 20);
+        local.cap = store_budget > floor * nthreads ? store_budget - floor * nthreads : 0;
+        o.pool = &local;
+        o.store_budget_bytes = floor;
+      }
+    } else {
+      o.store_budget_bytes = store_budget;
     }
+    // a level's successors beyond a quarter of a group's even share run in instance chunks
+    const size_t share = pool ? (size_t)pool->cap / (size_t)nthreads : store_budget / (size_t)nthreads;
+    if (share) o.succ_budget_bytes = std::min(o.succ_budget_bytes, std::max<size_t>(share / 4, 64 << 20));
   }
   std::atomic<int> next{0};
   auto worker = [&]() {
