@@ -127,7 +127,20 @@ def family_bytes(st, dim: int) -> dict:
             "merge": z * (st.merge_surv + st.merge_live + st.nodes)}
 
 
-def roofline(st, dim: int, peaks: dict, peak_kind: str) -> dict:
+def profiled_traffic(seed: int):
+    """DRAM bytes per query of the merge kernel from the committed ncu summary of this workload
+    (profiles/k_merge_dram_config2_seed<seed>.md, line `traffic_bytes_per_query: N`), or None."""
+    path = os.path.join(ROOT, "profiles", f"k_merge_dram_config2_seed{seed}.md")
+    try:
+        for ln in open(path):
+            if ln.startswith("traffic_bytes_per_query:"):
+                return int(ln.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+def roofline(st, dim: int, peaks: dict, peak_kind: str, traffic_per_query=None) -> dict:
     """HBM roofline of the dominant kernel family (CUDA-event time on the engine's stream): its
     algorithmic bytes per launch over its mean launch time, against the measured copy bandwidth;
     every family's figure beside it."""
@@ -141,8 +154,13 @@ def roofline(st, dim: int, peaks: dict, peak_kind: str) -> dict:
         per[k] = {"gbs": round(ach, 2), "bytes": int(b), "seconds": round(sec, 6), "launches": kern[k]["calls"]}
     dom = max(fb, key=lambda k: kern[k]["seconds"])
     peak = peaks.get("hbm_gbs", 1.0)
+    traffic = None
+    if traffic_per_query is not None and dom == "merge":
+        traffic = traffic_per_query / max(1, kern[dom]["calls"])   # per launch, like bytes_per_launch
     return {"bound": "hbm", "kernel": dom, "achieved": per[dom]["gbs"], "peak": peak, "unit": "GB/s",
-            "frac": per[dom]["gbs"] / peak, "traffic": None, "peak_source": peak_kind,
+            "frac": per[dom]["gbs"] / peak, "traffic": traffic, "peak_source": peak_kind,
+            "traffic_source": "k_merge DRAM read+write per query from the ncu capture in profiles/, per family "
+                              "launch" if traffic is not None else None,
             "bytes_per_launch": per[dom]["bytes"] / max(1, kern[dom]["calls"]),
             "path_gbs": round(sum(fb.values()) / max(1e-12, st.device_seconds) / 1e9, 2),
             "families": per,
@@ -629,7 +647,7 @@ def main():
                 "h2d_bytes_per_step": int(s0.h2d_bytes), "d2h_bytes_per_step": int(s0.d2h_bytes)},
         "gpu_launches": int(sum(s.kernel_launches for s in stats)),
     }
-    line["roofline"] = roofline(s0, net.dim, peaks, peak_kind)
+    line["roofline"] = roofline(s0, net.dim, peaks, peak_kind, profiled_traffic(args.seed))
     cs = clock_summary(clk, local)
     if cs:
         line["clocks"] = cs
