@@ -447,7 +447,8 @@ def leadsto_record(seed: int, cpu_seconds: float = 0.0) -> dict:
            "holds": holds, "successors": st.generated, "levels": st.levels, "graph_zones": st.stored,
            "value": st.generated / max(1e-12, st.device_seconds), "e2e": st.generated / max(1e-12, wall),
            "unit": UNIT, "time_to_verdict_s": wall,
-           "decided_by": "early witness" if (not holds and st.stored == 0) else "backward sweep" if st.stored else "no root",
+           "decided_by": ("early witness" if (not holds and st.stored == 0) else "backward sweep" if st.stored
+                           else "no reachable p-state"),
            "roofline": roofline(st, net.dim, *measured_peaks())}
     if cpu_seconds > 0:
         from oracle import pyoracle
@@ -558,7 +559,7 @@ def main():
     ap.add_argument("--budget", type=float, default=60.0)
     ap.add_argument("--rate", type=float, default=100.0)
     ap.add_argument("--rates", default="", help="serving: comma-separated offered loads (req/s)")
-    ap.add_argument("--leadsto-seeds", default="22,2",
+    ap.add_argument("--leadsto-seeds", default="22,2,168",
                     help="full-size config-3 seeds recorded on the default line (empty: none)")
     ap.add_argument("--serving-seconds", type=float, default=15.0,
                     help="seconds of arrivals per load of the serving sweep added to the default line (0: leave it out)")

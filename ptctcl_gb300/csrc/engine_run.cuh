@@ -26,33 +26,39 @@ namespace hgb {
     }                                                                              \
   } while (0)
 
-// A device allocation that frees itself. grow() keeps the first `keep` bytes.
+// A device allocation that frees itself, stream-ordered on the stream it was allocated on (the
+// calling thread's g_alloc_stream): work queued on that stream before the free still sees it, and
+// freeing synchronises nothing. grow() keeps the first `keep` bytes.
 struct DBuf {
   void* p = nullptr;
   size_t bytes = 0;
-  ~DBuf() { if (p) cudaFree(p); }
+  cudaStream_t st = nullptr;
+  ~DBuf() { if (p) cudaFreeAsync(p, st); }
   cudaError_t alloc(size_t b) {
-    if (p) { cudaFree(p); p = nullptr; }
+    if (p) { cudaFreeAsync(p, st); p = nullptr; }
     bytes = 0;
-    cudaError_t e = cudaMalloc(&p, b ? b : 16);
+    st = g_alloc_stream;
+    cudaError_t e = cudaMallocAsync(&p, b ? b : 16, st);
     if (e == cudaSuccess) bytes = b;
+    else p = nullptr;
     return e;
   }
   cudaError_t grow(size_t b, size_t keep, cudaStream_t s) {
     if (b <= bytes) return cudaSuccess;
     void* q = nullptr;
-    cudaError_t e = cudaMalloc(&q, b);
+    cudaError_t e = cudaMallocAsync(&q, b, s);
     if (e != cudaSuccess) return e;
     if (p && keep) {
       e = cudaMemcpyAsync(q, p, std::min(keep, bytes), cudaMemcpyDeviceToDevice, s);
-      if (e != cudaSuccess) { cudaFree(q); return e; }
-      cudaStreamSynchronize(s);
+      if (e != cudaSuccess) { cudaFreeAsync(q, s); return e; }
     }
-    if (p) cudaFree(p);
+    if (p) cudaFreeAsync(p, st == s ? s : st);
     p = q;
+    st = s;
     bytes = b;
     return cudaSuccess;
   }
+  void swap(DBuf& b) { std::swap(p, b.p); std::swap(bytes, b.bytes); std::swap(st, b.st); }
   template <class T> T* as() const { return static_cast<T*>(p); }
 };
 
@@ -122,6 +128,15 @@ struct Engine {
   RunOptions o;
   std::string& err;
   cudaStream_t s = nullptr;
+  // Destroys the stream after every later member (the device buffers, freed on it) is gone.
+  struct StreamEnd {
+    cudaStream_t* ps;
+    cudaStream_t prev = nullptr;   // the thread's allocation stream before this search
+    ~StreamEnd() {
+      if (*ps) { cudaStreamSynchronize(*ps); cudaStreamDestroy(*ps); }
+      if (*ps && g_alloc_stream == *ps) g_alloc_stream = prev;
+    }
+  } s_end{&s};
   int blocks = 0;
   DeviceNets dn;
   StoreBufs<D> S[2];
@@ -160,7 +175,6 @@ struct Engine {
     if (o.pool && pool_taken) o.pool->give(pool_taken);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
-    if (s) cudaStreamDestroy(s);
   }
 
   Store store(int k) {
@@ -277,11 +291,11 @@ struct Engine {
     HGB_CUDA(cudaGetLastError());
     HGB_CUDA(cudaStreamSynchronize(s));
     kt.collect();
-    std::swap(B.hkey.p, k2.p); std::swap(B.hkey.bytes, k2.bytes);
-    std::swap(B.kloff.p, o2.p); std::swap(B.kloff.bytes, o2.bytes);
-    std::swap(B.pend.p, p2.p); std::swap(B.pend.bytes, p2.bytes);
-    std::swap(B.pend_base.p, pb2.p); std::swap(B.pend_base.bytes, pb2.bytes);
-    std::swap(B.klive.p, l2.p); std::swap(B.klive.bytes, l2.bytes);
+    B.hkey.swap(k2);
+    B.kloff.swap(o2);
+    B.pend.swap(p2);
+    B.pend_base.swap(pb2);
+    B.klive.swap(l2);
     B.hcap = ncap;
     return HORA_OK;
   }
@@ -304,7 +318,7 @@ struct Engine {
     HGB_CUDA(cudaGetLastError());
     HGB_CUDA(cudaMemcpyAsync(&dctl()->arena_alloc, n2.p, 8, cudaMemcpyDeviceToDevice, s));
     HGB_CUDA(cudaStreamSynchronize(s));
-    std::swap(B.arena.p, a2.p); std::swap(B.arena.bytes, a2.bytes);
+    B.arena.swap(a2);
     B.acap = cap;
     const int rc = read_ctl();
     if (rc) return rc;
@@ -498,6 +512,9 @@ struct Engine {
     for (int k = 0; k < ninst; ++k)
       if (nets[k]->keybits > inst_shift) { err = "discrete key too wide for the batch"; return HORA_E_NOT_SUPPORTED; }
     HGB_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    s_end.prev = g_alloc_stream;
+    g_alloc_stream = s;   // this search's buffers are allocated and freed on its stream
+    prepare_device_pool();
     int dev = 0, nsm = 0;
     HGB_CUDA(cudaGetDevice(&dev));
     HGB_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
@@ -1030,7 +1047,7 @@ struct Engine {
           kt.end(s, KT_OTHER);
           ++launches;
           HGB_CUDA(cudaMemcpyAsync(&dctl()->walloc, na.p, 8, cudaMemcpyDeviceToDevice, s));
-          std::swap(warena.p, a2.p); std::swap(warena.bytes, a2.bytes);
+          warena.swap(a2);
           wcap = cap2;
           fx.warena = warena.template as<int>(); fx.wcap = wcap;
           if ((rc = read_ctl())) return rc;
@@ -1042,7 +1059,7 @@ struct Engine {
             Level<D>::gfp_compact(fx, n2, a3.template as<int>(), nb3.template as<unsigned long long>(), s);
             ++launches;
             HGB_CUDA(cudaMemcpyAsync(&dctl()->walloc, nb3.p, 8, cudaMemcpyDeviceToDevice, s));
-            std::swap(warena.p, a3.p); std::swap(warena.bytes, a3.bytes);
+            warena.swap(a3);
             wcap = cap3;
             fx.warena = warena.template as<int>(); fx.wcap = wcap;
           }
@@ -1305,13 +1322,19 @@ int run_expand(const HostNet& net, int n, const int* locs, const int* ints, cons
                int* out_src, int* out_ord, int* out_locs, int* out_ints, int* out_zones, int64_t* out_n,
                std::string& err) {
   constexpr long long Z2 = (long long)D * D;
+  cudaStream_t s;
+  HGB_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  // declared first, so it ends last: the buffers below are freed on the stream before it goes
+  struct StreamGuard {
+    cudaStream_t s, prev;
+    ~StreamGuard() { cudaStreamSynchronize(s); cudaStreamDestroy(s); g_alloc_stream = prev; }
+  } sg{s, g_alloc_stream};
+  g_alloc_stream = s;
+  prepare_device_pool();
   DeviceNets dn;
   std::vector<const HostNet*> v{&net};
   int rc = upload_nets(v, 63, dn, err);
   if (rc) return rc;
-  cudaStream_t s;
-  HGB_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
-  struct StreamGuard { cudaStream_t s; ~StreamGuard() { cudaStreamDestroy(s); } } sg{s};
   const int np = net.nprocs, ni = std::max(net.nints, 1);
   DBuf dl, di, dz, ctl;
   HGB_CUDA(dl.alloc((size_t)n * np * 4)); HGB_CUDA(di.alloc((size_t)n * ni * 4)); HGB_CUDA(dz.alloc((size_t)n * Z2 * 4));
@@ -1364,13 +1387,19 @@ template <int D>
 int run_has_deadlock(const HostNet& net, int n, const int* locs, const int* ints, const int* zones, int* out,
                      std::string& err) {
   constexpr long long Z2 = (long long)D * D;
+  cudaStream_t s;
+  HGB_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  // declared first, so it ends last: the buffers below are freed on the stream before it goes
+  struct StreamGuard {
+    cudaStream_t s, prev;
+    ~StreamGuard() { cudaStreamSynchronize(s); cudaStreamDestroy(s); g_alloc_stream = prev; }
+  } sg{s, g_alloc_stream};
+  g_alloc_stream = s;
+  prepare_device_pool();
   DeviceNets dn;
   std::vector<const HostNet*> v{&net};
   int rc = upload_nets(v, 63, dn, err);
   if (rc) return rc;
-  cudaStream_t s;
-  HGB_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
-  struct StreamGuard { cudaStream_t s; ~StreamGuard() { cudaStreamDestroy(s); } } sg{s};
   const int np = net.nprocs, ni = std::max(net.nints, 1);
   DBuf dl, di, dz, dout, ctl;
   HGB_CUDA(dl.alloc((size_t)n * np * 4)); HGB_CUDA(di.alloc((size_t)n * ni * 4));

@@ -324,11 +324,31 @@ int compile_net(const hora_net_desc* n, int kind, const hora_pred_desc* target, 
   return HORA_OK;
 }
 
+thread_local cudaStream_t g_alloc_stream = nullptr;
+
+// Keep up to 32 GiB of freed device memory in the device's default pool between calls (the pool
+// otherwise returns it to the driver at every synchronisation, and the next call maps it again).
+void prepare_device_pool() {
+  static std::mutex mu;
+  static std::vector<char> done;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return;
+  std::lock_guard<std::mutex> g(mu);
+  if ((int)done.size() <= dev) done.resize(dev + 1, 0);
+  if (done[dev]) return;
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+    uint64_t thr = uint64_t(32) << 30;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+  }
+  done[dev] = 1;
+}
+
 DeviceNets::~DeviceNets() {
-  for (void* b : blobs) cudaFree(b);
-  if (views) cudaFree(views);
-  if (views_plain) cudaFree(views_plain);
-  if (ok) cudaFree(ok);
+  if (!blobs.empty()) cudaFreeAsync(blobs[0], stream);
+  if (views) cudaFreeAsync(views, stream);
+  if (views_plain) cudaFreeAsync(views_plain, stream);
+  if (ok) cudaFreeAsync(ok, stream);
 }
 
 // The instance's device tables as one int32 blob (every array 16-byte aligned) and their offsets.
@@ -386,32 +406,40 @@ NetView make_view(const HostNet& H, const int32_t* b, const std::vector<size_t>&
   return V;
 }
 
+// Every instance's tables in one device allocation (one copy), on the calling thread's stream.
 int upload_nets(const std::vector<const HostNet*>& nets, int inst_shift, DeviceNets& out, std::string& err) {
   const int ninst = (int)nets.size();
+  const cudaStream_t s = g_alloc_stream;
+  out.stream = s;
   out.host_views.resize(ninst);
   std::vector<int> okv(ninst, 1);
-  std::vector<int32_t> blob;
-  std::vector<size_t> offs;
+  std::vector<int32_t> all, blob;
+  std::vector<std::vector<size_t>> offs(ninst);
+  std::vector<size_t> start(ninst);
   for (int k = 0; k < ninst; ++k) {
-    const HostNet& H = *nets[k];
-    build_blob(H, blob, offs);
-    void* d = nullptr;
-    cudaError_t e = cudaMalloc(&d, blob.size() * 4);
-    if (e != cudaSuccess) { err = std::string("CUDA: cudaMalloc: ") + cudaGetErrorString(e); return HORA_E_NOMEM; }
-    out.blobs.push_back(d);
+    build_blob(*nets[k], blob, offs[k]);   // each blob a multiple of 4 ints: every start stays 16-byte aligned
+    start[k] = all.size();
+    all.insert(all.end(), blob.begin(), blob.end());
     out.blob_bytes.push_back(blob.size() * 4);
-    e = cudaMemcpy(d, blob.data(), blob.size() * 4, cudaMemcpyHostToDevice);
-    if (e != cudaSuccess) { err = std::string("CUDA: cudaMemcpy: ") + cudaGetErrorString(e); return HORA_E_CUDA; }
-    out.host_views[k] = make_view(H, static_cast<const int32_t*>(d), offs, inst_shift);
   }
-  cudaError_t e = cudaMalloc(&out.views, sizeof(NetView) * std::max(ninst, 1));
-  if (e == cudaSuccess) e = cudaMemcpy(out.views, out.host_views.data(), sizeof(NetView) * ninst, cudaMemcpyHostToDevice);
+  void* d = nullptr;
+  cudaError_t e = cudaMallocAsync(&d, std::max<size_t>(all.size(), 4) * 4, s);
+  if (e != cudaSuccess) { err = std::string("CUDA: cudaMallocAsync: ") + cudaGetErrorString(e); return HORA_E_NOMEM; }
+  out.blobs.push_back(d);
+  if (!all.empty()) e = cudaMemcpyAsync(d, all.data(), all.size() * 4, cudaMemcpyHostToDevice, s);
+  for (int k = 0; k < ninst; ++k)
+    out.host_views[k] = make_view(*nets[k], static_cast<const int32_t*>(d) + start[k], offs[k], inst_shift);
   std::vector<NetView> plain = out.host_views;
   for (NetView& V : plain) V.av_on = 0;
-  if (e == cudaSuccess) e = cudaMalloc(&out.views_plain, sizeof(NetView) * std::max(ninst, 1));
-  if (e == cudaSuccess) e = cudaMemcpy(out.views_plain, plain.data(), sizeof(NetView) * ninst, cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = cudaMalloc(&out.ok, sizeof(int) * std::max(ninst, 1));
-  if (e == cudaSuccess) e = cudaMemcpy(out.ok, okv.data(), sizeof(int) * ninst, cudaMemcpyHostToDevice);
+  const size_t vb = sizeof(NetView) * std::max(ninst, 1), ob = sizeof(int) * std::max(ninst, 1);
+  if (e == cudaSuccess) e = cudaMallocAsync((void**)&out.views, vb, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(out.views, out.host_views.data(), sizeof(NetView) * ninst, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMallocAsync((void**)&out.views_plain, vb, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(out.views_plain, plain.data(), sizeof(NetView) * ninst, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMallocAsync((void**)&out.ok, ob, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(out.ok, okv.data(), sizeof(int) * ninst, cudaMemcpyHostToDevice, s);
+  // the host vectors go out of scope: finish the copies first (pageable sources)
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) { err = std::string("CUDA: ") + cudaGetErrorString(e); return HORA_E_CUDA; }
   return HORA_OK;
 }

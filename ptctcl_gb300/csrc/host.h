@@ -52,7 +52,16 @@ int compile_net(const hora_net_desc* net, int kind, const hora_pred_desc* p, con
                 std::string& err);
 
 // Device copy of one or more compiled instances: a blob per instance and the NetView array.
+// Device memory of the engine comes from the stream-ordered allocator (cudaMallocAsync /
+// cudaFreeAsync) on the stream of the search that owns it: freeing never synchronises the device,
+// so concurrent searches (the batched and serving forms) do not stall one another, and the device's
+// default pool keeps freed memory for reuse (up to a release threshold set once per device).
+// g_alloc_stream is that stream for the calling thread (nullptr: the legacy default stream).
+extern thread_local cudaStream_t g_alloc_stream;
+void prepare_device_pool();
+
 struct DeviceNets {
+  cudaStream_t stream = nullptr;   // the stream the tables were allocated on (freed on it)
   std::vector<void*> blobs;
   std::vector<size_t> blob_bytes;
   NetView* views = nullptr;   // device array

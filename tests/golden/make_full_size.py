@@ -18,8 +18,9 @@ from ptctcl_gb300.generator import config_instance  # noqa: E402
 
 SEEDS = (1055, 2483)   # 0.31M and 1.45M stored zones
 # config 3: violated by the early witness after 12 BFS levels (10.7M successors), and after 21 levels
-# (110M successors)
-LEADSTO_SEEDS = (22, 2)
+# (110M successors); holding after the whole reachability pass (2.97M successors, no p-state
+# reachable, so the subsumed graph is empty)
+LEADSTO_SEEDS = (22, 2, 168)
 KEYS = ("explored", "generated", "expanded", "stored", "keys", "levels")
 
 
