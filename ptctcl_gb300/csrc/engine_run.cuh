@@ -168,6 +168,7 @@ struct Engine {
   std::vector<double> t_fin;   // per instance: seconds from the start to its verdict (-1: not yet)
   std::vector<char> h_budget;  // per instance: stopped because the group's store budget ran out
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t ev_wait = nullptr;   // blocking-sync event (o.yield_wait)
   std::chrono::steady_clock::time_point t_start;
 
   Engine(const std::vector<const HostNet*>& n, const RunOptions& opt, std::string& e) : nets(n), o(opt), err(e) {}
@@ -175,6 +176,15 @@ struct Engine {
     if (o.pool && pool_taken) o.pool->give(pool_taken);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
+    if (ev_wait) cudaEventDestroy(ev_wait);
+  }
+
+  // Wait until the stream's work is done: spinning (lowest latency) or, when several searches share
+  // the host's cores, sleeping on a blocking-sync event so the threads do not take turns on them.
+  cudaError_t wait() {
+    if (!ev_wait) return cudaStreamSynchronize(s);
+    cudaError_t e = cudaEventRecord(ev_wait, s);
+    return e == cudaSuccess ? cudaEventSynchronize(ev_wait) : e;
   }
 
   Store store(int k) {
@@ -232,7 +242,7 @@ struct Engine {
   int read_ctl() {
     HGB_CUDA(cudaMemcpyAsync(&hctl, dctl(), sizeof(Ctl), cudaMemcpyDeviceToHost, s));
     d2h += sizeof(Ctl);
-    HGB_CUDA(cudaStreamSynchronize(s));
+    HGB_CUDA(wait());
     kt.collect();
     return HORA_OK;
   }
@@ -289,7 +299,7 @@ struct Engine {
     kt.end(s, KT_OTHER);
     ++launches;
     HGB_CUDA(cudaGetLastError());
-    HGB_CUDA(cudaStreamSynchronize(s));
+    HGB_CUDA(wait());
     kt.collect();
     B.hkey.swap(k2);
     B.kloff.swap(o2);
@@ -317,7 +327,7 @@ struct Engine {
     ++launches;
     HGB_CUDA(cudaGetLastError());
     HGB_CUDA(cudaMemcpyAsync(&dctl()->arena_alloc, n2.p, 8, cudaMemcpyDeviceToDevice, s));
-    HGB_CUDA(cudaStreamSynchronize(s));
+    HGB_CUDA(wait());
     B.arena.swap(a2);
     B.acap = cap;
     const int rc = read_ctl();
@@ -440,7 +450,7 @@ struct Engine {
     if (hctl.err) { err = "device error in the leads-to witness test"; return (int)hctl.err; }
     const size_t ni4 = (size_t)ninst * 4;
     HGB_CUDA(cudaMemcpyAsync(h_found.data(), is.found, ni4, cudaMemcpyDeviceToHost, s));
-    HGB_CUDA(cudaStreamSynchronize(s));
+    HGB_CUDA(wait());
     d2h += ni4;
     bool changed = false;
     const double now = elapsed();
@@ -515,6 +525,7 @@ struct Engine {
     s_end.prev = g_alloc_stream;
     g_alloc_stream = s;   // this search's buffers are allocated and freed on its stream
     prepare_device_pool();
+    if (o.yield_wait) HGB_CUDA(cudaEventCreateWithFlags(&ev_wait, cudaEventBlockingSync | cudaEventDisableTiming));
     int dev = 0, nsm = 0;
     HGB_CUDA(cudaGetDevice(&dev));
     HGB_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
@@ -568,7 +579,7 @@ struct Engine {
     if (hctl.err) { err = "device error in init"; return (int)hctl.err; }
     HGB_CUDA(cudaMemcpyAsync(h_found.data(), is.found, (size_t)ninst * 4, cudaMemcpyDeviceToHost, s));
     HGB_CUDA(cudaMemcpyAsync(h_done.data(), is.done, (size_t)ninst * 4, cudaMemcpyDeviceToHost, s));
-    HGB_CUDA(cudaStreamSynchronize(s));
+    HGB_CUDA(wait());
     *nf = (long long)hctl.nfront;
     return HORA_OK;
   }
@@ -589,7 +600,7 @@ struct Engine {
       HGB_CUDA(cudaMemcpyAsync(h_nfront.data(), is.nfront, ni8, cudaMemcpyDeviceToHost, s));
       HGB_CUDA(cudaMemsetAsync(is.nfront, 0, ni8, s));
       HGB_CUDA(cudaMemsetAsync(&dctl()->nfront, 0, 8, s));
-      HGB_CUDA(cudaStreamSynchronize(s));
+      HGB_CUDA(wait());
       if (!roots)
         for (int q = 0; q < ninst; ++q)
           if (!h_done[q] && h_nfront[q]) { explored[q] += h_nfront[q]; levels[q] = level; }
@@ -621,7 +632,7 @@ struct Engine {
         HGB_CUDA(cudaMemcpyAsync(h_found.data(), is.found, ni4, cudaMemcpyDeviceToHost, s));
         HGB_CUDA(cudaMemcpyAsync(h_nlive.data(), is.nlive, ni8, cudaMemcpyDeviceToHost, s));
         HGB_CUDA(cudaMemcpyAsync(h_nkeys.data(), is.nkeys, ni8, cudaMemcpyDeviceToHost, s));
-        HGB_CUDA(cudaStreamSynchronize(s));
+        HGB_CUDA(wait());
         bool changed = false;
         const double now = elapsed();
         for (int q = 0; q < ninst; ++q) {
@@ -662,7 +673,7 @@ struct Engine {
     InstState is = istate();
     if (mode >= 1) {
       HGB_CUDA(cudaMemcpyAsync(h_nlive.data(), is.nlive, ni8, cudaMemcpyDeviceToHost, s));
-      HGB_CUDA(cudaStreamSynchronize(s));
+      HGB_CUDA(wait());
     }
     if (o.pool && (double)hctl.nnodes > (double)budget_nodes()) grow_budget((long long)hctl.nnodes);
     const double allowed = (double)budget_nodes();
@@ -708,7 +719,7 @@ struct Engine {
     HGB_CUDA(cudaMemcpyAsync(h_hn.data(), hv_n.p, nh * 4, cudaMemcpyDeviceToHost, s));
     HGB_CUDA(cudaMemcpyAsync(h_ha.data(), hv_a.p, nh * 4, cudaMemcpyDeviceToHost, s));
     HGB_CUDA(cudaMemcpyAsync(h_hbm.data(), hv_bm.p, nh * 8, cudaMemcpyDeviceToHost, s));
-    HGB_CUDA(cudaStreamSynchronize(s));
+    HGB_CUDA(wait());
     // Largest keys first: a key's ordered fold is serial, so the level's merge ends no earlier than
     // its longest key; started first, it runs alongside all the others.
     h_order.resize(nh);
@@ -723,7 +734,7 @@ struct Engine {
     kt.end(s, KT_MERGE);
     ++launches;
     HGB_CUDA(cudaGetLastError());
-    HGB_CUDA(cudaStreamSynchronize(s));
+    HGB_CUDA(wait());
     d2h += nh * 16;
     // tiles of 32 x 32 pairs: survivors x earlier survivors, survivors x old zones
     long long tot = 0;
@@ -751,7 +762,7 @@ struct Engine {
       kt.end(s, KT_MERGE);
       ++launches;
       HGB_CUDA(cudaGetLastError());
-      HGB_CUDA(cudaStreamSynchronize(s));   // the prefix buffer is host memory
+      HGB_CUDA(wait());   // the prefix buffer is host memory
     }
     return HORA_OK;
   }
@@ -1115,7 +1126,7 @@ struct Engine {
       HGB_CUDA(cudaMemcpyAsync(ed.data(), edst.p, ne * 4, cudaMemcpyDeviceToHost, s));
       HGB_CUDA(cudaMemcpyAsync(eo.data(), eord.p, ne * 4, cudaMemcpyDeviceToHost, s));
     }
-    HGB_CUDA(cudaStreamSynchronize(s));
+    HGB_CUDA(wait());
     d2h += (size_t)n2 * 20 + (size_t)ne * 12;
     int root = -1;
     for (long long u = 0; u < n2 && root < 0; ++u)
@@ -1160,7 +1171,7 @@ struct Engine {
       for (int v = 0; v < ni; ++v)
         T.ints[(size_t)i * ni + v] = (int)((k >> H.kshift[np + v]) & ((1ull << H.kwidth[np + v]) - 1)) + H.int_lo[v];
     }
-    HGB_CUDA(cudaStreamSynchronize(s));
+    HGB_CUDA(wait());
     return HORA_OK;
   }
   unsigned long long gfp_iters = 0, pre_calls = 0;
@@ -1179,7 +1190,7 @@ struct Engine {
     HGB_CUDA(cudaMemcpyAsync(&hn, hit_node.p, 4, cudaMemcpyDeviceToHost, s));
     HGB_CUDA(cudaMemcpyAsync(&hr, hit_raw.p, 4, cudaMemcpyDeviceToHost, s));
     HGB_CUDA(cudaMemcpyAsync(&hk, hit_key.p, 8, cudaMemcpyDeviceToHost, s));
-    HGB_CUDA(cudaStreamSynchronize(s));
+    HGB_CUDA(wait());
     if (hn == -1) return HORA_OK;
     std::vector<int> path;                       // nodes, the initial one first
     std::vector<int> raws;
@@ -1190,7 +1201,7 @@ struct Engine {
       HGB_CUDA(cudaMemcpyAsync(&par, S[0].npar.template as<int>() + u, 4, cudaMemcpyDeviceToHost, s));
       HGB_CUDA(cudaMemcpyAsync(&raw, S[0].nraw.template as<int>() + u, 4, cudaMemcpyDeviceToHost, s));
       HGB_CUDA(cudaMemcpyAsync(&k, S[0].nkey.template as<unsigned long long>() + u, 8, cudaMemcpyDeviceToHost, s));
-      HGB_CUDA(cudaStreamSynchronize(s));
+      HGB_CUDA(wait());
       path.push_back(u); raws.push_back(raw); keys.push_back(k);
       if ((long long)path.size() > S[0].ncap + 1) { err = "trace walk did not reach the initial state"; return HORA_E_CUDA; }
       u = par;
@@ -1228,7 +1239,7 @@ struct Engine {
         if ((rc = fill((int)path.size(), hk, hit_zone.template as<int>()))) return rc;
       }
     }
-    HGB_CUDA(cudaStreamSynchronize(s));
+    HGB_CUDA(wait());
     d2h += (size_t)nsteps * (Z2 * 4 + 16);
     return HORA_OK;
   }
@@ -1251,7 +1262,7 @@ struct Engine {
     HGB_CUDA(cudaMemcpyAsync(h_found.data(), is.found, ni4, cudaMemcpyDeviceToHost, s));
     HGB_CUDA(cudaMemcpyAsync(h_nlive.data(), is.nlive, ni8, cudaMemcpyDeviceToHost, s));
     HGB_CUDA(cudaMemcpyAsync(h_nkeys.data(), is.nkeys, ni8, cudaMemcpyDeviceToHost, s));
-    HGB_CUDA(cudaStreamSynchronize(s));
+    HGB_CUDA(wait());
     d2h += 2 * ni8 + ni4 + ni8;
     const double wall = elapsed();
     res.assign(ninst, InstResult{});

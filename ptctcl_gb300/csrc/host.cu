@@ -809,6 +809,11 @@ int32_t run_batch(int32_t n, const hora_net_desc* nets, const hora_query_desc* q
   o.pool = pool;   // replaced by the call's own pool below when the caller gives none
   int nthreads = std::max(1, std::min(ng, 32));
   if (const char* e = std::getenv("HORA_GB_GROUP_THREADS")) nthreads = std::max(1, std::min(ng, std::atoi(e)));
+  // many concurrent groups (or the serving form's concurrent requests) on the host's cores: waiting
+  // threads sleep rather than spin
+  o.yield_wait = pool != nullptr ||
+                 (nthreads > 1 && (unsigned)nthreads >= std::max(1u, std::thread::hardware_concurrency() / 2));
+  if (const char* e = std::getenv("HORA_GB_YIELD_WAIT")) o.yield_wait = std::atoi(e) != 0;
   BudgetPool local;
   {
     // The concurrent groups share three quarters of the free device memory as a pool: each group

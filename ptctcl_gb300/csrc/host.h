@@ -118,6 +118,8 @@ struct RunOptions {
   bool has_t_call = false;    // per-instance times count from t_call (the batch call) when set
   std::chrono::steady_clock::time_point t_call{};
   Trace* trace = nullptr;     // E[] psi, one instance: fill with a witness when it holds
+  bool yield_wait = false;    // wait for the stream on a blocking-sync event (the host thread sleeps
+                              // instead of spinning): for groups that share the host's cores
 };
 
 // Run a group of instances that share the DBM dimension D (one level-synchronous BFS over all of

@@ -769,25 +769,48 @@ __device__ void merge_key_block(const NetView* nets, const InstState& is, const 
   const int tile_idx = warp * TPW + lane / D, ntiles = (blockDim.x >> 5) * TPW;
   const long long node_base = sh.node_base;
   int used = 0, cur = 0;
+  // survivor q + 1's drop flag and successor index, loaded during survivor q
+  unsigned pf_q = 0xffffffffu, pf_drop = 0;
+  int pf_as = 0;
   for (unsigned q = 0; q < n; ++q) {
-    if (rel && drop[q]) continue;   // every thread reads the same word: uniform
+    unsigned dq;
+    int a_s;
+    if (q == pf_q) { dq = pf_drop; a_s = pf_as; }
+    else { dq = rel ? drop[q] : 0u; a_s = sc.sorted[base + q]; }
+    if (dq) continue;   // every thread reads the same word: uniform
     int* const zc = sh.zbuf[cur];
     cur ^= 1;
-    const int a_s = sc.sorted[base + q];
     for (int e = tid; e < DD; e += blockDim.x) zc[e] = sc.zone[(long long)a_s * DD + e];
     if (tid == 0) sh.unioned = 0;
     __syncthreads();
+    if (q + 1 < n) {
+      pf_q = q + 1;
+      pf_drop = rel ? drop[q + 1] : 0u;
+      pf_as = sc.sorted[base + q + 1];
+    }
     const int clen = sh.clen, nhull = sh.nhull;
     // (1)+(2): with relations only the hulls stored this level remain to test; without, every
     // zone stored this level
     bool dropped = false;
     // A zone stored at position clen0 + u of this fold has node id node_base + u, so a hull's zone
-    // and liveness load without going through the list.
+    // and liveness load without going through the list. One pass over the hulls decides both
+    // directions: s_q dropped by a live hull, or (step 3) a live hull that s_q simulates, noted in
+    // hmask by the thread's iteration (bit i: hull tid + i * blockDim; later iterations test again
+    // in step 3). Nothing changes a hull's liveness between the two steps, so this is the same
+    // decision as testing them one after the other. The retire rows' first words load here too,
+    // before the barrier.
+    unsigned hmask = 0, w0 = 0, wt = 0;
+    const long long wq = ((long long)q + 31) / 32;
     if (rel) {
-      for (int h = tid; h < nhull && !dropped; h += blockDim.x) {
+      if (tid < r0w) w0 = r0[(long long)q * r0w + tid];
+      if (tid < wq) wt = rt[(long long)q * rtw + tid];
+      int it = 0;
+      for (int h = tid; h < nhull; h += blockDim.x, ++it) {
         const long long m = node_base + hull[h];
-        const bool live = !st.ndead[m];
-        dropped = alu_le_ptr<D>(zc, st.nzone + m * DD, Lr, Ur) && live;
+        if (st.ndead[m]) continue;
+        const int* zh = st.nzone + m * DD;
+        if (alu_le_ptr<D>(zc, zh, Lr, Ur)) { dropped = true; break; }
+        if (it < 32 && alu_le_ptr<D>(zh, zc, Lr, Ur)) hmask |= 1u << it;
       }
     } else {
       for (int k = clen0 + tid; k < clen && !dropped; k += blockDim.x) {
@@ -805,15 +828,15 @@ __device__ void merge_key_block(const NetView* nets, const InstState& is, const 
     if (rel) {
       const unsigned* row0 = r0 + (long long)q * r0w;
       for (long long w = tid; w < r0w; w += blockDim.x)
-        for (unsigned b = row0[w]; b; b &= b - 1) kill((int)(w * 32 + __ffs(b) - 1));
+        for (unsigned b = w == tid ? w0 : row0[w]; b; b &= b - 1) kill((int)(w * 32 + __ffs(b) - 1));
       const unsigned* rowt = rt + (long long)q * rtw;
-      const long long wq = ((long long)q + 31) / 32;
       for (long long w = tid; w < wq; w += blockDim.x)
-        for (unsigned b = rowt[w]; b; b &= b - 1) {
+        for (unsigned b = w == tid ? wt : rowt[w]; b; b &= b - 1) {
           const int p = tpos[w * 32 + __ffs(b) - 1];
           if (p >= 0) kill(clen0 + p);
         }
-      for (int h = tid; h < nhull; h += blockDim.x) {
+      for (unsigned b = hmask; b; b &= b - 1) kill(clen0 + hull[tid + (__ffs(b) - 1) * (int)blockDim.x]);
+      for (int h = tid + 32 * (int)blockDim.x; h < nhull; h += blockDim.x) {
         const int u = hull[h];
         const long long m = node_base + u;
         const bool live = !st.ndead[m];
