@@ -331,9 +331,13 @@ __device__ __forceinline__ bool facets_inside(const Tile<D>& t, const int (&z)[D
   return true;
 }
 
-// Exact convex union (dbm_try_union; netengine_metal.mm:310-335): a ∪ b is convex iff every
-// region the hull gains past one of a's constraints lies in b, and the same with a and b swapped.
-// On success `a` becomes the hull (the entrywise max of two canonical DBMs is canonical).
+// Exact convex union (dbm_try_union; netengine_metal.mm:310-335): a ∪ b is convex iff the hull
+// h (entrywise max) holds no point outside both. facets_inside(a, b, h) decides exactly whether
+// h \ a ⊆ b -- the part of h past a's loosened constraints is the union of the crossing regions it
+// tests -- and h \ a ⊆ b, h ⊆ a ∪ b and h \ b ⊆ a are the same statement. The reference also
+// tests the swapped direction, which can only agree; it is left out (the same answer, half the
+// closures on a success). On success `a` becomes the hull (the entrywise max of two canonical
+// DBMs is canonical).
 template <int D>
 __device__ __forceinline__ bool try_union(const Tile<D>& t, int (&a)[D], const int (&b)[D]) {
   if (union_axis_gap(t, a, b)) return false;
@@ -341,7 +345,6 @@ __device__ __forceinline__ bool try_union(const Tile<D>& t, int (&a)[D], const i
 #pragma unroll
   for (int j = 0; j < D; ++j) h[j] = a[j] > b[j] ? a[j] : b[j];
   if (!facets_inside(t, a, b, h)) return false;
-  if (!facets_inside(t, b, a, h)) return false;
 #pragma unroll
   for (int j = 0; j < D; ++j) a[j] = h[j];
   return true;

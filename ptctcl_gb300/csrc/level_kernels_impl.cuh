@@ -363,6 +363,21 @@ __device__ __forceinline__ bool alu_le_ptr(const int* Z, const int* Zp, const in
   return true;
 }
 
+// The x = 0 part of alu_le_ptr from the two zones' column 0 alone: true when it already shows that
+// Z is not simulated by Zp (most failing tests end here, as in the probe).
+template <int D>
+__device__ __forceinline__ bool alu_col0_fails(const int (&z0c)[D], const int (&zp0c)[D], const int (&L)[D],
+                                               const int (&U)[D]) {
+  if (U[0] == kAluNegInf || z0c[0] < r_le(-U[0])) return false;
+  bool w = false;
+#pragma unroll
+  for (int y = 1; y < D; ++y) {
+    if (L[y] == kAluNegInf) continue;
+    w |= zp0c[y] < z0c[y] && r_add(zp0c[y], r_lt(-L[y])) < z0c[0];
+  }
+  return w;
+}
+
 // Canonical rank of every survivor of a segment; threads [tid, n) step `stride`.
 __device__ __forceinline__ void rank_segment(const Succ& sc, unsigned base, unsigned n, unsigned tid, unsigned stride) {
   for (unsigned e = tid; e < n; e += stride) {
@@ -435,6 +450,12 @@ __device__ __forceinline__ void node_meta(const Store& st, long long node, int l
   st.nraw[node] = raw;
 }
 
+// The heavy fold keeps the liveness of the newest kRing list positions in shared memory, so the
+// scan for the union window reads no list entries from memory unless the window reaches further
+// back.
+constexpr int kRing = 256;
+constexpr int kHullList = 1024;   // open hull tests one survivor decides tile-wide
+
 template <int D>
 struct MergeShared {
   int zbuf[2][D * D];   // the survivor being added (becomes the hull on a union), double-buffered
@@ -443,6 +464,18 @@ struct MergeShared {
   int win[kMergeScan];  // list positions of the newest live zones, newest first
   long long cb;
   int nw, best, node, retired, clen, job, unioned, nhull, nkeep;
+  int hcomp;                   // hull count after the last compaction of the hull list
+  int hl_n;                    // live hulls whose column 0 leaves a test with s_q open
+  int hl_u[kHullList];         // their list positions (past the old zones)
+  int hl_f[kHullList];         // bit 0: s_q <= hull open, bit 1: hull <= s_q open, bit 2: hull retired
+  // The first kHC entries of the hull list (list positions and the zones' column 0), and the
+  // liveness of every position this fold stores (bit u: position clen0 + u), so the hull screen
+  // reads no memory outside the block.
+  static constexpr int kHC = (16384 / (4 * (D + 1))) < 1024 ? (16384 / (4 * (D + 1))) : 1024;
+  int hpos[kHC];
+  int hcol[kHC * D];
+  unsigned ulive[kRelMaxN / 32];
+  unsigned lbits[kRing / 32];  // liveness of list positions [clen - kRing, clen), bit p % kRing
   int wsum[64];         // per-warp sums of the block-wide finish
   long long scal[4];    // its frontier base, arena offset, live and new counts
 };
@@ -742,7 +775,10 @@ __device__ void merge_key_block(const NetView* nets, const InstState& is, const 
   const int a = sc.hv.a[j];
   const long long cb = sc.hv.cb[j], bm = sc.hv.bm[j];
   if (cb < 0) { __syncthreads(); return; }
-  if (tid == 0) { sh.clen = a; sh.retired = 0; sh.nhull = 0; }
+  if (tid == 0) { sh.clen = a; sh.retired = 0; sh.nhull = 0; sh.hcomp = 0; sh.hl_n = 0; }
+  for (int w = tid; w < kRing / 32; w += blockDim.x) sh.lbits[w] = 0u;
+  if (bm >= 0)
+    for (int w = tid; w < (int)((n + 31) / 32); w += blockDim.x) sh.ulive[w] = 0u;
   // node ids for every survivor that can be stored (the relations' drops excluded), reserved at once
   if (warp == 0) {
     int keep = 0;
@@ -757,6 +793,8 @@ __device__ void merge_key_block(const NetView* nets, const InstState& is, const 
   __syncthreads();
   int* cl = sc.clist + cb;
   const int clen0 = a;
+  for (int k = (a > kRing ? a - kRing : 0) + tid; k < a; k += blockDim.x)   // read after the first survivor's barrier
+    if (cl[k] >= 0) atomicOr(&sh.lbits[(k & (kRing - 1)) >> 5], 1u << (k & 31));
   const bool rel = bm >= 0;
   unsigned* R = rel ? sc.hv.pool + bm : nullptr;
   const long long rtw = ((long long)n + 31) / 32, r0w = ((long long)a + 31) / 32;
@@ -788,29 +826,135 @@ __device__ void merge_key_block(const NetView* nets, const InstState& is, const 
       pf_drop = rel ? drop[q + 1] : 0u;
       pf_as = sc.sorted[base + q + 1];
     }
-    const int clen = sh.clen, nhull = sh.nhull;
+    const int clen = sh.clen;
+    int nhull = sh.nhull;
+    // The hull list only grows, and hulls die (retired, or absorbed into a newer hull): when it has
+    // doubled since its last compaction, the block drops its dead entries (order kept).
+    if (rel && nhull >= 256 && nhull >= 2 * sh.hcomp) {
+      int carry = 0;
+      for (int c0 = 0; c0 < nhull; c0 += blockDim.x) {
+        const int h = c0 + tid;
+        const int u = h < nhull ? (h < MergeShared<D>::kHC ? sh.hpos[h] : hull[h]) : 0;
+        const bool live = h < nhull && ((sh.ulive[u >> 5] >> (u & 31)) & 1u);
+        int col[D];
+        if (live) {
+#pragma unroll
+          for (int y = 0; y < D; ++y)
+            col[y] = h < MergeShared<D>::kHC ? sh.hcol[h * D + y] : __ldcg(st.ncol0 + (node_base + u) * D + y);
+        }
+        const unsigned b = __ballot_sync(0xffffffffu, live);
+        if (lane == 0) sh.wsum[warp] = __popc(b);
+        __syncthreads();
+        int before = carry + __popc(b & ((1u << lane) - 1u));
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+          if (w < warp) before += sh.wsum[w];
+          carry += sh.wsum[w];
+        }
+        __syncthreads();   // every entry of this chunk is read before any is overwritten
+        if (live) {   // before <= h: entries of later chunks stay untouched
+          hull[before] = u;
+          if (before < MergeShared<D>::kHC) {
+            sh.hpos[before] = u;
+#pragma unroll
+            for (int y = 0; y < D; ++y) sh.hcol[before * D + y] = col[y];
+          }
+        }
+      }
+      __syncthreads();
+      if (tid == 0) { sh.nhull = carry; sh.hcomp = carry; }
+      nhull = carry;
+    }
     // (1)+(2): with relations only the hulls stored this level remain to test; without, every
     // zone stored this level
     bool dropped = false;
-    // A zone stored at position clen0 + u of this fold has node id node_base + u, so a hull's zone
-    // and liveness load without going through the list. One pass over the hulls decides both
-    // directions: s_q dropped by a live hull, or (step 3) a live hull that s_q simulates, noted in
-    // hmask by the thread's iteration (bit i: hull tid + i * blockDim; later iterations test again
-    // in step 3). Nothing changes a hull's liveness between the two steps, so this is the same
-    // decision as testing them one after the other. The retire rows' first words load here too,
-    // before the barrier.
-    unsigned hmask = 0, w0 = 0, wt = 0;
+    // A zone stored at position clen0 + u of this fold has node id node_base + u, so a hull's zone,
+    // column copy and liveness load without going through the list. Both directions against the
+    // live hulls are decided before the barrier: s_q dropped by a hull, or (step 3) a hull that s_q
+    // simulates. Nothing changes a hull's liveness between the two steps, so this is the same
+    // decision as testing them one after the other. Stage A (a thread per hull entry) settles most
+    // tests from the two column-0 copies and lists the live hulls where a direction stays open;
+    // stage B (a tile per listed hull) loads its rows at once and decides the open directions. The
+    // retire rows' first words load here too.
+    unsigned w0 = 0, wt = 0;
     const long long wq = ((long long)q + 31) / 32;
+    int nl = 0;
     if (rel) {
       if (tid < r0w) w0 = r0[(long long)q * r0w + tid];
       if (tid < wq) wt = rt[(long long)q * rtw + tid];
-      int it = 0;
-      for (int h = tid; h < nhull; h += blockDim.x, ++it) {
-        const long long m = node_base + hull[h];
-        if (st.ndead[m]) continue;
-        const int* zh = st.nzone + m * DD;
-        if (alu_le_ptr<D>(zc, zh, Lr, Ur)) { dropped = true; break; }
-        if (it < 32 && alu_le_ptr<D>(zh, zc, Lr, Ur)) hmask |= 1u << it;
+      if (nhull > 0) {
+        int zq0[D];   // column 0 of s_q
+#pragma unroll
+        for (int y = 0; y < D; ++y) zq0[y] = zc[y * D];
+        auto list_open = [&](int u, const int (&c)[D]) {
+          const int f = (alu_col0_fails<D>(zq0, c, Lr, Ur) ? 0 : 1) | (alu_col0_fails<D>(c, zq0, Lr, Ur) ? 0 : 2);
+          if (!f) return;
+          const int e = atomicAdd(&sh.hl_n, 1);
+          if (e < kHullList) { sh.hl_u[e] = u; sh.hl_f[e] = f; }
+        };
+        constexpr int kHC = MergeShared<D>::kHC;
+        const int ncached = nhull < kHC ? nhull : kHC;
+        for (int h = tid; h < ncached; h += blockDim.x) {   // cached entries: shared memory only
+          const int u = sh.hpos[h];
+          if (!((sh.ulive[u >> 5] >> (u & 31)) & 1u)) continue;
+          int c[D];
+#pragma unroll
+          for (int y = 0; y < D; ++y) c[y] = sh.hcol[h * D + y];
+          list_open(u, c);
+        }
+        for (int h = kHC + tid; h < nhull; h += blockDim.x) {   // the rest: positions and columns from memory
+          const int u = hull[h];
+          if (!((sh.ulive[u >> 5] >> (u & 31)) & 1u)) continue;
+          int c[D];
+#pragma unroll
+          for (int y = 0; y < D; ++y) c[y] = __ldcg(st.ncol0 + (node_base + u) * D + y);
+          list_open(u, c);
+        }
+        __syncthreads();
+        nl = sh.hl_n;
+        if (nl <= kHullList) {
+          if (in_tile) {
+            int z0q[D];   // row 0 of s_q
+#pragma unroll
+            for (int x = 0; x < D; ++x) z0q[x] = zc[x];
+            const int Ly = sel(Lr, t.i);
+            int za[D];
+#pragma unroll
+            for (int x = 0; x < D; ++x) za[x] = zc[t.i * D + x];
+            auto decide = [&](int e, const int (&zb)[D]) {
+              const int f = sh.hl_f[e];
+              if ((f & 1) && alu_le(t, za, zb, z0q, Ly, Ur)) dropped = true;
+              if (f & 2) {
+                int z0h[D];
+#pragma unroll
+                for (int x = 0; x < D; ++x) z0h[x] = t.shfl(zb[x], 0);
+                if (alu_le(t, zb, za, z0h, Ly, Ur) && t.i == 0) sh.hl_f[e] = f | 4;
+              }
+            };
+            if constexpr (D <= 12) {
+              // two listed hulls per tile per step, their rows loaded together
+              for (int e0 = tile_idx; e0 < nl; e0 += 2 * ntiles) {
+                const int e1 = e0 + ntiles;
+                int zb0[D], zb1[D];
+                load_rows_rw(t, zb0, st.nzone + (node_base + sh.hl_u[e0]) * DD);
+                if (e1 < nl) load_rows_rw(t, zb1, st.nzone + (node_base + sh.hl_u[e1]) * DD);
+                decide(e0, zb0);
+                if (e1 < nl) decide(e1, zb1);
+              }
+            } else {
+              for (int e = tile_idx; e < nl; e += ntiles) {
+                int zb[D];
+                load_rows_rw(t, zb, st.nzone + (node_base + sh.hl_u[e]) * DD);
+                decide(e, zb);
+              }
+            }
+          }
+        } else {
+          // more open tests than the list holds: each thread decides its own hulls' drop test
+          for (int h = tid; h < nhull && !dropped; h += blockDim.x) {
+            const long long m = node_base + hull[h];
+            if (!st.ndead[m]) dropped = alu_le_ptr<D>(zc, st.nzone + m * DD, Lr, Ur);
+          }
+        }
       }
     } else {
       for (int k = clen0 + tid; k < clen && !dropped; k += blockDim.x) {
@@ -818,12 +962,21 @@ __device__ void merge_key_block(const NetView* nets, const InstState& is, const 
         if (m >= 0) dropped = alu_le_ptr<D>(zc, st.nzone + (long long)m * DD, Lr, Ur);
       }
     }
-    if (__syncthreads_or(dropped)) continue;
+    if (__syncthreads_or(dropped)) {
+      if (tid == 0) sh.hl_n = 0;   // the list is read by no one before the next survivor's barrier
+      continue;
+    }
     // (3): retire the zones s_q simulates
     int ret = 0;
     auto kill = [&](int k) {
       const int m = cl[k];
-      if (m >= 0) { st.ndead[m] = 1; cl[k] = -1; ++ret; }
+      if (m >= 0) {
+        st.ndead[m] = 1;
+        cl[k] = -1;
+        ++ret;
+        if (k >= clen - kRing) atomicAnd(&sh.lbits[(k & (kRing - 1)) >> 5], ~(1u << (k & 31)));
+        if (rel && k >= clen0) atomicAnd(&sh.ulive[(k - clen0) >> 5], ~(1u << ((k - clen0) & 31)));
+      }
     };
     if (rel) {
       const unsigned* row0 = r0 + (long long)q * r0w;
@@ -835,12 +988,16 @@ __device__ void merge_key_block(const NetView* nets, const InstState& is, const 
           const int p = tpos[w * 32 + __ffs(b) - 1];
           if (p >= 0) kill(clen0 + p);
         }
-      for (unsigned b = hmask; b; b &= b - 1) kill(clen0 + hull[tid + (__ffs(b) - 1) * (int)blockDim.x]);
-      for (int h = tid + 32 * (int)blockDim.x; h < nhull; h += blockDim.x) {
-        const int u = hull[h];
-        const long long m = node_base + u;
-        const bool live = !st.ndead[m];
-        if (alu_le_ptr<D>(st.nzone + m * DD, zc, Lr, Ur) && live) kill(clen0 + u);
+      if (nl <= kHullList) {
+        for (int e = tid; e < nl; e += blockDim.x)
+          if (sh.hl_f[e] & 4) kill(clen0 + sh.hl_u[e]);
+      } else {
+        for (int h = tid; h < nhull; h += blockDim.x) {
+          const int u = hull[h];
+          const long long m = node_base + u;
+          const bool live = !st.ndead[m];
+          if (alu_le_ptr<D>(st.nzone + m * DD, zc, Lr, Ur) && live) kill(clen0 + u);
+        }
       }
     } else {
       for (int k = tid; k < clen; k += blockDim.x) {
@@ -854,7 +1011,16 @@ __device__ void merge_key_block(const NetView* nets, const InstState& is, const 
       __syncthreads();
       if (warp == 0) {
         int nw = 0;
-        for (int top = clen - 1; top >= 0 && nw < kMergeScan; top -= 32) {
+        const int lo = clen > kRing ? clen - kRing : 0;   // positions [lo, clen): the liveness ring
+        for (int top = clen - 1; top >= lo && nw < kMergeScan; top -= 32) {
+          const int k = top - lane;
+          const bool live = k >= lo && ((sh.lbits[(k & (kRing - 1)) >> 5] >> (k & 31)) & 1u);
+          const unsigned b = __ballot_sync(0xffffffffu, live);
+          const int before = __popc(b & ((1u << lane) - 1u));
+          if (live && nw + before < kMergeScan) sh.win[nw + before] = k;
+          nw += __popc(b);
+        }
+        for (int top = lo - 1; top >= 0 && nw < kMergeScan; top -= 32) {
           const int k = top - lane;
           const bool live = k >= 0 && cl[k] >= 0;
           const unsigned b = __ballot_sync(0xffffffffu, live);
@@ -875,21 +1041,40 @@ __device__ void merge_key_block(const NetView* nets, const InstState& is, const 
       int mybest = 0x7fffffff;
       int hl[D];
       if (in_tile) {
-        for (int c = tile_idx; c < nw; c += ntiles) {
-          int za[D], zb[D];
+        // a tile-uniform read: a partner found at a lower index makes later candidates irrelevant
+        auto best_now = [&]() { return t.shfl(*(volatile int*)&sh.best, 0); };
+        auto node_of = [&](int k) { return k >= clen0 ? node_base + (k - clen0) : (long long)cl[k]; };
+        auto attempt = [&](int c, const int (&zb)[D]) {
+          int za[D];
 #pragma unroll
           for (int e = 0; e < D; ++e) za[e] = zc[t.i * D + e];
-          const int k = sh.win[c];
-          const long long m = k >= clen0 ? node_base + (k - clen0) : (long long)cl[k];
-          load_rows_rw(t, zb, st.nzone + m * DD);
-          if (try_union(t, za, zb)) {
-            mybest = c;
+          if (!try_union(t, za, zb)) return false;
+          mybest = c;
 #pragma unroll
-            for (int e = 0; e < D; ++e) hl[e] = za[e];
-            break;
+          for (int e = 0; e < D; ++e) hl[e] = za[e];
+          if (t.i == 0) atomicMin(&sh.best, c);
+          return true;
+        };
+        if constexpr (D <= 12) {
+          // a tile's two candidates (c0, c0 + ntiles) have their rows loaded together
+          for (int c0 = tile_idx; c0 < nw; c0 += 2 * ntiles) {
+            if (c0 > best_now()) break;
+            const int c1 = c0 + ntiles;
+            const bool has1 = c1 < nw;
+            int zb0[D], zb1[D];
+            load_rows_rw(t, zb0, st.nzone + node_of(sh.win[c0]) * DD);
+            if (has1) load_rows_rw(t, zb1, st.nzone + node_of(sh.win[c1]) * DD);
+            if (attempt(c0, zb0)) break;
+            if (has1 && c1 <= best_now() && attempt(c1, zb1)) break;
+          }
+        } else {
+          for (int c = tile_idx; c < nw; c += ntiles) {
+            if (c > best_now()) break;
+            int zb[D];
+            load_rows_rw(t, zb, st.nzone + node_of(sh.win[c]) * DD);
+            if (attempt(c, zb)) break;
           }
         }
-        if (t.i == 0 && mybest != 0x7fffffff) atomicMin(&sh.best, mybest);
       }
       __syncthreads();
       const int best = sh.best;
@@ -902,6 +1087,8 @@ __device__ void merge_key_block(const NetView* nets, const InstState& is, const 
         const int k = sh.win[best];
         st.ndead[cl[k]] = 1;
         cl[k] = -1;
+        if (k >= clen - kRing) sh.lbits[(k & (kRing - 1)) >> 5] &= ~(1u << (k & 31));
+        if (rel && k >= clen0) sh.ulive[(k - clen0) >> 5] &= ~(1u << ((k - clen0) & 31));
         --dlive;
         sh.unioned = 1;
       }
@@ -913,9 +1100,21 @@ __device__ void merge_key_block(const NetView* nets, const InstState& is, const 
     if (tid == 0) {
       node_meta(st, node, level, inst, hk, sc.pnode[a_s], sc.raw[a_s]);
       cl[clen] = (int)node;
+      sh.lbits[(clen & (kRing - 1)) >> 5] |= 1u << (clen & 31);   // the slot of position clen - kRing
+      sh.hl_n = 0;
       if (rel) {
-        if (sh.unioned) hull[sh.nhull++] = clen - clen0;
-        else tpos[q] = clen - clen0;
+        const int u = clen - clen0;
+        sh.ulive[u >> 5] |= 1u << (u & 31);
+        if (sh.unioned) {
+          const int h = sh.nhull++;
+          hull[h] = u;
+          if (h < MergeShared<D>::kHC) {
+            sh.hpos[h] = u;
+            for (int y = 0; y < D; ++y) sh.hcol[h * D + y] = zc[y * D];
+          }
+        } else {
+          tpos[q] = u;
+        }
       }
       sh.clen = clen + 1;
       ++dlive;
