@@ -474,12 +474,15 @@ def run_batched(args):
 
 
 def serving_run(rate: float, duration: float, drain: float, budget_gb: float, inflight: int,
-                serve_config: int = 3) -> dict:
+                serve_config: int = 3, per_request_gb: float = 0.25, max_queued: int = 64) -> dict:
     """Config 5: Poisson arrivals of requests drawn from the config-3 distribution at `rate` per
-    second for `duration` seconds, admitted continuously by the server's device-memory pool; after
-    `drain` more seconds the server is destroyed (cancelling what still runs). Time to verdict runs
-    from submission to result; percentiles are over every offered request, those without a verdict
-    counted as beyond the run."""
+    second for `duration` seconds into the serving queue: admitted continuously while one of
+    `inflight` slots is free and the `budget_gb` pool holds the request's store reservation; a request
+    whose store outgrows `per_request_gb` stops with HORA_E_BUDGET (so every admitted request ends in
+    bounded time), and a submission that finds `max_queued` requests waiting is rejected at once.
+    Time to verdict runs from submission to result. After the arrivals the queue drains (at most
+    `drain` seconds). Percentiles of time to outcome are over every accepted request (verdict or
+    stopped at its limit), those of time to verdict over the requests with a verdict."""
     import ctypes
     import random
     from ptctcl_gb300 import capi
@@ -488,12 +491,13 @@ def serving_run(rate: float, duration: float, drain: float, budget_gb: float, in
     lib = capi.load()
     srv = ctypes.c_void_p()
     capi.check(lib.hora_gb_server_create(int(budget_gb * (1 << 30)), inflight, ctypes.byref(srv)), "server")
+    capi.check(lib.hora_gb_server_set_limits(srv, int(per_request_gb * (1 << 30)), max_queued), "server_limits")
     rng = random.Random(5)
     # up to 2000 distinct requests, offered in turn (descriptors built before the clock)
     reqs = [config_instance(serve_config, 100000 + k) for k in range(min(2000, int(rate * duration * 1.5) + 16))]
     descs = [(NetArrays(n), QueryArrays(kd, p, q)) for n, kd, p, q in reqs]
     t0 = time.perf_counter()
-    tickets, k, next_t = [], 0, 0.0
+    tickets, k, next_t, rejected = {}, 0, 0.0, 0
     while True:
         now = time.perf_counter() - t0
         if now >= duration:
@@ -501,15 +505,19 @@ def serving_run(rate: float, duration: float, drain: float, budget_gb: float, in
         if now >= next_t:
             na, qa = descs[k % len(descs)]
             tk = ctypes.c_int64(0)
-            if lib.hora_gb_server_submit(srv, ctypes.addressof(na.desc), ctypes.addressof(qa.desc),
-                                         ctypes.byref(tk)) == capi.OK:
-                tickets.append(tk.value)
+            rc = lib.hora_gb_server_submit(srv, ctypes.addressof(na.desc), ctypes.addressof(qa.desc), ctypes.byref(tk))
+            if rc == capi.OK:
+                tickets[tk.value] = k % len(descs)
+            elif rc == capi.E_BUDGET:
+                rejected += 1
             k += 1
             next_t += rng.expovariate(rate)
         else:
             time.sleep(min(0.002, next_t - now))
     submitted = time.perf_counter() - t0
-    pending, lat, gen, done, stopped = set(tickets), [], 0, 0, 0
+    pending, lat, out_t, gen, stopped, failed = set(tickets), [], [], 0, 0, 0
+    verdict_of = {}
+    t_last = submitted
     active = ctypes.c_int32(1)
     while pending and time.perf_counter() - t0 < duration + drain:
         lib.hora_gb_server_step(srv, ctypes.byref(active))
@@ -521,28 +529,92 @@ def serving_run(rate: float, duration: float, drain: float, budget_gb: float, in
             if d.value:
                 pending.discard(tk)
                 gen += st.generated
+                t_last = time.perf_counter() - t0
+                out_t.append(st.seconds)
                 if st.status == capi.OK:
-                    done += 1
                     lat.append(st.seconds)
+                    verdict_of[tk] = v.value
+                elif st.status == capi.E_BUDGET:
+                    stopped += 1
                 else:
-                    stopped += 1   # needed more than the pool had left (HORA_E_BUDGET) or failed
+                    failed += 1
     total = time.perf_counter() - t0
     lib.hora_gb_server_destroy(srv)
-    xs = sorted(lat) + [float("inf")] * (len(tickets) - len(lat))
-    p50, p99 = percentile(xs, 50), percentile(xs, 99)
-    return {"workload": f"config{serve_config} requests, Poisson {rate:g}/s for {duration:.0f} s, "
-            f"pool {budget_gb:g} GB, {inflight} in flight, {drain:.0f} s drain",
-            "offered": len(tickets), "verdicts": done, "stopped_over_budget": stopped,
-            "unfinished": len(pending), "value": gen / total, "unit": UNIT,
-            "p50_time_to_verdict_s": None if p50 in (None, float("inf")) else p50,
-            "p99_time_to_verdict_s": None if p99 in (None, float("inf")) else p99,
-            "p99_beyond_run": p99 == float("inf"), "seconds": total, "submit_seconds": submitted}
+    xs = sorted(out_t) + [float("inf")] * len(pending)
+    o50, o99 = percentile(xs, 50), percentile(xs, 99)
+    rec = {"workload": f"config{serve_config} requests, Poisson {rate:g}/s for {duration:.0f} s, "
+           f"pool {budget_gb:g} GB, {inflight} in flight, {per_request_gb:g} GB per request, "
+           f"at most {max_queued} waiting",
+           "offered": k, "accepted": len(tickets), "rejected_at_submit": rejected,
+           "verdicts": len(lat), "stopped_at_request_limit": stopped, "failed": failed,
+           "unfinished": len(pending), "value": gen / max(1e-9, t_last), "unit": UNIT,
+           "p50_time_to_verdict_s": percentile(lat, 50), "p99_time_to_verdict_s": percentile(lat, 99),
+           "p50_time_to_outcome_s": None if o50 in (None, float("inf")) else o50,
+           "p99_time_to_outcome_s": None if o99 in (None, float("inf")) else o99,
+           "seconds": total, "last_result_s": t_last, "submit_seconds": submitted}
+    rec["_verdicts"] = {tickets[tk]: v for tk, v in verdict_of.items()}
+    return rec
+
+
+def serving_plain(budget_gb: float, per_request_gb: float, seconds: float, serve_config: int = 3,
+                  served=None) -> dict:
+    """The plain single-instance form on the serving workload: the same request sequence run one at a
+    time (one slot, the same per-request store limit) for `seconds`; its verdicts are compared with
+    those the served runs gave for the same requests."""
+    from ptctcl_gb300 import capi, engine
+    from ptctcl_gb300.generator import config_instance
+    gen, done, stopped, agree, compared = 0, 0, 0, 0, 0
+    t0 = time.perf_counter()
+    busy = 0.0
+    k = 0
+    with engine.Server(budget_bytes=int(budget_gb * (1 << 30)), max_inflight=1,
+                       per_request_bytes=int(per_request_gb * (1 << 30))) as srv:
+        while time.perf_counter() - t0 < seconds:
+            it = config_instance(serve_config, 100000 + k)
+            t = time.perf_counter()
+            tk = srv.submit(*it)
+            while True:
+                r = srv.poll(tk)
+                if r is not None:
+                    break
+                srv.active()
+            busy += time.perf_counter() - t
+            v, st = r
+            gen += st["generated"]
+            if st["status"] == capi.OK:
+                done += 1
+                for sv in served or ():
+                    if k in sv:
+                        compared += 1
+                        agree += sv[k] == v
+            else:
+                stopped += 1
+            k += 1
+    return {"workload": f"config{serve_config} requests one at a time, {per_request_gb:g} GB per request",
+            "requests": k, "verdicts": done, "stopped_at_request_limit": stopped,
+            "value": gen / max(1e-9, busy), "unit": UNIT, "seconds": busy,
+            "verdicts_compared_with_served": compared, "verdicts_agree": agree == compared}
+
+
+def serving_sweep(rates, duration: float, drain: float, budget_gb: float, inflight: int, serve_config: int,
+                  per_request_gb: float, max_queued: int, plain_seconds: float) -> dict:
+    runs = [serving_run(r, duration, drain, budget_gb, inflight, serve_config, per_request_gb, max_queued)
+            for r in rates]
+    served = [r.pop("_verdicts") for r in runs]
+    out = {"loads": runs}
+    if plain_seconds > 0:
+        plain = serving_plain(budget_gb, per_request_gb, plain_seconds, serve_config, served)
+        out["plain_one_at_a_time"] = plain
+        for r in runs:
+            r["vs_plain"] = r["value"] / max(1e-12, plain["value"])
+    return out
 
 
 def run_serving(args):
     rates = [float(r) for r in args.rates.split(",")] if args.rates else [args.rate]
-    line = {"metric": METRIC, "serving": [serving_run(r, args.duration, args.drain, args.budget_gb, args.inflight,
-                                                      args.serve_config) for r in rates]}
+    line = {"metric": METRIC, "serving": serving_sweep(rates, args.duration, args.drain, args.budget_gb, args.inflight,
+                                                       args.serve_config, args.per_request_gb, args.max_queued,
+                                                       args.duration)}
     print(json.dumps(line), flush=True)
 
 
@@ -567,6 +639,10 @@ def main():
     ap.add_argument("--drain", type=float, default=120.0)
     ap.add_argument("--budget-gb", type=float, default=64.0)
     ap.add_argument("--inflight", type=int, default=64)
+    ap.add_argument("--per-request-gb", type=float, default=0.25,
+                    help="serving: a request whose store outgrows this stops with HORA_E_BUDGET")
+    ap.add_argument("--max-queued", type=int, default=64,
+                    help="serving: submissions that find this many requests waiting are rejected")
     ap.add_argument("--serve-config", type=int, default=3)
     ap.add_argument("--batched-budget", type=float, default=20.0,
                     help="seconds per form of the config-4 batched-vs-plain comparison added to the default "
@@ -666,8 +742,9 @@ def main():
     if seeds3 and world == 1:
         line["config3"] = [leadsto_record(sd, 0.0 if (args.no_cpu_baseline or k) else 60.0) for k, sd in enumerate(seeds3)]
     if args.serving_seconds > 0 and world == 1:
-        line["serving"] = [serving_run(r, args.serving_seconds, 2 * args.serving_seconds, args.budget_gb,
-                                       args.inflight) for r in (100.0, 1000.0)]
+        line["serving"] = serving_sweep((100.0, 1000.0, 5000.0), args.serving_seconds, 4 * args.serving_seconds,
+                                        args.budget_gb, args.inflight, 3, args.per_request_gb, args.max_queued,
+                                        args.serving_seconds)
     print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()

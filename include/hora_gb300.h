@@ -303,8 +303,14 @@ typedef struct hora_server hora_server;
  * reservation; while it runs its stores stay resident across BFS levels and grow by taking more from
  * the pool; a request whose store needs more than the pool has left stops with status HORA_E_BUDGET. */
 HORA_GB_API int32_t hora_gb_server_create(uint64_t budget_bytes, int32_t max_inflight, hora_server** out);
+/* Bounds a request's stores and the queue; call before the first submit (defaults: 0, 0 = no limit).
+ * per_request_bytes: a request whose store outgrows this stops with status HORA_E_BUDGET, so every
+ * admitted request ends in bounded time whatever its state space; max_queued: a submission that finds
+ * this many requests waiting for admission is rejected with HORA_E_BUDGET (reject rather than queue). */
+HORA_GB_API int32_t hora_gb_server_set_limits(hora_server* s, uint64_t per_request_bytes, int32_t max_queued);
 /* Queue a request; the descriptors are copied. *ticket identifies it. A request whose initial
- * reservation exceeds the whole pool is rejected with HORA_E_BUDGET. */
+ * reservation exceeds the whole pool, or that finds the queue full (hora_gb_server_set_limits), is
+ * rejected with HORA_E_BUDGET. */
 HORA_GB_API int32_t hora_gb_server_submit(hora_server* s, const hora_net_desc* net, const hora_query_desc* q,
                               int64_t* ticket);
 /* The worker threads admit and run requests on their own; this waits up to 1 ms for progress and sets

@@ -20,7 +20,7 @@ EXPORTS = (
     "hora_gb_exists_invariant_trace", "hora_gb_expand",
     "hora_gb_has_deadlock",
     "hora_gb_batch_run", "hora_gb_server_create", "hora_gb_server_submit", "hora_gb_server_step",
-    "hora_gb_server_poll", "hora_gb_server_destroy", "hora_gb_has_deadlock_noalloc",
+    "hora_gb_server_poll", "hora_gb_server_destroy", "hora_gb_server_set_limits", "hora_gb_has_deadlock_noalloc",
     "hora_gb_open", "hora_gb_run", "hora_gb_trace", "hora_gb_close",
 )
 
@@ -83,6 +83,8 @@ def load(build_if_missing: bool = True):
     L.hora_gb_server_create.restype = I32
     L.hora_gb_server_submit.argtypes = [VP, VP, VP, ctypes.POINTER(I64)]
     L.hora_gb_server_submit.restype = I32
+    L.hora_gb_server_set_limits.argtypes = [VP, U64, I32]
+    L.hora_gb_server_set_limits.restype = I32
     L.hora_gb_server_step.argtypes = [VP, ctypes.POINTER(I32)]
     L.hora_gb_server_step.restype = I32
     L.hora_gb_server_poll.argtypes = [VP, I64, ctypes.POINTER(I32), ctypes.POINTER(I32), VP]

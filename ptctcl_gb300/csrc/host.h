@@ -12,17 +12,27 @@
 namespace hgb {
 
 // Device memory shared by the requests of a server: each request's store starts from the reservation
-// it was admitted with and grows level by level while the pool has room (BudgetPool::take).
+// it was admitted with and grows level by level while the pool has room (BudgetPool::take). A pool
+// with a parent is one request's limit inside the server's pool: a take must fit both.
 struct BudgetPool {
   std::atomic<uint64_t> used{0};
   uint64_t cap = 0;
+  BudgetPool* parent = nullptr;
   bool take(uint64_t b) {
     uint64_t u = used.load();
-    while (u + b <= cap)
-      if (used.compare_exchange_weak(u, u + b)) return true;
+    while (u + b <= cap) {
+      if (used.compare_exchange_weak(u, u + b)) {
+        if (!parent || parent->take(b)) return true;
+        used.fetch_sub(b);
+        return false;
+      }
+    }
     return false;
   }
-  void give(uint64_t b) { used.fetch_sub(b); }
+  void give(uint64_t b) {
+    used.fetch_sub(b);
+    if (parent) parent->give(b);
+  }
 };
 
 

@@ -6,8 +6,9 @@
 // stream, so requests admitted while others run overlap with them on the device and a short request
 // is not held back by a long one. A running request's passed/waiting stores stay resident across its
 // BFS levels and grow by taking more from the shared pool; a request whose store needs more than the
-// pool has left stops with HORA_E_BUDGET. Destroying the server cancels the running requests at their
-// next level.
+// pool has left, or more than the server's per-request limit, stops with HORA_E_BUDGET. With a bounded
+// queue, a request that arrives while the queue is full is rejected at submission. Destroying the
+// server cancels the running requests at their next level.
 #include <cuda_runtime.h>
 
 #include <chrono>
@@ -33,6 +34,7 @@ struct Request {
   int done = 0;
   int verdict = -1;
   hora_stats st{};
+  BudgetPool limit;   // the request's growth beyond its reservation, inside the server's pool
   std::chrono::steady_clock::time_point t_submit;
 };
 
@@ -44,6 +46,8 @@ struct hora_server {
   hgb::BudgetPool pool;                // device memory of the admitted requests' stores
   int max_inflight = 0;
   int inflight = 0;
+  uint64_t per_request = 0;            // a request's store may hold at most this much (0: no limit)
+  int32_t max_queued = 0;              // submissions past this many waiting requests are rejected (0: none)
   int64_t next_ticket = 1;
   std::deque<std::unique_ptr<hgb::Request>> queue;
   std::set<int64_t> running;
@@ -64,7 +68,8 @@ static uint64_t reserve_bytes(const hora_server* s, const hora_net_desc* n) {
   const uint64_t d = (uint64_t)n->nclocks + 1;
   const uint64_t floor_bytes = (1ull << 16) * (d * d * 4 + 32) * 2;
   const uint64_t slice = s->pool.cap / (uint64_t)(4 * s->max_inflight);
-  return slice > floor_bytes ? slice : floor_bytes;
+  const uint64_t r = slice > floor_bytes ? slice : floor_bytes;
+  return s->per_request && r > s->per_request ? s->per_request : r;
 }
 
 static void worker_main(hora_server* s) {
@@ -86,7 +91,14 @@ static void worker_main(hora_server* s) {
     }
     int32_t verdict = -1;
     hora_stats st{};
-    const int rc = run_batch(1, &r->net.d, &r->net.q, &verdict, &st, &s->cancel, (size_t)r->est_bytes, &s->pool);
+    BudgetPool* grow = &s->pool;
+    if (s->per_request) {
+      // growth past the reservation must fit both the request's limit and the server's pool
+      r->limit.cap = s->per_request > r->est_bytes ? s->per_request - r->est_bytes : 0;
+      r->limit.parent = &s->pool;
+      grow = &r->limit;
+    }
+    const int rc = run_batch(1, &r->net.d, &r->net.q, &verdict, &st, &s->cancel, (size_t)r->est_bytes, grow);
     const auto now = std::chrono::steady_clock::now();
     {
       std::lock_guard<std::mutex> g(s->mu);
@@ -124,12 +136,18 @@ int32_t hora_gb_server_create(uint64_t budget_bytes, int32_t max_inflight, hora_
 
 int32_t hora_gb_server_submit(hora_server* s, const hora_net_desc* net, const hora_query_desc* q, int64_t* ticket) {
   if (!s || !net || !q || !ticket) return HORA_E_INVALID;
-  const uint64_t est = reserve_bytes(s, net);
+  const auto t_arrive = std::chrono::steady_clock::now();
+  uint64_t est = 0;
+  {
+    std::lock_guard<std::mutex> g(s->mu);
+    if (s->max_queued > 0 && (int64_t)s->queue.size() >= s->max_queued) return HORA_E_BUDGET;   // queue full
+    est = reserve_bytes(s, net);
+  }
   if (est > s->pool.cap) return HORA_E_BUDGET;
   auto r = std::make_unique<Request>();
   r->net.copy(net, q);
   r->est_bytes = est;
-  r->t_submit = std::chrono::steady_clock::now();
+  r->t_submit = t_arrive;
   {
     std::lock_guard<std::mutex> g(s->mu);
     r->ticket = s->next_ticket++;
@@ -137,6 +155,14 @@ int32_t hora_gb_server_submit(hora_server* s, const hora_net_desc* net, const ho
     s->queue.push_back(std::move(r));
   }
   s->cv.notify_all();
+  return HORA_OK;
+}
+
+int32_t hora_gb_server_set_limits(hora_server* s, uint64_t per_request_bytes, int32_t max_queued) {
+  if (!s || max_queued < 0) return HORA_E_INVALID;
+  std::lock_guard<std::mutex> g(s->mu);
+  s->per_request = per_request_bytes;
+  s->max_queued = max_queued;
   return HORA_OK;
 }
 

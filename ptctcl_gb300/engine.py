@@ -321,14 +321,19 @@ class Server:
     """The serving form (hora_gb_server_*): requests are queued and admitted in arrival order while
     at most `max_inflight` run and the `budget_bytes` pool holds their initial store reservation;
     each runs on its own worker and stream, its stores growing from the pool level by level.
+    `per_request_bytes` (0: none) bounds one request's store -- past it the request stops with
+    HORA_E_BUDGET; `max_queued` (0: none) rejects a submission that finds that many requests waiting.
     `poll` returns (verdict, stats dict) once a ticket is done (the result is then released), else
     None; closing cancels what still runs."""
 
-    def __init__(self, budget_bytes: int, max_inflight: int):
+    def __init__(self, budget_bytes: int, max_inflight: int, per_request_bytes: int = 0, max_queued: int = 0):
         self._lib = capi.load()
         self._h = ctypes.c_void_p()
         capi.check(self._lib.hora_gb_server_create(int(budget_bytes), int(max_inflight), ctypes.byref(self._h)),
                    "server_create")
+        if per_request_bytes or max_queued:
+            capi.check(self._lib.hora_gb_server_set_limits(self._h, int(per_request_bytes), int(max_queued)),
+                       "server_set_limits")
 
     def submit(self, net: Network, kind: int, p: Pred, q: Optional[Pred] = None) -> int:
         na, qa = NetArrays(net), QueryArrays(kind, p, q)

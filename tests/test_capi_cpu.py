@@ -57,6 +57,8 @@ def test_invalid_and_unsupported_inputs_are_rejected_without_a_device():
     rc = lib.hora_gb_deadlock_reachable(ctypes.addressof(na3.desc), capi.BACKEND_CUDA, ctypes.byref(st), None,
                                         ctypes.byref(res))
     assert rc == capi.E_NOT_SUPPORTED
+    # the serving form's limits need a server
+    assert lib.hora_gb_server_set_limits(None, 1 << 30, 4) == capi.E_INVALID
 
 
 @pytest.mark.skipif(capi.device_count() > 0, reason="needs a machine without a CUDA device")

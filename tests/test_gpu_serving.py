@@ -1,8 +1,9 @@
 """The batched and serving forms on the GPU: every request's verdict and counts are the same
 whether it runs alone, in a batch, or through the request queue mixed with other requests; a
 cancelled batch reports its unfinished instances as cancelled; the queue rejects a request whose
-initial reservation exceeds the whole pool, grows a running request's store from the pool, reports
-a result once, and cancels running requests when it is destroyed."""
+initial reservation exceeds the whole pool, grows a running request's store from the pool, stops a
+request at its per-request limit while others in the same server finish, rejects submissions once the
+queue is full, reports a result once, and cancels running requests when it is destroyed."""
 import ctypes
 
 import pytest
@@ -122,6 +123,49 @@ def test_server_store_grows_from_the_pool():
         srv.drain(timeout=300)
         v, st = srv.poll(t)
     assert st["status"] == capi.E_BUDGET and v == -1
+
+
+def test_server_per_request_limit_stops_only_the_large_request():
+    """With a large pool but a per-request limit of a few reservations, the large request stops with
+    HORA_E_BUDGET while a small request served beside it gets the batched form's verdict and
+    counts."""
+    small = config_instance(2, 23)
+    (sv,), (sst,) = engine.batch_run([small])
+    big = config_instance(2, 2483)                   # 1.45M stored zones
+    d = big[0].dim
+    floor = (1 << 16) * (d * d * 4 + 32) * 2
+    with engine.Server(budget_bytes=16 << 30, max_inflight=4, per_request_bytes=4 * floor) as srv:
+        tb = srv.submit(*big)
+        ts = srv.submit(*small)
+        srv.drain(timeout=300)
+        bv, bst = srv.poll(tb)
+        v, st = srv.poll(ts)
+    assert bst["status"] == capi.E_BUDGET and bv == -1
+    assert st["status"] == capi.OK and v == sv
+    for c in COUNTS:
+        assert st[c] == sst[c], c
+
+
+def test_server_rejects_when_the_queue_is_full():
+    """One slot, at most one waiting request: of five submissions made while a long request runs, at
+    most two are accepted (the running one and one waiting) and the rest are rejected at once."""
+    import time
+    big = config_instance(3, 0)                      # runs for seconds
+    srv = engine.Server(budget_bytes=8 << 30, max_inflight=1, max_queued=1)
+    try:
+        accepted, rejected = 0, 0
+        for _ in range(5):
+            try:
+                srv.submit(*big)
+                accepted += 1
+            except capi.HoraError as e:
+                assert e.code == capi.E_BUDGET
+                rejected += 1
+        assert 1 <= accepted <= 2 and rejected == 5 - accepted
+        t = time.perf_counter()
+    finally:
+        srv.close()
+    assert time.perf_counter() - t < 10.0
 
 
 def test_server_destroy_cancels_running_requests():
