@@ -269,8 +269,14 @@ HORA_GB_API int32_t hora_gb_has_deadlock_noalloc(const hora_net_desc* net, int32
  *     transitions whose integer guards and committed rules hold, in emission order, whether or not
  *     their zone is empty); zones[i] is the stored zone, which contains the exact successor of
  *     zones[i-1] by that transition (it may be extrapolated, or a convex union); *loop_to = -1.
- *     *nsteps = 0 when the goal was not reached, and for a leads-to violation found only by the
- *     backward sweep (its witness is a cycle of the subsumed graph, not recorded).
+ *     *nsteps = 0 when the goal was not reached;
+ *   a leads-to violation found by the backward sweep: the same path of the passed store to the
+ *     p-state a surviving root was cut from, then the root (ords = -2: that state restricted to p and
+ *     !q, no transition), then a path of the !q graph through nodes whose fixpoint value is not empty,
+ *     each step's zone containing the exact successor of the previous one in the network restricted
+ *     to !q, ending at a node with a stop set (a whole zone where time may diverge inside !q
+ *     preferred, else one holding deadlocked valuations) or closing a cycle back to step *loop_to by
+ *     transition *loop_ord.
  * A handle that has not run returns HORA_E_INVALID. A handle is used by one thread at a time. */
 typedef struct hora_handle_s* hora_handle;
 HORA_GB_API int32_t hora_gb_open(const hora_net_desc* net, const hora_query_desc* q, hora_handle* out);

@@ -2070,6 +2070,44 @@ static int stop_fed(Model* m, const hora_pred_desc* q, const int32_t* locs, cons
   return whole;
 }
 
+/* Leads-to phase 2 for one state, for replaying a counterexample trace: the restricted model (the
+ * network restricted to !q, !q adjoined to the invariants as close_succ_zone adjoins it). */
+static int lt_model(const hora_net_desc* net, const hora_pred_desc* q, Model* m) {
+  if (model_build(net, m)) return 0;
+  m->avoid = q;
+  m->avoid_psi = 0;
+  if (q->nclk == 1) {
+    m->avoid_neg[0] = q->clk_cond[1]; m->avoid_neg[1] = q->clk_cond[0]; m->avoid_neg[2] = r_negate(q->clk_cond[2]);
+  }
+  return 1;
+}
+int32_t orc_lt_successor_raw(const hora_net_desc* net, const hora_pred_desc* q, const uint8_t* qmask,
+                             const int32_t* locs, const int32_t* ints, const int32_t* zone, int32_t raw,
+                             int32_t* out_locs, int32_t* out_ints, int32_t* out_zone) {
+  Model m;
+  if (!lt_model(net, q, &m)) { model_free(&m); return 0; }
+  uint8_t qm[64] = {0};
+  if (qmask) memcpy(qm, qmask, (size_t)m.dim);
+  RawCtx x = {raw, 0, net->nprocs, net->nints, m.dim * m.dim, out_locs, out_ints, out_zone};
+  successors(&m, locs, ints, zone, m.L, m.U, qm, 0, raw_emit, &x);
+  model_free(&m);
+  return x.hit;
+}
+int32_t orc_lt_stop(const hora_net_desc* net, const hora_pred_desc* q, const uint8_t* qmask,
+                    const int32_t* locs, const int32_t* ints, const int32_t* zone) {
+  Model m;
+  if (!lt_model(net, q, &m)) { model_free(&m); return -1; }
+  uint8_t qm[64] = {0};
+  if (qmask) memcpy(qm, qmask, (size_t)m.dim);
+  Fed f;
+  fed_init(&f, m.dim * m.dim);
+  const int whole = stop_fed(&m, q, locs, ints, zone, qm, &f);
+  const int32_t r = whole ? 2 : f.n > 0 ? 1 : 0;
+  fed_free(&f);
+  model_free(&m);
+  return r;
+}
+
 /* The early witness of p --> q at a reachable zone (leadsto_witness, construction.cpp:786-826): its
  * p-part, cut to !q, holds a valuation where a maximal !q-run may stop (Stop above) -- that run
  * never meets q, so the property is violated. m->avoid is set for the test only (phase 1 explores

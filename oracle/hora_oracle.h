@@ -63,6 +63,13 @@ int32_t orc_has_deadlock(const hora_net_desc* net, int32_t n, const int32_t* loc
  * out buffers filled when it is non-empty, else 0. The step check of the forward routes' traces. */
 int32_t orc_successor_raw(const hora_net_desc* net, const uint8_t* qmask, const int32_t* locs, const int32_t* ints,
                           const int32_t* zone, int32_t raw, int32_t* out_locs, int32_t* out_ints, int32_t* out_zone);
+/* Leads-to phase 2 (the network restricted to !q): the successor by transition index raw (0: none),
+ * and the stop set of a state's zone (0 empty, 1 its deadlocked valuations, 2 the whole zone). */
+int32_t orc_lt_successor_raw(const hora_net_desc* net, const hora_pred_desc* q, const uint8_t* qmask,
+                             const int32_t* locs, const int32_t* ints, const int32_t* zone, int32_t raw,
+                             int32_t* out_locs, int32_t* out_ints, int32_t* out_zone);
+int32_t orc_lt_stop(const hora_net_desc* net, const hora_pred_desc* q, const uint8_t* qmask,
+                    const int32_t* locs, const int32_t* ints, const int32_t* zone);
 
 /* ---- whole queries (level-synchronous BFS in the canonical order the engine uses) ---- */
 int32_t orc_reachable_net(const hora_net_desc* net, const hora_pred_desc* target, hora_stats* st,

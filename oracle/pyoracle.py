@@ -64,6 +64,10 @@ def lib():
         L.orc_set_time_limit.restype = None
         L.orc_successor_raw.argtypes = [VP, ctypes.POINTER(ctypes.c_uint8), P32, P32, P32, I32, P32, P32, P32]
         L.orc_successor_raw.restype = I32
+        L.orc_lt_successor_raw.argtypes = [VP, VP, ctypes.POINTER(ctypes.c_uint8), P32, P32, P32, I32, P32, P32, P32]
+        L.orc_lt_successor_raw.restype = I32
+        L.orc_lt_stop.argtypes = [VP, VP, ctypes.POINTER(ctypes.c_uint8), P32, P32, P32]
+        L.orc_lt_stop.restype = I32
         L.orc_set_threads.argtypes = [I32]
         L.orc_set_threads.restype = I32
     return _lib
@@ -216,6 +220,41 @@ def successor_raw(net: Network, locs, ints, zone, raw: int, qmask=None):
     if not ok:
         return None
     return ol[:np_], oi[:ni], oz.reshape(d, d)
+
+
+def lt_successor_raw(net: Network, q: Pred, locs, ints, zone, raw: int, qmask=None):
+    """Leads-to phase 2: the successor by transition index `raw` in the network restricted to !q
+    (!q adjoined to the invariants), or None when that transition yields nothing."""
+    na, qa = NetArrays(net), PredArrays(q)
+    np_, ni, d = len(net.procs), len(net.ints), net.dim
+    l = np.ascontiguousarray(locs, np.int32).reshape(-1)
+    i = np.ascontiguousarray(ints, np.int32).reshape(-1) if ni else np.zeros(1, np.int32)
+    z = np.ascontiguousarray(zone, np.int32).reshape(-1)
+    qm = np.zeros(64, np.uint8)
+    if qmask is not None:
+        qm[:len(qmask)] = np.asarray(qmask, np.uint8)
+    ol, oi, oz = np.zeros(max(np_, 1), np.int32), np.zeros(max(ni, 1), np.int32), np.zeros(d * d, np.int32)
+    ok = lib().orc_lt_successor_raw(ctypes.addressof(na.desc), ctypes.addressof(qa.desc),
+                                    qm.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)),
+                                    _p(l), _p(i), _p(z), int(raw), _p(ol), _p(oi), _p(oz))
+    if not ok:
+        return None
+    return ol[:np_], oi[:ni], oz.reshape(d, d)
+
+
+def lt_stop(net: Network, q: Pred, locs, ints, zone, qmask=None) -> int:
+    """Leads-to phase 2: the stop set of a state's zone -- 0 empty, 1 its deadlocked valuations,
+    2 the whole zone."""
+    na, qa = NetArrays(net), PredArrays(q)
+    ni = len(net.ints)
+    l = np.ascontiguousarray(locs, np.int32).reshape(-1)
+    i = np.ascontiguousarray(ints, np.int32).reshape(-1) if ni else np.zeros(1, np.int32)
+    z = np.ascontiguousarray(zone, np.int32).reshape(-1)
+    qm = np.zeros(64, np.uint8)
+    if qmask is not None:
+        qm[:len(qmask)] = np.asarray(qmask, np.uint8)
+    return int(lib().orc_lt_stop(ctypes.addressof(na.desc), ctypes.addressof(qa.desc),
+                                 qm.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)), _p(l), _p(i), _p(z)))
 
 
 def initial_state(net: Network, qmask=None):

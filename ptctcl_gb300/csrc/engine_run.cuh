@@ -1106,6 +1106,133 @@ struct Engine {
     if ((rc = read_ctl())) return rc;
     gfp_iters = rounds;
     pre_calls = npre;
+    if (o.trace && ninst == 1 && nets[0]->kind == HORA_Q_LEADSTO) return sweep_trace(n2, ne, fx);
+    return HORA_OK;
+  }
+
+  // Counterexample of p --> q decided by the sweep: a root whose W is not empty, reached from the
+  // initial state by the creation path of the phase-1 node whose p-part it is, then a path of the !q
+  // graph through nodes whose W is not empty -- to the nearest node whose whole zone is a stop set,
+  // else to the nearest node with a stop set, else around a cycle (every node of W without a stop set
+  // has an edge into W, by the fixpoint). Steps: the phase-1 path (ords = transition index, the
+  // initial state -1), the root (ords = -2: the previous state cut to p and !q, no transition), the
+  // !q path (ords = the edge's transition index); loop_to / loop_ord close a cycle.
+  int sweep_trace(long long n2, long long ne, const Fix& fx) {
+    Trace& T = *o.trace;
+    T = Trace{};
+    if (n2 <= 0) return HORA_OK;
+    std::vector<int> wc((size_t)n2), sw((size_t)n2), sh((size_t)n2), lev((size_t)n2), es((size_t)ne), ed((size_t)ne),
+        er((size_t)ne);
+    std::vector<unsigned long long> key((size_t)n2);
+    HGB_CUDA(cudaMemcpyAsync(wc.data(), fx.wcnt, n2 * 4, cudaMemcpyDeviceToHost, s));
+    HGB_CUDA(cudaMemcpyAsync(sw.data(), fx.swhole, n2 * 4, cudaMemcpyDeviceToHost, s));
+    HGB_CUDA(cudaMemcpyAsync(sh.data(), fx.shead, n2 * 4, cudaMemcpyDeviceToHost, s));
+    HGB_CUDA(cudaMemcpyAsync(lev.data(), S[1].nlevel.p, n2 * 4, cudaMemcpyDeviceToHost, s));
+    HGB_CUDA(cudaMemcpyAsync(key.data(), S[1].nkey.p, n2 * 8, cudaMemcpyDeviceToHost, s));
+    if (ne > 0) {
+      HGB_CUDA(cudaMemcpyAsync(es.data(), esrc.p, ne * 4, cudaMemcpyDeviceToHost, s));
+      HGB_CUDA(cudaMemcpyAsync(ed.data(), edst.p, ne * 4, cudaMemcpyDeviceToHost, s));
+      HGB_CUDA(cudaMemcpyAsync(er.data(), eraw.p, ne * 4, cudaMemcpyDeviceToHost, s));
+    }
+    HGB_CUDA(wait());
+    d2h += (size_t)n2 * 24 + (size_t)ne * 12;
+    int root = -1;
+    for (long long u = 0; u < n2 && root < 0; ++u)
+      if (wc[u] > 0 && lev[u] == 0) root = (int)u;
+    if (root < 0) return HORA_OK;   // holds
+    std::vector<long long> off((size_t)n2 + 1, 0);   // edges by source
+    for (long long e = 0; e < ne; ++e) off[es[e] + 1]++;
+    for (long long u = 0; u < n2; ++u) off[u + 1] += off[u];
+    std::vector<long long> fill(off.begin(), off.end() - 1), byu((size_t)std::max<long long>(ne, 1));
+    for (long long e = 0; e < ne; ++e) byu[fill[es[e]]++] = e;
+    // breadth-first over the nodes of W from the root; the nearest whole stop set, else any stop set
+    std::vector<long long> via((size_t)n2, -2);   // edge that reached the node (-1: the root)
+    std::vector<int> q{root};
+    via[root] = -1;
+    int goal_whole = -1, goal_part = -1;
+    for (size_t h = 0; h < q.size() && goal_whole < 0; ++h) {
+      const int u = q[h];
+      if (sw[u]) { goal_whole = u; break; }
+      if (sh[u] >= 0 && goal_part < 0) goal_part = u;
+      for (long long k = off[u]; k < off[u + 1]; ++k) {
+        const long long e = byu[k];
+        const int v = ed[e];
+        if (wc[v] > 0 && via[v] == -2) { via[v] = e; q.push_back(v); }
+      }
+    }
+    std::vector<int> path;        // !q graph nodes from the root
+    std::vector<int> praw;        // transition index into each (-1 for the root)
+    const int goal = goal_whole >= 0 ? goal_whole : goal_part;
+    if (goal >= 0) {
+      for (int u = goal; u != root; u = es[via[u]]) { path.push_back(u); praw.push_back(er[via[u]]); }
+      path.push_back(root); praw.push_back(-1);
+      std::reverse(path.begin(), path.end());
+      std::reverse(praw.begin(), praw.end());
+    } else {
+      std::vector<int> seen((size_t)n2, -1);
+      int u = root, raw = -1;
+      for (;;) {
+        seen[u] = (int)path.size();
+        path.push_back(u);
+        praw.push_back(raw);
+        long long pick = -1;
+        for (long long k = off[u]; k < off[u + 1] && pick < 0; ++k)
+          if (wc[ed[byu[k]]] > 0) pick = byu[k];
+        if (pick < 0) { err = "counterexample walk left the fixpoint"; return HORA_E_CUDA; }
+        const int v = ed[pick];
+        if (seen[v] >= 0) { T.loop_to = seen[v]; T.loop_ord = er[pick]; break; }
+        u = v;
+        raw = er[pick];
+      }
+    }
+    // the phase-1 creation path of the root's source node
+    int src = -1;
+    HGB_CUDA(cudaMemcpyAsync(&src, S[1].npar.template as<int>() + root, 4, cudaMemcpyDeviceToHost, s));
+    HGB_CUDA(wait());
+    std::vector<int> pre, preraw;
+    std::vector<unsigned long long> prekey;
+    for (int u = src; u >= 0;) {
+      int par = -1, raw = -1;
+      unsigned long long k = 0;
+      HGB_CUDA(cudaMemcpyAsync(&par, S[0].npar.template as<int>() + u, 4, cudaMemcpyDeviceToHost, s));
+      HGB_CUDA(cudaMemcpyAsync(&raw, S[0].nraw.template as<int>() + u, 4, cudaMemcpyDeviceToHost, s));
+      HGB_CUDA(cudaMemcpyAsync(&k, S[0].nkey.template as<unsigned long long>() + u, 8, cudaMemcpyDeviceToHost, s));
+      HGB_CUDA(wait());
+      pre.push_back(u); preraw.push_back(raw); prekey.push_back(k);
+      if ((long long)pre.size() > S[0].ncap + 1) { err = "trace walk did not reach the initial state"; return HORA_E_CUDA; }
+      u = par;
+    }
+    std::reverse(pre.begin(), pre.end());
+    std::reverse(preraw.begin(), preraw.end());
+    std::reverse(prekey.begin(), prekey.end());
+    const HostNet& H = *nets[0];
+    const int np = H.nprocs, ni = H.nints;
+    const int n0 = (int)pre.size(), nsteps = n0 + (int)path.size();
+    T.nsteps = nsteps;
+    if (T.loop_to >= 0) T.loop_to += n0;
+    T.ords.assign(nsteps, -1);
+    T.locs.resize((size_t)nsteps * np);
+    T.ints.resize((size_t)nsteps * std::max(ni, 0));
+    T.zones.resize((size_t)nsteps * Z2);
+    auto fill_step = [&](int i, unsigned long long k, const int* dz) -> int {
+      HGB_CUDA(cudaMemcpyAsync(T.zones.data() + (size_t)i * Z2, dz, Z2 * 4, cudaMemcpyDeviceToHost, s));
+      const unsigned long long kk = k & ((1ull << inst_shift) - 1);
+      for (int p = 0; p < np; ++p) T.locs[(size_t)i * np + p] = (int)((kk >> H.kshift[p]) & ((1ull << H.kwidth[p]) - 1));
+      for (int v = 0; v < ni; ++v)
+        T.ints[(size_t)i * ni + v] = (int)((kk >> H.kshift[np + v]) & ((1ull << H.kwidth[np + v]) - 1)) + H.int_lo[v];
+      return HORA_OK;
+    };
+    int rc;
+    for (int i = 0; i < n0; ++i) {
+      T.ords[i] = i == 0 ? -1 : preraw[i];
+      if ((rc = fill_step(i, prekey[i], S[0].nzone.template as<int>() + (long long)pre[i] * Z2))) return rc;
+    }
+    for (size_t j = 0; j < path.size(); ++j) {
+      T.ords[n0 + j] = j == 0 ? -2 : praw[j];
+      if ((rc = fill_step(n0 + (int)j, key[path[j]], S[1].nzone.template as<int>() + (long long)path[j] * Z2))) return rc;
+    }
+    HGB_CUDA(wait());
+    d2h += (size_t)nsteps * (Z2 * 4 + 16);
     return HORA_OK;
   }
 
@@ -1304,6 +1431,7 @@ template <int D>
 int run_group(const std::vector<const HostNet*>& nets, std::vector<InstResult>& res, const RunOptions& o,
               std::string& err) {
   Engine<D> E(nets, o, err);
+  if (o.trace) *o.trace = Trace{};
   int rc = E.setup();
   if (rc) return rc;
   long long nf = 0;
@@ -1319,7 +1447,9 @@ int run_group(const std::vector<const HostNet*>& nets, std::vector<InstResult>& 
     E.finish(res, status, leadsto);
     return status;
   }
-  if (status == HORA_OK && o.trace && nets.size() == 1 && nets[0]->kind != HORA_Q_EG && (status = E.hit_trace())) {
+  // a forward search's goal; for leads-to, the early witness unless the sweep already left a trace
+  if (status == HORA_OK && o.trace && nets.size() == 1 && nets[0]->kind != HORA_Q_EG && o.trace->nsteps == 0 &&
+      (status = E.hit_trace())) {
     E.finish(res, status, leadsto);
     return status;
   }

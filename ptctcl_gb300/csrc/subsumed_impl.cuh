@@ -158,6 +158,9 @@ __global__ void __launch_bounds__(kBlock) k_incl_store(const NetView* nets, Inst
     st.ncol0[node * D + t.i] = z[0];
     if (t.i == 0) {
       st.nlevel[node] = level; st.ndead[node] = 0; st.ninst[node] = inst; st.nkey[node] = hk;
+      // the source node (for a root: the phase-1 node whose p-part it is) and the transition index,
+      // read by a counterexample trace
+      st.npar[node] = sc.pnode[s]; st.nraw[node] = sc.raw[s];
       sc.rank[s] = (int)node;
       const unsigned long long f = atomicAdd(&ctl->nfront, 1ull);
       out.key[f] = hk; out.node[f] = (int)node; out.rank[f] = 0; out.inst[f] = inst;

@@ -184,7 +184,9 @@ class QueryHandle:
         """The trace of the last run (hora_gb_trace): the witness of an E[] query (as
         exists_invariant_trace); for reach / deadlock / a leads-to violation found by the early
         witness, the counterexample path from the initial state to the goal, ords[i] the transition
-        index of step i. None when there is none."""
+        index of step i; for a leads-to violation found by the backward sweep, the path to a p-state,
+        the root cut from it (ords -2), then a path of the !q graph to a stop set or around a cycle
+        (loop_to, loop_ord). None when there is none."""
         net = self.net
         np_, ni, d2 = len(net.procs), len(net.ints), net.dim * net.dim
         n, lt, lo = ctypes.c_int32(0), ctypes.c_int32(0), ctypes.c_int32(0)

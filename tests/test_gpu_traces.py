@@ -71,7 +71,61 @@ def _disc_ok(pred, locs, ints):
 
 CASES = ([("c1", 1, s) for s in range(12)] + [("c2", 2, s) for s in (0, 3, 10, 23)] +
          [("c4", 4, s) for s in (0, 1, 2, 3, 4, 5, 8, 9, 12, 13, 14, 18, 19, 22, 23, 25, 26, 75)] +
-         [("c3", 3, s) for s in (0, 1, 13, 19, 20, 33)])
+         [("c3", 3, s) for s in (0, 1, 13, 19, 20, 33)] +
+         # violations decided by the backward sweep (no early witness)
+         [("c3", 3, s) for s in (14, 17, 23, 25, 37, 39)])
+
+
+def _check_sweep_trace(net, p, q, qm, tr):
+    """A leads-to counterexample found by the backward sweep: the passed-store path from the initial
+    state to a p-state (as for the forward routes), the root (ords -2) inside that state cut to p and
+    !q, then steps of the network restricted to !q -- each the oracle's restricted successor of the
+    step before by the recorded transition, inside the step's zone, outside q -- ending at a state
+    whose stop set is not empty or closing a cycle by a restricted successor inside the step it
+    returns to."""
+    ords = tr["ords"]
+    n = len(ords)
+    r = ords.index(-2)
+    assert r >= 1 and ords.count(-2) == 1 and ords[0] == -1
+    ok, l0, i0, z0 = pyoracle.initial_state(net, qm)
+    assert ok and np.array_equal(l0, tr["locs"][0]) and np.array_equal(i0, tr["ints"][0])
+    assert (tr["zones"][0] >= z0).all()
+    for i in range(1, r):
+        succ = pyoracle.successor_raw(net, tr["locs"][i - 1], tr["ints"][i - 1], tr["zones"][i - 1], ords[i], qm)
+        assert succ is not None, i
+        sl, si, sz = succ
+        assert np.array_equal(sl, tr["locs"][i]) and np.array_equal(si, tr["ints"][i]), i
+        assert (tr["zones"][i] >= sz).all(), i
+    # the root: the same discrete state, a p-state outside q's discrete part or cut by q's clock atom
+    assert np.array_equal(tr["locs"][r], tr["locs"][r - 1]) and np.array_equal(tr["ints"][r], tr["ints"][r - 1])
+    assert _disc_ok(p, tr["locs"][r], tr["ints"][r])
+    cut = pyoracle.Dbm(net.nclocks, tr["zones"][r - 1])
+    assert all(cut.constrain(i, j, v) for (i, j, v) in p.clk_cond)
+    in_q = _disc_ok(q, tr["locs"][r], tr["ints"][r])
+    assert not (in_q and not q.clk_cond)
+    for i in range(r, n):
+        if _disc_ok(q, tr["locs"][i], tr["ints"][i]):
+            # every valuation of a !q-graph zone lies outside q's clock atom
+            (a, b, v), = q.clk_cond
+            d = pyoracle.Dbm(net.nclocks, tr["zones"][i])
+            assert not d.constrain(a, b, v), i
+    for i in range(r + 1, n):
+        succ = pyoracle.lt_successor_raw(net, q, tr["locs"][i - 1], tr["ints"][i - 1], tr["zones"][i - 1], ords[i], qm)
+        assert succ is not None, i
+        sl, si, sz = succ
+        assert np.array_equal(sl, tr["locs"][i]) and np.array_equal(si, tr["ints"][i]), i
+        assert (tr["zones"][i] >= sz).all(), i
+    if tr["loop_to"] >= 0:
+        j = tr["loop_to"]
+        assert r <= j < n
+        succ = pyoracle.lt_successor_raw(net, q, tr["locs"][n - 1], tr["ints"][n - 1], tr["zones"][n - 1],
+                                         tr["loop_ord"], qm)
+        assert succ is not None
+        sl, si, sz = succ
+        assert np.array_equal(sl, tr["locs"][j]) and np.array_equal(si, tr["ints"][j])
+        assert (tr["zones"][j] >= sz).all()
+    else:
+        assert pyoracle.lt_stop(net, q, tr["locs"][n - 1], tr["ints"][n - 1], tr["zones"][n - 1], qm) > 0
 
 
 @pytest.mark.parametrize("name,cfg,seed", CASES, ids=[f"{n}-{s}" for n, _, s in CASES])
@@ -88,10 +142,11 @@ def test_counterexample_replays(name, cfg, seed):
     if not goal:
         assert tr is None
         return
-    if kind == Q_LEADSTO and tr is None:
-        pytest.skip("violation found by the backward sweep (no forward witness)")
     assert tr is not None
     qm = _qmask(net, p) if kind == Q_REACH else _qmask(net, p, q) if kind == Q_LEADSTO else _qmask(net)
+    if kind == Q_LEADSTO and -2 in tr["ords"]:
+        _check_sweep_trace(net, p, q, qm, tr)
+        return
     n = len(tr["ords"])
     assert tr["ords"][0] == -1 and tr["loop_to"] == -1
     ok, l0, i0, z0 = pyoracle.initial_state(net, qm)
