@@ -1,9 +1,23 @@
 // level_kernels_impl.cuh -- bodies of the level kernels. Included once per DBM dimension by the
 // generated translation units (dim_<D>.cu), which instantiate hgb::Level<D>.
 #pragma once
+#include <cooperative_groups.h>
+
 #include "level_kernels.cuh"
 
 namespace hgb {
+
+// One index from a shared counter for each calling thread. The threads of a warp that call it
+// together take theirs with one atomic: an atomic per successor or survivor on one counter
+// serialises in L2.
+__device__ __forceinline__ unsigned long long take_index(unsigned long long* counter) {
+  namespace cg = cooperative_groups;
+  cg::coalesced_group g = cg::coalesced_threads();
+  unsigned long long b = 0;
+  if (g.thread_rank() == 0) b = atomicAdd(counter, (unsigned long long)g.size());
+  return g.shfl(b, 0) + g.thread_rank();
+}
+
 
 constexpr int kBlock = 128;   // threads per block: 4 warps, each holding floor(32/D) tiles
 
@@ -138,7 +152,7 @@ __global__ void __launch_bounds__(kBlock) k_expand(const NetView* nets, InstStat
     bool hit = false;
     auto emit = [&](const int* tl, const int* ti, const int (&z)[D], int raw) {
       unsigned long long idx = 0;
-      if (t.i == 0) idx = atomicAdd(&ctl->nsucc, 1ull);
+      if (t.i == 0) idx = take_index(&ctl->nsucc);
       idx = t.shfl64(idx, 0);
       if ((long long)idx < sc.cap) {
         store_rows(t, z, sc.zone + (long long)idx * D * D);
@@ -188,6 +202,9 @@ __global__ void __launch_bounds__(kBlock, 8) k_probe(const NetView* nets, InstSt
   Tile<D> t;
   if (!make_tile(t, threadIdx.x & 31)) return;
   const int ishift = nets[0].inst_shift;
+  // the probe counters are summed per lane over the whole loop and added once per tile at the end:
+  // one global atomic per lane and successor on the same two counters serialised in L2
+  unsigned long long nprobe_sum = 0, nfull_sum = 0;
   for (long long s = tile_id<D>(); s < nsucc; s += tile_count<D>()) {
     const unsigned long long hk = sc.key[s];
     const int inst = (int)(hk >> ishift);
@@ -239,8 +256,8 @@ __global__ void __launch_bounds__(kBlock, 8) k_probe(const NetView* nets, InstSt
         killed = t.any(mine);
       }
     }
-    if (nprobe) atomicAdd(&ctl->probes, nprobe);
-    if (nfull) atomicAdd(&ctl->probe_full, nfull);
+    nprobe_sum += nprobe;
+    nfull_sum += nfull;
     if (t.i == 0) {
       if (killed) {
         sc.slot[s] = -1;
@@ -249,9 +266,19 @@ __global__ void __launch_bounds__(kBlock, 8) k_probe(const NetView* nets, InstSt
         if (r == 0) sc.touched[atomicAdd(&ctl->ntouched, 1ull)] = (int)slot;
         sc.slot[s] = (int)slot;
         sc.rank[s] = (int)r;
-        sc.surv[atomicAdd(&ctl->nsurv, 1ull)] = (int)s;
+        sc.surv[take_index(&ctl->nsurv)] = (int)s;
       }
     }
+  }
+  unsigned long long tp = 0, tf = 0;
+#pragma unroll
+  for (int l = 0; l < D; ++l) {
+    tp += t.shfl64(nprobe_sum, l);
+    tf += t.shfl64(nfull_sum, l);
+  }
+  if (t.i == 0) {
+    if (tp) atomicAdd(&ctl->probes, tp);
+    if (tf) atomicAdd(&ctl->probe_full, tf);
   }
 }
 
@@ -1209,7 +1236,7 @@ __device__ void merge_key_tile(const NetView* nets, const InstState& is, const S
     }
     // (5)
     long long node = 0;
-    if (t.i == 0) node = (long long)atomicAdd(&ctl->nnodes, 1ull);
+    if (t.i == 0) node = (long long)take_index(&ctl->nnodes);
     node = (long long)t.shfl64((unsigned long long)node, 0);
     store_rows(t, z, st.nzone + node * D * D);
     st.ncol0[node * D + t.i] = z[0];
@@ -1246,7 +1273,7 @@ __global__ void __launch_bounds__(kMergeBlock, 2) k_merge(const NetView* nets, I
   if (!in_tile) return;
   for (;;) {
     unsigned long long j = 0;
-    if (t.i == 0) j = atomicAdd(&ctl->light_next, 1ull);
+    if (t.i == 0) j = take_index(&ctl->light_next);
     j = t.shfl64(j, 0);
     if ((long long)j >= nlight) break;
     merge_key_tile<D>(nets, is, sc, st, out, ctl, sc.light[j], level, t);
@@ -1331,7 +1358,7 @@ __global__ void __launch_bounds__(kBlock) k_graph_probe(const NetView* nets, Ins
       } else {
         sc.slot[s] = result;
         if (result == -2) sc.rank[s] = (int)ref;
-        else sc.surv[atomicAdd(&ctl->nsurv, 1ull)] = (int)s;
+        else sc.surv[take_index(&ctl->nsurv)] = (int)s;
         // keys are counted once, by the successor that first inserts the discrete key
         bool ins = false;
         const long long ks = slot_find_insert(st, hk, &ins);
@@ -1355,7 +1382,7 @@ __global__ void __launch_bounds__(kBlock) k_graph_store(const NetView* nets, Ins
     const unsigned long long hk = sc.key[s];
     const int inst = (int)(hk >> ishift);
     long long node = 0;
-    if (t.i == 0) node = (long long)atomicAdd(&ctl->nnodes, 1ull);
+    if (t.i == 0) node = (long long)take_index(&ctl->nnodes);
     node = (long long)t.shfl64((unsigned long long)node, 0);
     int z[D];
     load_rows(t, z, sc.zone + (long long)s * D * D);
@@ -1389,7 +1416,7 @@ static __global__ void k_graph_edges(Succ sc, Front fr, Edges ed, Ctl* ctl, long
       const unsigned r = (unsigned)sc.rank[s];
       node = (r & kZRefSucc) ? sc.rank[r & ~kZRefSucc] : (int)r;
     }
-    const unsigned long long e = atomicAdd(&ctl->nedges, 1ull);
+    const unsigned long long e = take_index(&ctl->nedges);
     if ((long long)e < ed.cap) { ed.src[e] = fr.node[sc.parent[s]]; ed.dst[e] = node; ed.ord[e] = sc.ord[s]; }
     else atomicMax(&ctl->err, 4u);
   }

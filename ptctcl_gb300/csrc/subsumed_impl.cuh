@@ -27,6 +27,7 @@ __global__ void __launch_bounds__(kBlock) k_incl_probe(const NetView* nets, Inst
   Tile<D> t;
   if (!make_tile(t, threadIdx.x & 31)) return;
   const int ishift = nets[0].inst_shift;
+  unsigned long long nprobe_sum = 0;   // added once per tile at the end (one atomic per test serialises)
   for (long long s = tile_id<D>(); s < nsucc; s += tile_count<D>()) {
     const unsigned long long hk = sc.key[s];
     const int inst = (int)(hk >> ishift);
@@ -73,7 +74,7 @@ __global__ void __launch_bounds__(kBlock) k_incl_probe(const NetView* nets, Inst
         if (bal) cover = t.shfl(mine, __ffs(bal) - 1 - t.base);
       }
     }
-    if (nprobe) atomicAdd(&ctl->probes, nprobe);
+    nprobe_sum += nprobe;
     if (t.i == 0) {
       if (cover >= 0) {
         sc.slot[s] = -2;
@@ -83,10 +84,14 @@ __global__ void __launch_bounds__(kBlock) k_incl_probe(const NetView* nets, Inst
         if (r == 0) sc.touched[atomicAdd(&ctl->ntouched, 1ull)] = (int)slot;
         sc.slot[s] = (int)slot;
         sc.rank[s] = (int)r;
-        sc.surv[atomicAdd(&ctl->nsurv, 1ull)] = (int)s;
+        sc.surv[take_index(&ctl->nsurv)] = (int)s;
       }
     }
   }
+  unsigned long long tp = 0;
+#pragma unroll
+  for (int l = 0; l < D; ++l) tp += t.shfl64(nprobe_sum, l);
+  if (t.i == 0 && tp) atomicAdd(&ctl->probes, tp);
 }
 
 // One contiguous segment of survivors per touched key.
@@ -150,7 +155,7 @@ __global__ void __launch_bounds__(kBlock) k_incl_store(const NetView* nets, Inst
     const unsigned long long hk = sc.key[s];
     const int inst = (int)(hk >> ishift);
     long long node = 0;
-    if (t.i == 0) node = (long long)atomicAdd(&ctl->nnodes, 1ull);
+    if (t.i == 0) node = (long long)take_index(&ctl->nnodes);
     node = (long long)t.shfl64((unsigned long long)node, 0);
     int z[D];
     load_rows(t, z, sc.zone + (long long)s * D * D);
@@ -248,7 +253,7 @@ __global__ void __launch_bounds__(kBlock) k_incl_cover(Succ sc, Store st, Ctl* c
 static __global__ void k_incl_edges(Succ sc, Front fr, Edges ed, Ctl* ctl, long long nsucc) {
   for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < nsucc; s += (long long)gridDim.x * blockDim.x) {
     if (sc.slot[s] == -1) continue;
-    const unsigned long long e = atomicAdd(&ctl->nedges, 1ull);
+    const unsigned long long e = take_index(&ctl->nedges);
     if ((long long)e < ed.cap) {
       ed.src[e] = fr.node[sc.parent[s]]; ed.dst[e] = sc.rank[s]; ed.ord[e] = sc.ord[s]; ed.raw[e] = sc.raw[s];
     } else {
