@@ -106,6 +106,7 @@ struct Ctl {
   unsigned int stop_over;        // the stop-set arena overflowed (the pass re-runs with more)
   unsigned long long probe_full; // stored zones the probe read whole (column 0 did not decide)
   unsigned long long merge_live; // live zones of the keys the merge folded into, before each merge
+  unsigned long long nlong;      // successors whose key list is long, probed by a whole warp each
 };
 constexpr unsigned long long kCtlChunkBytes = 10 * 8 + 2 * 4;
 

@@ -141,7 +141,7 @@ struct Engine {
   DeviceNets dn;
   StoreBufs<D> S[2];
   DBuf skey, sparent, sord, sraw, sflag, spnode, sslot, srank, szone, ssurv, sseg, ssorted, stouched, sokh, sokl, sskh, sskl,
-      sheavy, slight;
+      sheavy, slight, slong;
   long long scap = 0;
   DBuf clist;
   long long ccap = 0;
@@ -209,7 +209,7 @@ struct Engine {
     sc.zone = szone.template as<int>(); sc.surv = ssurv.template as<int>(); sc.seg = sseg.template as<int>();
     sc.sorted = ssorted.template as<int>(); sc.touched = stouched.template as<int>(); sc.cap = scap;
     sc.okh = sokh.template as<unsigned long long>(); sc.okl = sokl.template as<unsigned long long>();
-    sc.heavy = sheavy.template as<int>(); sc.light = slight.template as<int>();
+    sc.heavy = sheavy.template as<int>(); sc.light = slight.template as<int>(); sc.longs = slong.template as<int>();
     sc.skh = sskh.template as<unsigned long long>(); sc.skl = sskl.template as<unsigned long long>();
     sc.clist = clist.template as<int>(); sc.ccap = ccap;
     sc.hv.n = hv_n.template as<int>(); sc.hv.a = hv_a.template as<int>();
@@ -270,7 +270,7 @@ struct Engine {
     HGB_CUDA(ssurv.alloc(cap * 4)); HGB_CUDA(sseg.alloc(cap * 4)); HGB_CUDA(ssorted.alloc(cap * 4));
     HGB_CUDA(stouched.alloc(cap * 4));
     HGB_CUDA(sokh.alloc(cap * 8)); HGB_CUDA(sokl.alloc(cap * 8));
-    HGB_CUDA(sheavy.alloc(cap * 4)); HGB_CUDA(slight.alloc(cap * 4));
+    HGB_CUDA(sheavy.alloc(cap * 4)); HGB_CUDA(slight.alloc(cap * 4)); HGB_CUDA(slong.alloc(cap * 4));
     HGB_CUDA(sskh.alloc(cap * 8)); HGB_CUDA(sskl.alloc(cap * 8));
     return HORA_OK;
   }
@@ -824,10 +824,12 @@ struct Engine {
     }
     // ---- probe
     if (nsucc > 0) {
+      HGB_CUDA(cudaMemsetAsync(&dctl()->nlong, 0, 8, s));
       kt.begin(s);
       Level<D>::probe(V, is, succ(), store(k), dctl(), nsucc, blocks, s);
-      kt.end(s, KT_PROBE);
-      ++launches;
+      Level<D>::probe_long(V, is, succ(), store(k), dctl(), blocks, s);   // reads the count on the device
+      kt.end(s, KT_PROBE, 2);
+      launches += 2;
       HGB_CUDA(cudaGetLastError());
     }
     if ((rc = read_ctl())) return rc;

@@ -86,6 +86,7 @@ struct Succ {                 // successors of the current level
   int* touched;               // touched slots
   int* heavy;                 // touched slots merged block-wide
   int* light;                 // touched slots merged by one tile
+  int* longs;                 // successors whose key list is long (the probe's warp-wide pass)
   unsigned long long* okh;    // canonical order key of each successor: parent's hash key ...
   unsigned long long* okl;    // ... then (parent's rank << 32) | emission ordinal
   unsigned long long* skh;    // the same keys gathered at the successor's segment position
@@ -133,6 +134,7 @@ struct Level {
   // expands the frontier entries of instances [i0, i1)
   static void expand(const NetView* nets, InstState is, Front fr, int nfront, const int* src_zone, Succ sc, Ctl* ctl,
                      int roots, int i0, int i1, int blocks, cudaStream_t s);
+  static void probe_long(const NetView* nets, InstState is, Succ sc, Store st, Ctl* ctl, int blocks, cudaStream_t s);
   static void probe(const NetView* nets, InstState is, Succ sc, Store st, Ctl* ctl, long long nsucc, int blocks,
                     cudaStream_t s);
   static void deadlock(const NetView* nets, InstState is, Succ sc, Ctl* ctl, long long n, int all, int blocks,

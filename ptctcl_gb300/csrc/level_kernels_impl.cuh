@@ -20,6 +20,7 @@ __device__ __forceinline__ unsigned long long take_index(unsigned long long* cou
 
 
 constexpr int kBlock = 128;   // threads per block: 4 warps, each holding floor(32/D) tiles
+constexpr int kLongList = 96; // a successor whose key has more live zones is probed by a whole warp
 
 template <int D>
 __device__ __forceinline__ long long tile_id() {
@@ -229,6 +230,11 @@ __global__ void __launch_bounds__(kBlock, 8) k_probe(const NetView* nets, InstSt
     slot = (long long)t.shfl64((unsigned long long)slot, 0);
     inserted = t.shfl(inserted, 0);
     if (slot < 0) { if (t.i == 0) { atomicMax(&ctl->err, 4u); sc.slot[s] = -1; } continue; }
+    if (!inserted && __ldg(st.klive + slot) > kLongList) {
+      // a long list: left to k_probe_long, whose warps test 32 list entries per round
+      if (t.i == 0) { sc.slot[s] = (int)slot; sc.longs[take_index(&ctl->nlong)] = (int)s; }
+      continue;
+    }
     bool killed = false;
     unsigned long long nprobe = 0, nfull = 0;
     if (!inserted) {
@@ -279,6 +285,84 @@ __global__ void __launch_bounds__(kBlock, 8) k_probe(const NetView* nets, InstSt
   if (t.i == 0) {
     if (tp) atomicAdd(&ctl->probes, tp);
     if (tf) atomicAdd(&ctl->probe_full, tf);
+  }
+}
+
+// The probe of the successors whose key has more than kLongList live zones, one warp each: the
+// warp's 32 lanes take 32 list entries per round (a tile takes D), so a long scan needs a third to a
+// sixteenth of the rounds and runs with every lane of the warp busy. Same decisions as k_probe: the
+// successor is dropped iff some live zone simulates it; survivors get their rank in the slot's
+// pending list. The count of such successors is read on the device (no host round trip).
+template <int D>
+__global__ void __launch_bounds__(kBlock) k_probe_long(const NetView* nets, InstState is, Succ sc, Store st, Ctl* ctl) {
+  const int lane = threadIdx.x & 31;
+  const long long nlong = (long long)*(volatile unsigned long long*)&ctl->nlong;
+  const long long nw = (long long)gridDim.x * (blockDim.x >> 5);
+  const int ishift = nets[0].inst_shift;
+  unsigned long long nprobe = 0, nfull = 0;
+  for (long long w = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < nlong; w += nw) {
+    const int s = sc.longs[w];
+    const unsigned long long hk = sc.key[s];
+    const int inst = (int)(hk >> ishift);
+    const NetView& N = nets[inst];
+    const long long slot = sc.slot[s];
+    int locs[kMaxProcs], ints[kMaxInts];
+    key_decode(N, key_part(hk, ishift), locs, ints);
+    // per-clock bounds: lane c < D computes clock c's (key_bounds' rule), then every lane takes all
+    int l = kAluNegInf, u = kAluNegInf;
+    if (lane == 0) {
+      l = u = 0;
+    } else if (lane < D) {
+      for (int p = 0; p < N.nprocs; ++p) {
+        const int gl = N.loc_base[p] + locs[p];
+        l = max(l, N.Lloc[gl * N.dim + lane]);
+        u = max(u, N.Uloc[gl * N.dim + lane]);
+      }
+      l = max(l, N.Lq[lane]);
+      u = max(u, N.Uq[lane]);
+    }
+    int Lall[D], U[D], zc0[D];
+    const int* zs = sc.zone + (long long)s * D * D;
+#pragma unroll
+    for (int x = 0; x < D; ++x) {
+      Lall[x] = __shfl_sync(0xffffffffu, l, x);
+      U[x] = __shfl_sync(0xffffffffu, u, x);
+      zc0[x] = __ldg(zs + x * D);
+    }
+    const int nl = __ldg(st.klive + slot);
+    const int* lst = st.arena + __ldg(st.kloff + slot);
+    bool killed = false;
+    for (int k0 = nl - 1; k0 >= 0 && !killed; k0 -= 32) {
+      const int k = k0 - lane;
+      bool mine = false;
+      if (k >= 0) {
+        ++nprobe;
+        const int m = __ldg(lst + k);
+        const bool col0_pass = !alu_col0_witness<D>(zc0, st.ncol0 + (long long)m * D, Lall);
+        nfull += col0_pass;
+        mine = col0_pass && alu_le_lane<D>(zs, st.nzone + (long long)m * D * D, Lall, U);
+      }
+      killed = __any_sync(0xffffffffu, mine);
+    }
+    if (lane == 0) {
+      if (killed) {
+        sc.slot[s] = -1;
+      } else {
+        const unsigned r = atomicAdd(&st.pend[slot], 1u);
+        if (r == 0) sc.touched[atomicAdd(&ctl->ntouched, 1ull)] = (int)slot;
+        sc.rank[s] = (int)r;
+        sc.surv[take_index(&ctl->nsurv)] = s;
+      }
+    }
+  }
+#pragma unroll
+  for (int o = 16; o; o >>= 1) {
+    nprobe += __shfl_xor_sync(0xffffffffu, nprobe, o);
+    nfull += __shfl_xor_sync(0xffffffffu, nfull, o);
+  }
+  if (lane == 0) {
+    if (nprobe) atomicAdd(&ctl->probes, nprobe);
+    if (nfull) atomicAdd(&ctl->probe_full, nfull);
   }
 }
 
@@ -1615,6 +1699,10 @@ void Level<D>::probe(const NetView* nets, InstState is, Succ sc, Store st, Ctl* 
                      cudaStream_t s) {
   constexpr int TPB = (kBlock / 32) * (32 / D);
   k_probe<D><<<grid_for(nsucc, TPB, blocks), kBlock, 0, s>>>(nets, is, sc, st, ctl, nsucc);
+}
+template <int D>
+void Level<D>::probe_long(const NetView* nets, InstState is, Succ sc, Store st, Ctl* ctl, int blocks, cudaStream_t s) {
+  k_probe_long<D><<<blocks, kBlock, 0, s>>>(nets, is, sc, st, ctl);
 }
 template <int D>
 void Level<D>::deadlock(const NetView* nets, InstState is, Succ sc, Ctl* ctl, long long n, int all, int blocks,
