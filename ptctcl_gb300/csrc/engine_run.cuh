@@ -826,7 +826,7 @@ struct Engine {
     if (nsucc > 0) {
       HGB_CUDA(cudaMemsetAsync(&dctl()->nlong, 0, 8, s));
       kt.begin(s);
-      Level<D>::probe(V, is, succ(), store(k), dctl(), nsucc, blocks, s);
+      Level<D>::probe(V, is, succ(), store(k), dctl(), nsucc, o.long_list, blocks, s);
       Level<D>::probe_long(V, is, succ(), store(k), dctl(), blocks, s);   // reads the count on the device
       kt.end(s, KT_PROBE, 2);
       launches += 2;

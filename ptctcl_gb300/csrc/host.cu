@@ -533,6 +533,7 @@ static RunOptions run_options(const volatile int32_t* cancel) {
     const long long b = std::atoll(e);
     if (b > 0) o.succ_budget_bytes = (size_t)b;
   }
+  if (const char* e = std::getenv("HORA_GB_LONG_LIST")) o.long_list = std::max(0, std::atoi(e));
   return o;
 }
 

@@ -130,6 +130,7 @@ struct RunOptions {
   Trace* trace = nullptr;     // E[] psi, one instance: fill with a witness when it holds
   bool yield_wait = false;    // wait for the stream on a blocking-sync event (the host thread sleeps
                               // instead of spinning): for groups that share the host's cores
+  int long_list = 4;          // the probe scans a key list longer than this with a whole warp
 };
 
 // Run a group of instances that share the DBM dimension D (one level-synchronous BFS over all of

@@ -135,7 +135,7 @@ struct Level {
   static void expand(const NetView* nets, InstState is, Front fr, int nfront, const int* src_zone, Succ sc, Ctl* ctl,
                      int roots, int i0, int i1, int blocks, cudaStream_t s);
   static void probe_long(const NetView* nets, InstState is, Succ sc, Store st, Ctl* ctl, int blocks, cudaStream_t s);
-  static void probe(const NetView* nets, InstState is, Succ sc, Store st, Ctl* ctl, long long nsucc, int blocks,
+  static void probe(const NetView* nets, InstState is, Succ sc, Store st, Ctl* ctl, long long nsucc, int long_list, int blocks,
                     cudaStream_t s);
   static void deadlock(const NetView* nets, InstState is, Succ sc, Ctl* ctl, long long n, int all, int blocks,
                        cudaStream_t s);

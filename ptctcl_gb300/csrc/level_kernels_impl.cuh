@@ -20,7 +20,6 @@ __device__ __forceinline__ unsigned long long take_index(unsigned long long* cou
 
 
 constexpr int kBlock = 128;   // threads per block: 4 warps, each holding floor(32/D) tiles
-constexpr int kLongList = 96; // a successor whose key has more live zones is probed by a whole warp
 
 template <int D>
 __device__ __forceinline__ long long tile_id() {
@@ -199,7 +198,7 @@ __global__ void __launch_bounds__(kBlock) k_expand(const NetView* nets, InstStat
 // extra resident warps hide more of that latency than the spills cost (19% faster on config 2).
 template <int D>
 __global__ void __launch_bounds__(kBlock, 8) k_probe(const NetView* nets, InstState is, Succ sc, Store st, Ctl* ctl,
-                                                  long long nsucc) {
+                                                  long long nsucc, int long_list) {
   Tile<D> t;
   if (!make_tile(t, threadIdx.x & 31)) return;
   const int ishift = nets[0].inst_shift;
@@ -230,7 +229,7 @@ __global__ void __launch_bounds__(kBlock, 8) k_probe(const NetView* nets, InstSt
     slot = (long long)t.shfl64((unsigned long long)slot, 0);
     inserted = t.shfl(inserted, 0);
     if (slot < 0) { if (t.i == 0) { atomicMax(&ctl->err, 4u); sc.slot[s] = -1; } continue; }
-    if (!inserted && __ldg(st.klive + slot) > kLongList) {
+    if (!inserted && __ldg(st.klive + slot) > long_list) {
       // a long list: left to k_probe_long, whose warps test 32 list entries per round
       if (t.i == 0) { sc.slot[s] = (int)slot; sc.longs[take_index(&ctl->nlong)] = (int)s; }
       continue;
@@ -288,7 +287,7 @@ __global__ void __launch_bounds__(kBlock, 8) k_probe(const NetView* nets, InstSt
   }
 }
 
-// The probe of the successors whose key has more than kLongList live zones, one warp each: the
+// The probe of the successors whose key has more than long_list live zones, one warp each: the
 // warp's 32 lanes take 32 list entries per round (a tile takes D), so a long scan needs a third to a
 // sixteenth of the rounds and runs with every lane of the warp busy. Same decisions as k_probe: the
 // successor is dropped iff some live zone simulates it; survivors get their rank in the slot's
@@ -1695,10 +1694,10 @@ void Level<D>::expand(const NetView* nets, InstState is, Front fr, int nfront, c
   k_expand<D><<<grid_for(nfront, TPB, blocks), kBlock, 0, s>>>(nets, is, fr, nfront, src_zone, sc, ctl, roots, i0, i1);
 }
 template <int D>
-void Level<D>::probe(const NetView* nets, InstState is, Succ sc, Store st, Ctl* ctl, long long nsucc, int blocks,
-                     cudaStream_t s) {
+void Level<D>::probe(const NetView* nets, InstState is, Succ sc, Store st, Ctl* ctl, long long nsucc, int long_list,
+                     int blocks, cudaStream_t s) {
   constexpr int TPB = (kBlock / 32) * (32 / D);
-  k_probe<D><<<grid_for(nsucc, TPB, blocks), kBlock, 0, s>>>(nets, is, sc, st, ctl, nsucc);
+  k_probe<D><<<grid_for(nsucc, TPB, blocks), kBlock, 0, s>>>(nets, is, sc, st, ctl, nsucc, long_list);
 }
 template <int D>
 void Level<D>::probe_long(const NetView* nets, InstState is, Succ sc, Store st, Ctl* ctl, int blocks, cudaStream_t s) {
