@@ -181,6 +181,17 @@ HORA_GB_API int32_t hora_gb_abi_version(void);
 /* Number of visible CUDA devices (0 when none); returns a status. */
 HORA_GB_API int32_t hora_gb_device_count(int32_t* count);
 
+/* Process-wide tuning per DBM dimension D = clocks + 1 (entry D of each array; ndims entries,
+ * at most 18). long_list[D]: the key-list length past which the passed-store probe scans a
+ * successor's key with a whole warp instead of one DBM tile; group_max[D]: the most instances of
+ * dimension D the batched form runs as one group; blocks_per_sm[D]: the grid of the level kernels,
+ * in blocks per SM. A negative or zero entry, or a null array, keeps the built-in default (4, 64,
+ * 16); each call replaces the whole table. No reference counterpart: like the reference's
+ * process-global options (include/hora/config.hpp:4-6), set it before queries run. Verdicts and
+ * counts do not depend on it. ptctcl_gb300/tuner.py measures the values on the device at hand. */
+HORA_GB_API int32_t hora_gb_set_tuning(const int32_t* long_list, const int32_t* group_max,
+                                       const int32_t* blocks_per_sm, int32_t ndims);
+
 /* ---- single-query entry points ---------------------------------------------------------------- */
 
 /* E<> target. On HORA_OK, *result = 1 iff a symbolic state matching target is reachable. */

@@ -20,7 +20,7 @@ EXPORTS = (
     "hora_gb_exists_invariant_trace", "hora_gb_expand",
     "hora_gb_has_deadlock",
     "hora_gb_batch_run", "hora_gb_server_create", "hora_gb_server_submit", "hora_gb_server_step",
-    "hora_gb_server_poll", "hora_gb_server_destroy", "hora_gb_server_set_limits", "hora_gb_has_deadlock_noalloc",
+    "hora_gb_server_poll", "hora_gb_server_destroy", "hora_gb_server_set_limits", "hora_gb_set_tuning", "hora_gb_has_deadlock_noalloc",
     "hora_gb_open", "hora_gb_run", "hora_gb_trace", "hora_gb_close",
 )
 
@@ -91,8 +91,39 @@ def load(build_if_missing: bool = True):
     L.hora_gb_server_poll.restype = I32
     L.hora_gb_server_destroy.argtypes = [VP]
     L.hora_gb_server_destroy.restype = I32
+    L.hora_gb_set_tuning.argtypes = [P32, P32, P32, I32]
+    L.hora_gb_set_tuning.restype = I32
     _lib = L
+    apply_tuning()
     return L
+
+
+TUNING_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuning.json")
+
+
+def set_tuning(table: dict):
+    """Install a per-dimension tuning table (hora_gb_set_tuning): {"long_list": {D: n}, "group_max":
+    {D: n}, "blocks_per_sm": {D: n}}, D the DBM dimension; missing entries keep the defaults."""
+    n = 18
+    arrs = []
+    for key in ("long_list", "group_max", "blocks_per_sm"):
+        a = np.full(n, -1, np.int32)
+        for d, v in (table.get(key) or {}).items():
+            if 0 <= int(d) < n:
+                a[int(d)] = int(v)
+        arrs.append(a)
+    check(load().hora_gb_set_tuning(p32(arrs[0]), p32(arrs[1]), p32(arrs[2]), n), "set_tuning")
+
+
+def apply_tuning(path: str = TUNING_PATH):
+    """The tuner's measured table, when one is installed beside the library (ptctcl_gb300/tuning.json);
+    without one, or with HORA_GB_TUNING=0, the built-in defaults."""
+    if os.environ.get("HORA_GB_TUNING", "1") == "0" or not os.path.exists(path):
+        set_tuning({})
+        return
+    import json
+    with open(path) as f:
+        set_tuning(json.load(f).get("choice", {}))
 
 
 def last_error() -> str:

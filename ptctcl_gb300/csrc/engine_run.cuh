@@ -529,7 +529,7 @@ struct Engine {
     int dev = 0, nsm = 0;
     HGB_CUDA(cudaGetDevice(&dev));
     HGB_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    blocks = o.blocks > 0 ? o.blocks : nsm * 16;
+    blocks = o.blocks > 0 ? o.blocks : nsm * std::max(1, o.blocks_per_sm);
     merge_blocks = nsm * std::max(1, Level<D>::merge_blocks_per_sm());
     int rc = upload_nets(nets, inst_shift, dn, err);
     if (rc) return rc;

@@ -457,8 +457,33 @@ int upload_nets(const std::vector<const HostNet*>& nets, int inst_shift, DeviceN
                                           std::string&);
 HGB_FOR_DIMS(HGB_DECL)
 
+// Per-dimension tuning (hora_gb_set_tuning): entry D holds the value for DBM dimension D, -1 the
+// built-in default. Process-wide, read when a group starts.
+struct Tuning {
+  int long_list[kMaxDim + 1];
+  int group_max[kMaxDim + 1];
+  int blocks_per_sm[kMaxDim + 1];
+};
+static Tuning default_tuning() {
+  Tuning t;
+  for (int d = 0; d <= kMaxDim; ++d) t.long_list[d] = t.group_max[d] = t.blocks_per_sm[d] = -1;
+  return t;
+}
+static Tuning g_tuning = default_tuning();
+static std::mutex g_tuning_mu;
+static Tuning tuning() {
+  std::lock_guard<std::mutex> g(g_tuning_mu);
+  return g_tuning;
+}
+
 static int dispatch_group(int dim, const std::vector<const HostNet*>& nets, std::vector<InstResult>& res,
-                          const RunOptions& o, std::string& err) {
+                          const RunOptions& o_in, std::string& err) {
+  RunOptions o = o_in;
+  if (dim >= 0 && dim <= kMaxDim) {
+    const Tuning t = tuning();
+    if (!o.long_list_env && t.long_list[dim] >= 0) o.long_list = t.long_list[dim];
+    if (t.blocks_per_sm[dim] > 0) o.blocks_per_sm = t.blocks_per_sm[dim];
+  }
   switch (dim) {
 #define HGB_CASE(D) case D: return run_group<D>(nets, res, o, err);
     HGB_FOR_DIMS(HGB_CASE)
@@ -533,7 +558,10 @@ static RunOptions run_options(const volatile int32_t* cancel) {
     const long long b = std::atoll(e);
     if (b > 0) o.succ_budget_bytes = (size_t)b;
   }
-  if (const char* e = std::getenv("HORA_GB_LONG_LIST")) o.long_list = std::max(0, std::atoi(e));
+  if (const char* e = std::getenv("HORA_GB_LONG_LIST")) {
+    o.long_list = std::max(0, std::atoi(e));
+    o.long_list_env = true;
+  }
   return o;
 }
 
@@ -551,6 +579,20 @@ static int32_t ensure_device() {
 }
 
 extern "C" {
+
+int32_t hora_gb_set_tuning(const int32_t* long_list, const int32_t* group_max, const int32_t* blocks_per_sm,
+                           int32_t ndims) {
+  g_last_error.clear();
+  if (ndims < 0 || ndims > kMaxDim + 1) return fail(HORA_E_INVALID, "ndims outside [0, 18]");
+  std::lock_guard<std::mutex> g(g_tuning_mu);
+  g_tuning = default_tuning();
+  for (int d = 0; d < ndims; ++d) {
+    if (long_list && long_list[d] >= 0) g_tuning.long_list[d] = long_list[d];
+    if (group_max && group_max[d] > 0) g_tuning.group_max[d] = group_max[d];
+    if (blocks_per_sm && blocks_per_sm[d] > 0) g_tuning.blocks_per_sm[d] = std::min(blocks_per_sm[d], 64);
+  }
+  return HORA_OK;
+}
 
 const char* hora_gb_last_error(void) { return g_last_error.c_str(); }
 int32_t hora_gb_abi_version(void) { return HORA_GB_ABI_VERSION; }
@@ -788,9 +830,12 @@ int32_t run_batch(int32_t n, const hora_net_desc* nets, const hora_query_desc* q
   // median time to verdict from 18 s to 1 s and raised throughput by 1.4x
   std::vector<std::pair<int, std::vector<int>>> groups;
   {
-    long long gmax = 64;
-    if (const char* e = std::getenv("HORA_GB_GROUP_MAX")) gmax = std::atoll(e);
+    long long gmax_env = -1;
+    if (const char* e = std::getenv("HORA_GB_GROUP_MAX")) gmax_env = std::atoll(e);
+    const Tuning tn = tuning();
     for (auto& kv : by_dim) {
+      const int dim = kv.first / 4;
+      const long long gmax = gmax_env >= 0 ? gmax_env : (tn.group_max[dim] > 0 ? tn.group_max[dim] : 64);
       if (gmax <= 0 || (long long)kv.second.size() <= gmax) { groups.emplace_back(kv.first, kv.second); continue; }
       for (size_t a = 0; a < kv.second.size(); a += (size_t)gmax)
         groups.emplace_back(kv.first, std::vector<int>(kv.second.begin() + a,

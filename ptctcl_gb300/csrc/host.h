@@ -131,6 +131,8 @@ struct RunOptions {
   bool yield_wait = false;    // wait for the stream on a blocking-sync event (the host thread sleeps
                               // instead of spinning): for groups that share the host's cores
   int long_list = 4;          // the probe scans a key list longer than this with a whole warp
+  bool long_list_env = false; // long_list came from the environment (it then overrides the tuning)
+  int blocks_per_sm = 16;     // grid of the level kernels: this many blocks per SM (when blocks is 0)
 };
 
 // Run a group of instances that share the DBM dimension D (one level-synchronous BFS over all of

@@ -59,6 +59,12 @@ def test_invalid_and_unsupported_inputs_are_rejected_without_a_device():
     assert rc == capi.E_NOT_SUPPORTED
     # the serving form's limits need a server
     assert lib.hora_gb_server_set_limits(None, 1 << 30, 4) == capi.E_INVALID
+    # the tuning table holds at most one entry per DBM dimension (0..17); it touches no device
+    assert lib.hora_gb_set_tuning(None, None, None, 19) == capi.E_INVALID
+    assert lib.hora_gb_set_tuning(None, None, None, 0) == capi.OK
+    capi.set_tuning({"long_list": {9: 0, "7": 16}, "group_max": {9: 32}, "blocks_per_sm": {9: 8}})
+    capi.set_tuning({})
+    capi.apply_tuning()
 
 
 @pytest.mark.skipif(capi.device_count() > 0, reason="needs a machine without a CUDA device")
@@ -108,3 +114,10 @@ def test_handle_run_without_a_device_is_an_error():
     with pytest.raises(capi.HoraError):
         h.run()
     h.close()
+
+
+def test_tuner_keeps_the_default_within_the_margin():
+    from ptctcl_gb300.tuner import pick
+    assert pick({0: 0.99, 4: 1.0, 16: 1.01}, 4, 0.03) == 4       # 1% faster: noise
+    assert pick({0: 0.90, 4: 1.0, 16: 1.01}, 4, 0.03) == 0       # 10% faster: taken
+    assert pick({8: 1.2, 16: 1.0, 32: 1.1}, 16, 0.03) == 16
