@@ -150,6 +150,8 @@ struct Engine {
   DBuf esrc, edst, eord, eraw;
   long long ecap = 0;
   int merge_blocks = 0;         // resident blocks of the merge kernel (it schedules keys itself)
+  int pass_blocks = 0;          // grid of the heavy keys' sort and relation passes (256-thread blocks)
+  bool merge_wide = false;      // a single query at D >= 9: the merge runs in 512-thread blocks
   DBuf hv_n, hv_a, hv_cb, hv_bm, hv_bounds, hv_pool, hv_prefix, hv_order;   // keys merged block-wide
   long long hv_cap = 0, pool_cap = 0, prefix_cap = 0;
   std::vector<int> h_hn, h_ha, h_order;
@@ -530,7 +532,9 @@ struct Engine {
     HGB_CUDA(cudaGetDevice(&dev));
     HGB_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     blocks = o.blocks > 0 ? o.blocks : nsm * std::max(1, o.blocks_per_sm);
-    merge_blocks = nsm * std::max(1, Level<D>::merge_blocks_per_sm());
+    merge_wide = ninst == 1 && Level<D>::merge_wide_pays();
+    merge_blocks = nsm * std::max(1, Level<D>::merge_blocks_per_sm(merge_wide));
+    pass_blocks = nsm * 2;
     int rc = upload_nets(nets, inst_shift, dn, err);
     if (rc) return rc;
     for (size_t k = 0; k < dn.blob_bytes.size(); ++k) h2d += dn.blob_bytes[k];
@@ -730,7 +734,7 @@ struct Engine {
     HGB_CUDA(cudaMemcpyAsync(hv_order.p, h_order.data(), nh * 4, cudaMemcpyHostToDevice, s));
     h2d += nh * 4;
     kt.begin(s);
-    Level<D>::heavy_prep(V, is, succ(), store(k), dctl(), nh, merge_blocks, hv_order.template as<int>(), s);
+    Level<D>::heavy_prep(V, is, succ(), store(k), dctl(), nh, pass_blocks, hv_order.template as<int>(), s);
     kt.end(s, KT_MERGE);
     ++launches;
     HGB_CUDA(cudaGetLastError());
@@ -755,7 +759,7 @@ struct Engine {
       HGB_CUDA(cudaMemcpyAsync(hv_prefix.p, h_prefix.data(), (nh + 1) * 8, cudaMemcpyHostToDevice, s));
       h2d += (nh + 1) * 8;
       kt.begin(s);
-      if (Level<D>::heavy_pairs(V, succ(), store(k), hv_prefix.template as<long long>(), nh, tot, merge_blocks * 4, s)) {
+      if (Level<D>::heavy_pairs(V, succ(), store(k), hv_prefix.template as<long long>(), nh, tot, pass_blocks * 4, s)) {
         err = "cannot size the relation pass's shared memory";
         return HORA_E_CUDA;
       }
@@ -860,7 +864,8 @@ struct Engine {
         kt.begin(s);
         Level<D>::group(succ(), store(k), dctl(), nsucc, ntouched, s);
         kt.end(s, KT_GROUP, 2);
-        Level<D>::merge(V, is, succ(), store(k), front(cur ^ 1), dctl(), ntouched, level, merge_blocks, nullptr, s);
+        Level<D>::merge(V, is, succ(), store(k), front(cur ^ 1), dctl(), ntouched, level, merge_blocks, merge_wide,
+                        nullptr, s);
         launches += 3;
         HGB_CUDA(cudaGetLastError());
       }
@@ -886,7 +891,7 @@ struct Engine {
       if ((rc = read_ctl())) return rc;
       if ((rc = heavy_relations(V, k))) return rc;
       kt.begin(s);
-      Level<D>::merge(V, is, succ(), store(k), front(cur ^ 1), dctl(), ntouched, level, merge_blocks,
+      Level<D>::merge(V, is, succ(), store(k), front(cur ^ 1), dctl(), ntouched, level, merge_blocks, merge_wide,
                       hctl.nheavy ? hv_order.template as<int>() : nullptr, s);
       kt.end(s, KT_MERGE);
       launches += 1;

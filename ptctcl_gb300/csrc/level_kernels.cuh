@@ -142,8 +142,9 @@ struct Level {
   static void group(Succ sc, Store st, Ctl* ctl, long long nsucc, long long ntouched, cudaStream_t s);
   // order: the heavy keys' merge order (largest first), or null for their index order
   static void merge(const NetView* nets, InstState is, Succ sc, Store st, Front out, Ctl* ctl, long long ntouched,
-                    int level, int blocks, const int* order, cudaStream_t s);
-  static int merge_blocks_per_sm();
+                    int level, int blocks, bool wide, const int* order, cudaStream_t s);
+  static int merge_blocks_per_sm(bool wide);
+  static bool merge_wide_pays();
   // keys merged block-wide: sort + gather + bounds, then their pairwise relations
   static void heavy_prep(const NetView* nets, InstState is, Succ sc, Store st, Ctl* ctl, long long nheavy,
                          int blocks, const int* order, cudaStream_t s);

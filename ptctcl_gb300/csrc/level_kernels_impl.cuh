@@ -454,6 +454,15 @@ static __global__ void k_seg_scatter(Succ sc, Store st, long long nsucc) {
 // key's chain is relinked through its live zones only.
 // ---------------------------------------------------------------------------------------------
 constexpr int kMergeBlock = 256;
+constexpr int kMergeBlockWide = 512;
+// A heavy key's fold tests its union window (kMergeScan candidates) and its open hulls on every tile
+// of its block at once. Where a 256-thread block holds fewer tiles than the window (D >= 9: 3 or
+// fewer tiles per warp), a single query's merge runs in blocks of 512 threads, one per SM, which
+// cover the window in one round (config 2, D = 9: the merge 0.37 s -> 0.32 s per query). At D <= 8
+// the 256-thread block already does, and twice the blocks keep twice the heavy keys folding (config
+// 3, D = 7: 512 threads made the merge 1.5x slower); the batched form keeps 256-thread blocks.
+template <int D>
+constexpr bool wide_fold_pays() { return (kMergeBlock / 32) * (32 / D) < kMergeScan; }
 
 // Z ≼_aLU Zp decided by one thread from whole matrices behind plain pointers (global or shared).
 template <int D>
@@ -1335,8 +1344,8 @@ __device__ void merge_key_tile(const NetView* nets, const InstState& is, const S
   t.sync();
 }
 
-template <int D>
-__global__ void __launch_bounds__(kMergeBlock, 2) k_merge(const NetView* nets, InstState is, Succ sc, Store st,
+template <int D, int NT>
+__global__ void __launch_bounds__(NT, kMergeBlockWide / NT) k_merge(const NetView* nets, InstState is, Succ sc, Store st,
                                                           Front out, Ctl* ctl, int level, const int* order) {
   __shared__ MergeShared<D> sh;
   Tile<D> t;
@@ -1734,16 +1743,33 @@ int Level<D>::heavy_pairs(const NetView* nets, Succ sc, Store st, const long lon
   return 0;
 }
 template <int D>
-int Level<D>::merge_blocks_per_sm() {
+bool Level<D>::merge_wide_pays() {
+  return wide_fold_pays<D>();
+}
+template <int D>
+int Level<D>::merge_blocks_per_sm(bool wide) {
   int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_merge<D>, kMergeBlock, 0) != cudaSuccess) n = 1;
+  cudaError_t e;
+  if constexpr (wide_fold_pays<D>()) {
+    e = wide ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_merge<D, kMergeBlockWide>, kMergeBlockWide, 0)
+             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_merge<D, kMergeBlock>, kMergeBlock, 0);
+  } else {
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_merge<D, kMergeBlock>, kMergeBlock, 0);
+  }
+  if (e != cudaSuccess) n = 1;
   return n;
 }
 template <int D>
 void Level<D>::merge(const NetView* nets, InstState is, Succ sc, Store st, Front out, Ctl* ctl, long long ntouched,
-                     int level, int blocks, const int* order, cudaStream_t s) {
+                     int level, int blocks, bool wide, const int* order, cudaStream_t s) {
   const long long g = ntouched < blocks ? ntouched : blocks;
-  k_merge<D><<<(int)(g > 0 ? g : 1), kMergeBlock, 0, s>>>(nets, is, sc, st, out, ctl, level, order);
+  if constexpr (wide_fold_pays<D>()) {
+    if (wide) {
+      k_merge<D, kMergeBlockWide><<<(int)(g > 0 ? g : 1), kMergeBlockWide, 0, s>>>(nets, is, sc, st, out, ctl, level, order);
+      return;
+    }
+  }
+  k_merge<D, kMergeBlock><<<(int)(g > 0 ? g : 1), kMergeBlock, 0, s>>>(nets, is, sc, st, out, ctl, level, order);
 }template <int D>
 void Level<D>::graph_probe(const NetView* nets, InstState is, Succ sc, Store st, ZTab zt, Ctl* ctl, long long nsucc,
                            int blocks, cudaStream_t s) {
