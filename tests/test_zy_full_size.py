@@ -2,8 +2,8 @@
 tests/golden/make_full_size.py because the oracle needs minutes per query: config 2 (A[] not
 deadlock, up to 1.45M stored zones and 20M successors) and config 3 (p --> q, violated by the early
 witness after up to 110M successors). A second run must reproduce every count (the merge order is
-canonical, not scheduling-dependent). Kept in the file collected last so that a failure here comes
-after every other test has run."""
+canonical, not scheduling-dependent). Collected near the end (only the allocation-free entry
+point's test comes after it), so that a failure here comes after the parity tests have run."""
 import json
 import os
 

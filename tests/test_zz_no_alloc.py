@@ -4,8 +4,7 @@ hora_gb_has_deadlock_noalloc takes device buffers the caller already owns and ke
 network in the library's static device array; it must give exactly the answers of the allocating
 entry point hora_gb_has_deadlock (integer results: exact equality), on two calls in a row (the
 array keeps the previous call's contents), and must refuse a network too large for the array.
-Kept in a file collected at the end (before only the full-size queries) so that a failure here
-comes after the parity tests have run.
+Kept in the file collected last, so that a failure here comes after every other test has run.
 """
 import ctypes
 
