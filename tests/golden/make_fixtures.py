@@ -218,6 +218,68 @@ def parse_conj(text, net: Network, negate: bool = False, allow_neg: bool = False
     return p
 
 
+def split_or(text: str):
+    """Top-level `||` / `or` terms of a formula body (parentheses respected), outer parentheses
+    around the whole body removed first."""
+    text = text.strip()
+    while text.startswith("(") and text.endswith(")"):
+        depth, whole = 0, True
+        for i, ch in enumerate(text):
+            depth += ch == "("
+            depth -= ch == ")"
+            if depth == 0 and i < len(text) - 1:
+                whole = False
+                break
+        if not whole:
+            break
+        text = text[1:-1].strip()
+    terms, depth, cur, i = [], 0, "", 0
+    while i < len(text):
+        ch = text[i]
+        if ch == "(":
+            depth += 1
+        elif ch == ")":
+            depth -= 1
+        if depth == 0 and text.startswith("||", i):
+            terms.append(cur); cur = ""; i += 2; continue
+        if depth == 0 and re.match(r"\bor\b", text[i:i + 3]) and (i == 0 or text[i - 1] == " "):
+            terms.append(cur); cur = ""; i += 2; continue
+        cur += ch
+        i += 1
+    terms.append(cur)
+    return [t.strip() for t in terms if t.strip()]
+
+
+def parse_formula_dnf(f: str, net: Network):
+    """A formula whose top-level operand is a disjunction, lowered to several engine queries the
+    binding combines: E<> (t1 || t2) = any E<> ti; A[] not (t1 || t2) = not any E<> ti;
+    (p1 || p2) --> q = all pi --> q; A<> (a1 || a2) with single-atom terms = not E[] (!a1 && !a2).
+    -> (terms [(kind, p, q)], combine "any" | "all", negate)."""
+    f = f.strip()
+    if f.startswith("E<>"):
+        return [(Q_REACH, parse_conj(t, net), Pred()) for t in split_or(f[3:])], "any", False
+    if f.startswith("A[]"):
+        body = f[3:].strip()
+        m = re.match(r"^(?:not|!)\s*\((.*)\)$", body)
+        if not m:
+            raise Unsupported("A[] form")
+        return [(Q_REACH, parse_conj(t, net), Pred()) for t in split_or(m.group(1))], "any", True
+    if f.startswith("A<>"):
+        terms = split_or(f[3:])
+        p = Pred()
+        for t in terms:
+            a = parse_conj(t, net, negate=True, allow_neg=True)
+            p.loc_req += a.loc_req; p.int_cond += a.int_cond; p.clk_cond += a.clk_cond
+        return [(Q_EG, p, Pred())], "any", True
+    if "-->" in f:
+        a, b = f.split("-->")
+        if "!" in b or "||" in b or re.search(r"\bor\b", b):
+            raise Unsupported("disjunctive or negated q")
+        q = parse_conj(b, net)
+        return [(Q_LEADSTO, parse_conj(t, net), q) for t in split_or(a)], "all", False
+    raise Unsupported("formula")
+
+
 def parse_formula(f: str, net: Network):
     """-> (kind, p, q, negate) where the verdict 'satisfied' = (engine result) xor negate."""
     f = f.strip()
@@ -258,7 +320,7 @@ def find_model(ref: str, name: str):
 def main(ref: str):
     out_models = os.path.join(HERE, "models")
     os.makedirs(out_models, exist_ok=True)
-    rows, skipped, nets = [], [], {}
+    rows, skipped, nets, dnf_rows = [], [], {}, []
     tables = sorted(f for f in os.listdir(os.path.join(ref, "tests/uppaal-differential")) if f.endswith(".txt"))
     for tab in tables:
         for line in open(os.path.join(ref, "tests/uppaal-differential", tab)):
@@ -279,6 +341,13 @@ def main(ref: str):
                 net = nets[key]
                 if net is None:
                     raise Unsupported("model not convertible")
+                if "||" in formula or re.search(r"\bor\b", formula):
+                    terms, combine, neg = parse_formula_dnf(formula, net)
+                    sat = v[0] == "SAT"
+                    dnf_rows.append({"model": key, "formula": formula, "table": tab, "combine": combine,
+                                     "terms": [query_to_json(k_, p_, q_) for k_, p_, q_ in terms],
+                                     "result": (not sat) if neg else sat})
+                    continue
                 kind, p, q, neg = parse_formula(formula, net)
             except (Unsupported, KeyError) as e:
                 skipped.append((tab, mname, formula, str(e)))
@@ -303,7 +372,16 @@ def main(ref: str):
             uniq.append(r)
     with open(os.path.join(HERE, "verdicts.json"), "w") as fh:
         json.dump(uniq, fh, indent=0)
-    print(f"{len(uniq)} verdict rows over {sum(1 for n in nets.values() if n)} models; skipped {len(skipped)}")
+    seen, duniq = set(), []
+    for r in dnf_rows:
+        k = (r["model"], r["formula"])
+        if k not in seen:
+            seen.add(k)
+            duniq.append(r)
+    with open(os.path.join(HERE, "verdicts_dnf.json"), "w") as fh:
+        json.dump(duniq, fh, indent=0)
+    print(f"{len(uniq)} verdict rows and {len(duniq)} disjunctive rows over {sum(1 for n in nets.values() if n)} "
+          f"models; skipped {len(skipped)}")
     for s in skipped:
         print("  skip", *s)
 

@@ -34,3 +34,13 @@ def toy_networks():
                              [Edge(0, 1, guard=[c_ge(1, 2)], resets=[1]),
                               Edge(1, 0, guard=[c_ge(1, 1)], resets=[1])], 0)], clock_names=["0", "x"])
     return ta, t2
+
+
+def verdict_rows_dnf():
+    """Rows whose formula has a top-level disjunction, lowered by the binding into several engine
+    queries: (model, formula, combine, [(kind, p, q)], result) -- the recorded verdict is any (E<>,
+    A<> as !E[]) or all (p --> q) of the terms' results (tests/golden/make_fixtures.py)."""
+    with open(os.path.join(GOLDEN, "verdicts_dnf.json")) as fh:
+        rows = json.load(fh)
+    return [(r["model"], r["formula"], r["combine"], [query_from_json(t) for t in r["terms"]], r["result"])
+            for r in rows]

@@ -15,7 +15,7 @@ from ptctcl_gb300 import engine
 from ptctcl_gb300.engine import Backend, ReachStats
 from ptctcl_gb300.generator import config_instance
 from ptctcl_gb300.model import Pred
-from golden_util import load_model, verdict_rows
+from golden_util import load_model, verdict_rows, verdict_rows_dnf
 from states import sample_states
 
 pytestmark = pytest.mark.gpu
@@ -212,3 +212,32 @@ def test_eg_batched_matches_single():
     verdicts, stats = engine.batch_run(items)
     for (m, f, k, p, q, res), v in zip(rows, verdicts):
         assert v == int(res), (m, f)
+
+
+DNF_ROWS = verdict_rows_dnf()
+
+
+@pytest.mark.parametrize("model,formula,combine,terms,result", DNF_ROWS, ids=[f"{r[0]}:{r[1]}" for r in DNF_ROWS])
+def test_reference_disjunctive_verdicts_gpu(model, formula, combine, terms, result):
+    """Formulas with a top-level disjunction, as the binding lowers them: one query per term
+    ((p1 || p2) --> q: every pi --> q must hold; A<> of single-atom terms: one E[] of their
+    negations), each term's verdict and counts equal to the oracle's (the grc4 rows, slow in the
+    oracle, are checked against the recorded verdict only)."""
+    net = load_model(model)
+    got = []
+    for (kind, p, q) in terms:
+        st = ReachStats()
+        if kind == 2:
+            v = engine.leads_to_clocks(net, p, q, Backend.Cuda, st)
+        elif kind == 3:
+            v = engine.exists_invariant_run(net, p, Backend.Cuda, st)
+        else:
+            v = engine.reachable_net(net, p, Backend.Cuda, st)
+        got.append(v)
+        if model != "grc4":
+            want, wst = (pyoracle.leads_to(net, p, q) if kind == 2 else pyoracle.exists_invariant(net, p)
+                         if kind == 3 else pyoracle.reachable_net(net, p))
+            assert v == want
+            for k in LT_COUNTS:
+                assert getattr(st, k) == wst[k], (k, getattr(st, k), wst[k])
+    assert (any(got) if combine == "any" else all(got)) == result, (formula, got)

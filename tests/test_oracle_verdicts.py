@@ -10,7 +10,7 @@ import pytest
 
 from oracle import pyoracle
 from ptctcl_gb300.model import Pred, c_le, c_ge, c_gt
-from golden_util import load_model, verdict_rows, toy_networks
+from golden_util import load_model, verdict_rows, verdict_rows_dnf, toy_networks
 
 
 def test_dbm_tests_reachability():
@@ -77,3 +77,25 @@ def test_reference_eg_verdicts(model, formula, kind, p, q, result):
     net = load_model(model)
     got, st = pyoracle.exists_invariant(net, p)
     assert got == result, (formula, st)
+
+
+# Disjunctive formulas, each term one oracle query: (p1 || p2) --> q holds iff every pi --> q holds;
+# A<> (a1 || a2) with single-atom terms is !E[] (!a1 && !a2), one term. The grc4 rows run on the GPU
+# tests and here only with HORA_SLOW_ORACLE=1.
+DNF_ROWS = [r for r in verdict_rows_dnf() if r[0] != "grc4" or os.environ.get("HORA_SLOW_ORACLE") == "1"]
+
+
+def oracle_term(net, kind, p, q):
+    if kind == 0:
+        return pyoracle.reachable_net(net, p)[0]
+    if kind == 2:
+        return pyoracle.leads_to(net, p, q)[0]
+    return pyoracle.exists_invariant(net, p)[0]
+
+
+@pytest.mark.parametrize("model,formula,combine,terms,result", DNF_ROWS,
+                         ids=[f"{r[0]}:{r[1]}" for r in DNF_ROWS])
+def test_reference_disjunctive_verdicts(model, formula, combine, terms, result):
+    net = load_model(model)
+    got = [oracle_term(net, k, p, q) for (k, p, q) in terms]
+    assert (any(got) if combine == "any" else all(got)) == result, (formula, got)
