@@ -50,3 +50,25 @@ def test_full_size_deadlock_query_matches_oracle(row):
     for k in KEYS:
         assert runs[0][k] == row[k], (k, runs[0][k], row[k])
     assert runs[1] == runs[0]
+
+
+SERVE_ROWS = [r for r in ROWS if r["config"] == 5]
+
+
+@pytest.mark.skipif(not SERVE_ROWS, reason="no serving requests in the fixture")
+def test_served_requests_match_oracle():
+    """Requests of the serving workload's sequence (config-3 instances at full size) submitted
+    together to the serving queue, so they overlap on the device: every verdict and count equals the
+    oracle's for the same request run alone."""
+    items = [config_instance(3, r["seed"]) for r in SERVE_ROWS]
+    with engine.Server(budget_bytes=32 << 30, max_inflight=8) as srv:
+        tickets = [srv.submit(*it) for it in items]
+        srv.drain(timeout=600)
+        got = [srv.poll(t) for t in tickets]
+    for row, g in zip(SERVE_ROWS, got):
+        assert g is not None, row["seed"]
+        v, st = g
+        assert st["status"] == 0, (row["seed"], st["status"])
+        assert bool(v) == row["holds"], row["seed"]
+        for k in KEYS:
+            assert st[k] == row[k], (row["seed"], k, st[k], row[k])
