@@ -122,8 +122,14 @@ def apply_tuning(path: str = TUNING_PATH):
         set_tuning({})
         return
     import json
-    with open(path) as f:
-        set_tuning(json.load(f).get("choice", {}))
+    import warnings
+    try:
+        with open(path) as f:
+            table = json.load(f).get("choice", {})
+        set_tuning(table)
+    except (OSError, ValueError, AttributeError, TypeError) as e:   # a damaged table: the defaults
+        warnings.warn(f"ignoring {path}: {e}")
+        set_tuning({})
 
 
 def last_error() -> str:

@@ -76,6 +76,7 @@ static void worker_main(hora_server* s) {
   cudaSetDevice(s->device);
   for (;;) {
     std::unique_ptr<Request> r;
+    uint64_t per_request = 0;
     {
       std::unique_lock<std::mutex> g(s->mu);
       s->cv.wait(g, [&] {
@@ -88,13 +89,14 @@ static void worker_main(hora_server* s) {
       r = std::move(s->queue.front());
       s->queue.pop_front();
       s->running.insert(r->ticket);
+      per_request = s->per_request;
     }
     int32_t verdict = -1;
     hora_stats st{};
     BudgetPool* grow = &s->pool;
-    if (s->per_request) {
+    if (per_request) {
       // growth past the reservation must fit both the request's limit and the server's pool
-      r->limit.cap = s->per_request > r->est_bytes ? s->per_request - r->est_bytes : 0;
+      r->limit.cap = per_request > r->est_bytes ? per_request - r->est_bytes : 0;
       r->limit.parent = &s->pool;
       grow = &r->limit;
     }
