@@ -791,11 +791,14 @@ __global__ void __launch_bounds__(kMergeBlock) k_heavy_pairs(const NetView* nets
         if (pairs_ss) {
           const bool ok = c < q;
           const bool dq = ok && alu_le_ptr<D>(A + r * P, B + lane * P, L, U);   // s_q ≼ s_c
-          const bool rq = ok && alu_le_ptr<D>(B + lane * P, A + r * P, L, U);   // s_c ≼ s_q
-          const unsigned bd = __ballot_sync(0xffffffffu, dq), br = __ballot_sync(0xffffffffu, rq);
-          if (lane == 0) {
-            if (bd) drop[q] = 1u;
-            if (br) rt[q * rtw + bj] = br;
+          const unsigned bd = __ballot_sync(0xffffffffu, dq);
+          if (bd) {
+            // s_q is dropped, so the fold never reads its retire row: the reverse tests are skipped
+            if (lane == 0) drop[q] = 1u;
+          } else {
+            const bool rq = ok && alu_le_ptr<D>(B + lane * P, A + r * P, L, U);   // s_c ≼ s_q
+            const unsigned br = __ballot_sync(0xffffffffu, rq);
+            if (lane == 0 && br) rt[q * rtw + bj] = br;
           }
         } else {
           const bool rq = c < a && alu_le_ptr<D>(B + lane * P, A + r * P, L, U);   // old zone c ≼ s_q
